@@ -1,0 +1,156 @@
+"""Generate the golden fixtures in this folder by running the UNMODIFIED reference.
+
+This script is the only place that imports the reference (cmtip) itself, from the
+read-only checkout at /root/reference; it runs in the development container only.
+Third-party modules the reference needs but that are absent here are replaced by
+stubs in ``sys.modules`` before import:
+
+* ``finufft``  -> ``oracle.nufft`` (FP64 ES-kernel NUFFT with finufft's signatures);
+* ``skopi``    -> ``quaternion2rot3d`` (cmtip/eval/geom.py:25-46 convention),
+                  ``get_uniform_quat`` / ``get_random_quat`` (seeded project generators);
+* ``np.infty`` -> ``np.inf`` (numpy 2 removed the alias; cmtip/phasing/phase.py:203).
+
+The package ``cmtip`` is registered without executing ``cmtip/__init__.py`` (which
+pulls in h5py/mrcfile/skopi-GPU drivers); only the hot-path submodules are loaded.
+Outputs: small ``.npz`` files holding inputs and the reference's outputs.
+
+Run:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = "/root/reference"
+sys.path.insert(0, REPO)
+
+from cmtip_gb300 import geometry  # noqa: E402
+from oracle import nufft as onufft  # noqa: E402
+
+
+def _install_stubs(rng_seed=1234):
+    np.infty = np.inf
+    sys.modules["finufft"] = onufft
+    sk = types.ModuleType("skopi")
+    sk.quaternion2rot3d = geometry.quaternion2rot3d
+    sk.get_uniform_quat = lambda n, avoid_symmetric=True: geometry.uniform_quaternions(n)
+    _rng = np.random.default_rng(rng_seed)
+    sk.get_random_quat = lambda n: geometry.random_quaternions(n, _rng)
+    sys.modules["skopi"] = sk
+    pkg = types.ModuleType("cmtip")
+    pkg.__path__ = [os.path.join(REF, "cmtip")]
+    sys.modules["cmtip"] = pkg
+
+
+def _load_reference():
+    _install_stubs()
+    import importlib
+    nufft = importlib.import_module("cmtip.nufft")
+    ac = importlib.import_module("cmtip.autocorrelation.autocorrelation")
+    al = importlib.import_module("cmtip.alignment.align")
+    return nufft, ac, al
+
+
+def synthetic_case(M, n_img, P, n_atoms, radius, seed):
+    """Seeded particle, AC, detector, orientations and FP64 intensities (small)."""
+    rng = np.random.default_rng(seed)
+    rho = geometry.gaussian_particle(M, n_atoms, radius, rng)
+    ac = geometry.autocorrelation_of(rho)
+    ppr, rext = geometry.ewald_detector(P)
+    rext = rext / 0.9
+    quats = geometry.random_quaternions(n_img, rng).astype(np.float32)
+    rot = np.array([np.linalg.inv(geometry.quaternion2rot3d(q)) for q in quats])
+    H, K, L = np.einsum("ijk,klm->jilm", rot, ppr)
+    x = [(a.astype(np.float32).ravel() / rext * np.pi).astype(np.float64) for a in (H, K, L)]
+    intens = onufft.type2(x[0], x[1], x[2], ac.astype(np.complex128), eps=1e-12, isign=-1).real
+    return dict(ac=ac.astype(np.float32), ppr=ppr, rext=np.float64(rext), quats=quats,
+                slices=intens.reshape(n_img, 1, -1).astype(np.float32))
+
+
+def main():
+    nufft, ref_ac, ref_al = _load_reference()
+    out = {}
+
+    # 1. NUFFT wrappers (forward/adjoint, support, recip-sym, /M^3) on random points.
+    rng = np.random.default_rng(7)
+    M = 15
+    N = 3000
+    H_, K_, L_ = [rng.uniform(-0.95 * np.pi, 0.95 * np.pi, N).astype(np.float32) for _ in range(3)]
+    ugrid = rng.standard_normal((M,) * 3).astype(np.float32)
+    support = (rng.random((M,) * 3) > 0.3).astype(np.float32)
+    nuvect = (rng.standard_normal(N) + 1j * rng.standard_normal(N)).astype(np.complex64)
+    fwd = nufft.forward_cpu(ugrid.copy(), H_, K_, L_, support, True)
+    adj = nufft.adjoint_cpu(nuvect, H_, K_, L_, M, True, support)
+    adj_c = nufft.adjoint_cpu(nuvect, H_, K_, L_, M, False, None)
+    np.savez_compressed(os.path.join(HERE, "nufft_wrappers.npz"), H=H_, K=K_, L=L_, ugrid=ugrid,
+                        support=support, nuvect=nuvect, forward=fwd, adjoint=adj, adjoint_complex=adj_c, M=M)
+    out["nufft_wrappers"] = (fwd.shape, adj.shape)
+
+    # 2. positions, antisupport, linops, CG on a small seeded reconstruction.
+    case = synthetic_case(M=21, n_img=12, P=8, n_atoms=20, radius=4.0, seed=11)
+    H, K, L = ref_ac.gen_nonuniform_positions(case["quats"], case["ppr"])
+    anti = {m: ref_ac.gen_F_antisupport(m) for m in (9, 21, 22)}
+    Mg = 21
+    Mtot = Mg ** 3
+    slices = case["slices"]
+    N = np.prod(slices.shape)  # numpy integer, as in autocorrelation.py:201 (makes rlambda float64)
+    Hf, Kf, Lf = H.astype(np.float32), K.astype(np.float32), L.astype(np.float32)
+    data = slices.flatten().astype(np.float32)
+    est = (case["ac"] + 0.05 * rng.standard_normal(case["ac"].shape)).astype(np.float32)
+    from scipy.ndimage import gaussian_filter
+    ac_support = (gaussian_filter(est, 0.5) > 1e-12).astype(np.float32)
+    x0 = (est * ac_support).flatten()
+    weights = np.ones(N, dtype=np.float32)
+    alambda, rlambda, flambda = 1, Mtot / N / 1000, 1e3
+    W, d = ref_ac.setup_linops(Hf, Kf, Lf, data, ac_support, weights, x0, Mg, Mtot, N, case["rext"],
+                               alambda, rlambda, flambda, use_gpu=False, use_recip_sym=True)
+    probe = rng.standard_normal((3, Mtot))
+    Wp = np.stack([W.matvec(p.astype(np.complex128)) for p in probe])
+    from scipy.sparse.linalg import cg
+    x10, _ = cg(W, d, x0=x0, maxiter=10, rtol=0.0)
+    ac_solved = ref_ac.solve_ac(1, case["ppr"], case["rext"], slices, Mg,
+                                orientations=case["quats"], ac_estimate=est.copy(), use_gpu=False)
+    ac_gen0 = ref_ac.solve_ac(0, case["ppr"], case["rext"], slices, Mg,
+                              orientations=case["quats"], ac_estimate=None, use_gpu=False)
+    np.savez_compressed(os.path.join(HERE, "autocorrelation.npz"),
+                        quats=case["quats"], ppr=case["ppr"], rext=case["rext"], slices=slices,
+                        ac_true=case["ac"], estimate=est, H=H, K=K, L=L,
+                        anti9=anti[9], anti21=anti[21], anti22=anti[22],
+                        ac_support=ac_support, x0=x0, d=d, probe=probe, W_probe=Wp,
+                        x_cg10=x10, ac_solved=ac_solved, ac_gen0=ac_gen0, M=Mg)
+    out["autocorrelation"] = (d.dtype, x10.dtype, ac_solved.dtype)
+
+    # 3. alignment: weights, slices, distances and the reference's own match test
+    #    (true orientations spliced into 100 refs, nbatches=2; cmtip/tests/test_align.py:44-61).
+    case = synthetic_case(M=21, n_img=3, P=8, n_atoms=20, radius=4.0, seed=21)
+    w0 = ref_al.generate_weights(case["ppr"], order=0)
+    w2 = ref_al.generate_weights(case["ppr"], order=-2)
+    w1 = ref_al.generate_weights(case["ppr"], order=1)
+    sl = ref_al.compute_slices(case["quats"], case["ppr"], case["rext"], case["ac"], use_gpu=False)
+    ref_q = geometry.uniform_quaternions(40).astype(np.float32)
+    model = ref_al.compute_slices(ref_q, case["ppr"], case["rext"], case["ac"]).reshape(40, -1)
+    data2 = case["slices"].reshape(3, -1)
+    dist = ref_al.calc_eudist(model * w2, data2 * w2)
+    np.random.seed(5)
+    matched = ref_al.match_orientations(0, case["ppr"], case["rext"], case["slices"], case["ac"], 100,
+                                        nbatches=2, order=0, use_gpu=False,
+                                        true_orientations=case["quats"])
+    np.random.seed(5)
+    ref_list = geometry.uniform_quaternions(100).astype(np.float32)
+    ref_list = np.vstack((ref_list[:-3], case["quats"]))
+    np.random.shuffle(ref_list)
+    np.savez_compressed(os.path.join(HERE, "alignment.npz"),
+                        quats=case["quats"], ppr=case["ppr"], rext=case["rext"], ac=case["ac"],
+                        slices=case["slices"], w0=w0, w2=w2, w1=w1, slices_model=sl,
+                        ref_q=ref_q, dist=dist, matched=matched, shuffled_refs=ref_list)
+    out["alignment"] = (matched.shape,)
+    print(out)
+
+
+if __name__ == "__main__":
+    main()

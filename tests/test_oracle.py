@@ -1,0 +1,130 @@
+"""The oracle pinned against the reference: golden fixtures made by running the
+unmodified cmtip code (tests/golden/make_golden.py), known-answer uniform-grid tests
+(the restatement of cmtip/tests/test_nufft.py:40-96 with a synthetic AC), and the
+fast FP64 NUFFT against exact direct sums."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from cmtip_gb300 import geometry
+from oracle import nufft as on
+from oracle import reference_port as rp
+
+
+def _uniform_points(M):
+    # cmtip/tests/test_nufft.py:31-36: pi * midpoints of linspace(-1, 1, M+1)
+    ls = np.linspace(-1, 1, M + 1)
+    ls = (ls[:-1] + ls[1:]) / 2
+    h, k, l = np.meshgrid(ls, ls, ls, indexing="ij")
+    return [(np.pi * a.ravel()).astype(np.float32) for a in (h, k, l)]
+
+
+@pytest.fixture(scope="module")
+def synthetic_ac():
+    rng = np.random.default_rng(3)
+    rho = geometry.gaussian_particle(25, 30, 5.0, rng)
+    ivol = np.abs(np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(rho)))) ** 2
+    ac = np.fft.fftshift(np.abs(np.fft.ifftn(ivol))).astype(np.float32)
+    return ivol.astype(np.float32), ac
+
+
+def test_forward_uniform_known_answer(synthetic_ac):
+    ivol, ac = synthetic_ac
+    M = ac.shape[0]
+    H, K, L = _uniform_points(M)
+    calc = rp.forward_cpu(ac.copy(), H, K, L, support=None, use_recip_sym=True).real
+    calc_np = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(ac)).real)
+    assert np.mean(np.abs(calc_np.ravel() - calc)) < 1e-4 * max(1.0, np.abs(calc_np).mean())
+
+
+def test_adjoint_uniform_known_answer():
+    # cmtip/tests/test_nufft.py:71-79: adjoint of ivol at uniform points /M^3 == |ifftn(ivol)| (shifted)
+    rng = np.random.default_rng(4)
+    M = 17
+    rho = geometry.gaussian_particle(M, 10, 3.0, rng)
+    F = np.fft.fftn(np.fft.ifftshift(rho))
+    ivol = np.fft.fftshift(np.abs(F) ** 2).astype(np.float32)
+    H, K, L = _uniform_points(M)
+    ac_np = np.fft.fftshift(np.fft.ifftn(np.fft.ifftshift(ivol)).real)
+    calc = rp.adjoint_cpu(ivol.ravel(), H, K, L, M)
+    assert np.mean(np.abs(ac_np - calc)) < 1e-4 * max(1.0, np.abs(ac_np).mean())
+
+
+@pytest.mark.parametrize("eps,tol", [(1e-6, 1e-5), (1e-12, 1e-11)])
+def test_fast_vs_direct(eps, tol):
+    rng = np.random.default_rng(0)
+    M, N = 13, 1500
+    x, y, z = [rng.uniform(-np.pi, np.pi, N) for _ in range(3)]
+    c = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    f = rng.standard_normal((M,) * 3) + 1j * rng.standard_normal((M,) * 3)
+    for isign in (-1, 1):
+        assert rel_l2(on.type1(x, y, z, c, M, eps=eps, isign=isign), on.nudft3d1(x, y, z, c, M, isign)) < tol
+        assert rel_l2(on.type2(x, y, z, f, eps=eps, isign=isign), on.nudft3d2(x, y, z, f, isign)) < tol
+
+
+def test_wrapped_points_even_modes():
+    rng = np.random.default_rng(1)
+    N = 800
+    x = rng.uniform(-2.9 * np.pi, 2.9 * np.pi, N)
+    y, z = [rng.uniform(-np.pi, np.pi, N) for _ in range(2)]
+    f = rng.standard_normal((16,) * 3) + 0j
+    assert rel_l2(on.type2(x, y, z, f), on.nudft3d2(x, y, z, f)) < 1e-10
+    c = rng.standard_normal(N) + 0j
+    assert rel_l2(on.type1(x, y, z, c, 16), on.nudft3d1(x, y, z, c, 16)) < 1e-10
+
+
+def test_nufft_wrappers_match_reference(golden):
+    g = golden("nufft_wrappers")
+    fwd = rp.forward_cpu(g["ugrid"].copy(), g["H"], g["K"], g["L"], g["support"], True)
+    assert rel_l2(fwd, g["forward"]) < 1e-6
+    adj = rp.adjoint_cpu(g["nuvect"], g["H"], g["K"], g["L"], int(g["M"]), True, g["support"])
+    assert rel_l2(adj, g["adjoint"]) < 1e-6
+    adjc = rp.adjoint_cpu(g["nuvect"], g["H"], g["K"], g["L"], int(g["M"]), False, None)
+    assert rel_l2(adjc, g["adjoint_complex"]) < 1e-6
+
+
+def test_positions_and_antisupport_match_reference(golden):
+    g = golden("autocorrelation")
+    H, K, L = rp.gen_nonuniform_positions(g["quats"], g["ppr"])
+    for a, b in ((H, g["H"]), (K, g["K"]), (L, g["L"])):
+        assert np.array_equal(a, b)
+    for m in (9, 21, 22):
+        assert np.array_equal(rp.gen_F_antisupport(m), g[f"anti{m}"])
+
+
+def test_linops_and_cg_match_reference(golden):
+    g = golden("autocorrelation")
+    M = int(g["M"])
+    s = rp.solve_ac_inputs(g["ppr"], g["slices"], M, g["quats"], g["estimate"].copy())
+    assert np.array_equal(s["ac_support"], g["ac_support"])
+    W, d, _ = rp.setup_linops(s["H"], s["K"], s["L"], s["data"], s["ac_support"], s["weights"], s["x0"],
+                              M, s["Mtot"], s["N"], g["rext"], s["alambda"], s["rlambda"], s["flambda"])
+    assert d.dtype == g["d"].dtype
+    assert rel_l2(d, g["d"]) < 1e-6
+    for p, wp in zip(g["probe"], g["W_probe"]):
+        assert rel_l2(W.matvec(p.astype(np.complex128)), wp) < 1e-6
+    from scipy.sparse.linalg import cg
+    x10, _ = cg(W, d, x0=s["x0"], maxiter=10, rtol=0.0)
+    assert rel_l2(x10, g["x_cg10"]) < 1e-6
+    ac, _ = rp.solve_ac(g["ppr"], g["rext"], g["slices"], M, g["quats"], g["estimate"].copy())
+    assert rel_l2(ac, g["ac_solved"]) < 1e-5
+    ac0, _ = rp.solve_ac(g["ppr"], g["rext"], g["slices"], M, g["quats"], None)
+    assert rel_l2(ac0, g["ac_gen0"]) < 1e-5
+
+
+def test_alignment_matches_reference(golden):
+    g = golden("alignment")
+    for order, key in ((0, "w0"), (-2, "w2"), (1, "w1")):
+        assert np.allclose(rp.generate_weights(g["ppr"], order), g[key], rtol=1e-12, atol=0)
+    sl = rp.compute_slices(g["quats"], g["ppr"], g["rext"], g["ac"])
+    assert rel_l2(sl, g["slices_model"]) < 1e-6
+    model = rp.compute_slices(g["ref_q"], g["ppr"], g["rext"], g["ac"]).reshape(len(g["ref_q"]), -1)
+    d = rp.calc_eudist(model * g["w2"], g["slices"].reshape(3, -1) * g["w2"])
+    assert np.allclose(d, g["dist"], rtol=1e-5)
+    rng = np.random.RandomState(5)
+    refs = rp.reference_orientations(100, nbatches=2, true_orientations=g["quats"],
+                                     ref_orientations=geometry.uniform_quaternions(100), shuffle_rng=rng)
+    assert np.array_equal(refs, g["shuffled_refs"])
+    q, idx = rp.match_orientations(g["ppr"], g["rext"], g["slices"], g["ac"], refs, nbatches=2)
+    assert np.array_equal(q, g["matched"])
+    assert np.array_equal(q, g["quats"])  # cmtip/tests/test_align.py:60: true orientations recovered
