@@ -1,0 +1,238 @@
+"""Autocorrelation solve on the GPU, mirroring ``cmtip.autocorrelation.autocorrelation``.
+
+``solve_ac`` keeps the reference's signature (``autocorrelation.py:176``) and behaviour:
+support from ``gaussian_filter(ac_estimate, 0.5) > 1e-12`` with the estimate masked in
+place (:217-220), ``alambda = 1``, ``rlambda = Mtot / N / 1000``, ``flambda = 1e3`` (:223-225),
+CG from ``x0 = ac_estimate`` with scipy's stopping rule and ``maxiter = 100`` (:226, :239),
+float64 ``(M, M, M)`` result of the real part (:240-243).  Extra keyword arguments select
+the precision (``prec=32``: FP32 vectors and NUFFT, FP64 inner products and step scalars;
+``prec=64``: the plain-FP64 GPU form), the data-term operator (``"toeplitz"`` as the
+reference, or ``"pair"``: the fused type-2 then type-1 NUFFT pair) and the NUFFT tolerance.
+
+``setup_linops`` returns ``(W, d)`` like the reference (:113-173); ``W`` is a scipy
+``LinearOperator`` whose matvec runs on the GPU (numpy in, numpy out) and which also
+exposes ``W.solver`` for device-resident use.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .nufft import DEFAULT_EPS, Plan, _ptr, _stream_ptr, inverse_rotations
+
+TOEPLITZ, PAIR = 0, 1
+
+
+def gen_F_antisupport(M):
+    """autocorrelation.py:66-85: ones where |q| > pi on linspace(-pi, pi, M)^3 (|q| to 4 dp)."""
+    lu = np.linspace(-np.pi, np.pi, M)
+    q2 = lu[:, None, None] ** 2 + lu[None, :, None] ** 2 + lu[None, None, :] ** 2
+    return np.around(np.sqrt(q2), 4) > np.pi
+
+
+def gen_nonuniform_positions(orientations, pixel_position_reciprocal, device="cuda"):
+    """autocorrelation.py:12-29 on the device: H, K, L = inv(R(q)) . ppr, float64 tensors of
+    shape (n_images, n_panels, n_pixels)."""
+    ppr = torch.as_tensor(np.asarray(pixel_position_reciprocal), device=device, dtype=torch.float64)
+    q = np.asarray(orientations)
+    if q.shape[0] > 0:
+        rot = inverse_rotations(q.astype(np.float32) if q.dtype != np.float32 else q, device=device)
+    else:
+        rot = torch.eye(3, dtype=torch.float64, device=device)[None]
+    hkl = torch.einsum("ijk,klm->jilm", rot, ppr)
+    return hkl[0], hkl[1], hkl[2]
+
+
+class CGSolver:
+    """Device CG solver of the reference's normal equations (``cmt_cg``)."""
+
+    def __init__(self, M, prec=32, op=TOEPLITZ, stream=None, device=None):
+        self.M, self.prec, self.op = int(M), int(prec), int(op)
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.dtype = torch.float64 if self.prec == 64 else torch.float32
+        with torch.cuda.device(self.device):
+            self.stream = stream if stream is not None else torch.cuda.current_stream()
+            h = ctypes.c_void_p()
+            _lib.call("cmt_cg_create", self.M, self.prec, self.op, _stream_ptr(self.stream), ctypes.byref(h))
+        self._h = h
+        self._keep = {}
+
+    def set_kernel(self, t_circ: torch.Tensor):
+        t = t_circ.to(self.device, self.dtype).contiguous()
+        with torch.cuda.device(self.device):
+            _lib.call("cmt_cg_set_kernel", self._h, _ptr(t))
+        self._keep["kernel"] = t
+
+    def set_operator(self, support, alambda, rlambda, flambda, mask_fft=None):
+        sup = torch.as_tensor(support, device=self.device).to(torch.float32).contiguous()
+        if mask_fft is None:
+            mask_fft = np.fft.ifftshift(gen_F_antisupport(self.M))
+        mask = torch.as_tensor(np.asarray(mask_fft, dtype=np.float32), device=self.device).contiguous()
+        with torch.cuda.device(self.device):
+            _lib.call("cmt_cg_set_operator", self._h, _ptr(mask), _ptr(sup), float(alambda), float(rlambda),
+                      float(flambda))
+        self._keep["support"], self._keep["mask"] = sup, mask
+
+    def set_pair_plan(self, plan: Plan):
+        with torch.cuda.device(self.device):
+            _lib.call("cmt_cg_set_pair_plan", self._h, plan._h)
+        self._keep["plan"] = plan
+
+    def matvec(self, x: torch.Tensor, out: torch.Tensor | None = None):
+        x = x.to(self.device, self.dtype).reshape(-1).contiguous()
+        out = out if out is not None else torch.empty_like(x)
+        with torch.cuda.device(self.device):
+            _lib.call("cmt_cg_matvec", self._h, _ptr(x), _ptr(out))
+        return out
+
+    def solve(self, d, x0, maxiter=100, rtol=1e-5, atol=0.0, use_graph=True):
+        d = d.to(self.device, self.dtype).reshape(-1).contiguous()
+        x = x0.to(self.device, self.dtype).reshape(-1).clone()
+        it, rho = ctypes.c_int(), ctypes.c_double()
+        with torch.cuda.device(self.device):
+            _lib.call("cmt_cg_solve", self._h, _ptr(d), _ptr(x), int(maxiter), float(rtol), float(atol),
+                      int(bool(use_graph)), ctypes.byref(it), ctypes.byref(rho))
+        return x, it.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.call("cmt_cg_destroy", self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def support_from_estimate(ac_estimate: torch.Tensor, inplace: bool = True):
+    """(gaussian_filter(est, 0.5) > 1e-12) as float32, est *= support (autocorrelation.py:217-220)."""
+    est = ac_estimate
+    M = est.shape[0]
+    sup = torch.empty_like(est)
+    scratch = torch.empty(2 * est.numel(), dtype=torch.float32, device=est.device)
+    with torch.cuda.device(est.device):
+        _lib.call("cmt_support_from_estimate", _ptr(est), M, _ptr(sup), _ptr(scratch), int(inplace), _stream_ptr())
+    return sup
+
+
+def toeplitz_kernel(plan_2M: Plan, M: int) -> torch.Tensor:
+    """Re(type-1 of ones onto 2M modes) / (2M)^3 in FFT order (autocorrelation.py:141-148)."""
+    M2 = 2 * M
+    return plan_2M.execute(None, scale=1.0 / float(M2) ** 3, real_out=True, fft_order=True)
+
+
+class _DeviceOperator:
+    """scipy-compatible W (numpy matvec) backed by a CGSolver."""
+
+    def __new__(cls, solver: CGSolver):
+        from scipy.sparse.linalg import LinearOperator
+        n = solver.M ** 3
+
+        def mv(u):
+            u = np.asarray(u)
+            if np.iscomplexobj(u):
+                u = u.real
+            y = solver.matvec(torch.from_numpy(np.ascontiguousarray(u)))
+            return y.cpu().numpy().astype(np.float64)
+
+        op = LinearOperator(dtype=np.complex64, shape=(n, n), matvec=mv)
+        op.solver = solver
+        return op
+
+
+def _as_device(a, dtype, device="cuda"):
+    t = a if torch.is_tensor(a) else torch.from_numpy(np.ascontiguousarray(a))
+    return t.to(device=device, dtype=dtype)
+
+
+def setup_linops(H, K, L, data, ac_support, weights, x0, M, Mtot, N, reciprocal_extent,
+                 alambda, rlambda, flambda, use_gpu=True, use_recip_sym=True, prec=32,
+                 operator="toeplitz", eps=DEFAULT_EPS):
+    """autocorrelation.py:113-173 on the GPU: returns (W, d) with d as float64 numpy (or a
+    device tensor when ``data`` is a CUDA tensor)."""
+    if not use_recip_sym:
+        raise NotImplementedError("the GPU solver implements the reference's use_recip_sym=True path")
+    numpy_io = not torch.is_tensor(data)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    rt = torch.float64 if prec == 64 else torch.float32
+    # H_ = H.flatten() / reciprocal_extent * pi (float64 when reciprocal_extent is a numpy float)
+    xs = [(_as_device(a, torch.float64).reshape(-1) / float(reciprocal_extent) * np.pi).to(rt) for a in (H, K, L)]
+    op = PAIR if operator == "pair" else TOEPLITZ
+    solver = CGSolver(M, prec=prec, op=op)
+    sup = _as_device(ac_support, torch.float32).reshape(-1)
+    solver.set_operator(sup, alambda, rlambda, flambda)
+    plan_M = Plan(1, M, eps=eps, isign=1, prec=prec).set_pts(*xs)
+    if op == TOEPLITZ:
+        plan_2M = Plan(1, 2 * M, eps=eps, isign=1, prec=prec).set_pts(*xs)
+        solver.set_kernel(toeplitz_kernel(plan_2M, M))
+        plan_2M.close()
+    else:
+        solver.set_pair_plan(plan_M)
+    db = _as_device(data, torch.float32).reshape(-1) * _as_device(weights, torch.float32).reshape(-1)
+    adb = plan_M.execute(db.to(rt), support=sup, scale=1.0 / float(M) ** 3, real_out=True).reshape(-1)
+    d = float(alambda) * adb.to(torch.float64) + float(rlambda) * _as_device(x0, torch.float64).reshape(-1)
+    W = _DeviceOperator(solver)
+    W.plan_M = plan_M
+    return W, (d.cpu().numpy() if numpy_io else d)
+
+
+def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, M, orientations=None,
+             ac_estimate=None, use_gpu=True, use_recip_sym=True, *, maxiter=100, rtol=1e-5, prec=32,
+             operator="toeplitz", eps=DEFAULT_EPS, use_graph=True, return_info=False, rng=None):
+    """autocorrelation.py:176-248 on the GPU.  Returns the float64 (M, M, M) autocorrelation
+    (numpy for numpy inputs, a CUDA tensor for tensor inputs); with ``return_info`` also a
+    dict with the iteration count."""
+    if not use_recip_sym:
+        raise NotImplementedError("the GPU solver implements the reference's use_recip_sym=True path")
+    numpy_io = not torch.is_tensor(slices_)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    Mtot = M ** 3
+    n_images = slices_.shape[0]
+    N = int(np.prod(slices_.shape))
+    if orientations is None:
+        from .geometry import random_quaternions
+        orientations = random_quaternions(n_images, rng or np.random.default_rng())
+    rt = torch.float64 if prec == 64 else torch.float32
+    ppr = _as_device(pixel_position_reciprocal, torch.float64).reshape(3, -1)
+    quats = orientations if torch.is_tensor(orientations) else np.asarray(orientations, dtype=np.float32)
+    inv_rot = inverse_rotations(quats, device=dev)
+    data = _as_device(slices_, torch.float32).reshape(-1)
+    if ac_estimate is None:
+        sup = torch.ones(Mtot, dtype=torch.float32, device=dev)
+        x0 = torch.zeros(Mtot, dtype=torch.float64, device=dev)
+    else:
+        if torch.is_tensor(ac_estimate):
+            est = ac_estimate.to(dev, torch.float32).contiguous()
+        else:
+            est = torch.from_numpy(np.ascontiguousarray(ac_estimate, dtype=np.float32)).to(dev)
+        sup = support_from_estimate(est, inplace=True).reshape(-1)
+        if isinstance(ac_estimate, np.ndarray) and ac_estimate.dtype == np.float32:
+            ac_estimate *= sup.reshape(ac_estimate.shape).cpu().numpy()  # the reference masks in place
+        x0 = est.reshape(-1).to(torch.float64)
+    alambda, rlambda, flambda = 1.0, Mtot / N / 1000, 1e3
+    op = PAIR if operator == "pair" else TOEPLITZ
+    solver = CGSolver(M, prec=prec, op=op)
+    solver.set_operator(sup, alambda, rlambda, flambda)
+    plan_M = Plan(1, M, eps=eps, isign=1, prec=prec)
+    plan_M.set_pts_quat(inv_rot, ppr, float(reciprocal_extent))
+    if op == TOEPLITZ:
+        plan_2M = Plan(1, 2 * M, eps=eps, isign=1, prec=prec)
+        plan_2M.set_pts_quat(inv_rot, ppr, float(reciprocal_extent))
+        solver.set_kernel(toeplitz_kernel(plan_2M, M))
+        plan_2M.close()
+    else:
+        solver.set_pair_plan(plan_M)
+    adb = plan_M.execute(data.to(rt), support=sup, scale=1.0 / float(M) ** 3, real_out=True).reshape(-1)
+    d = alambda * adb.to(torch.float64) + rlambda * x0
+    x, iters = solver.solve(d, x0, maxiter=maxiter, rtol=rtol, use_graph=use_graph)
+    ac = x.to(torch.float64).reshape((M,) * 3)
+    solver.close()
+    plan_M.close()
+    print(f"Recovered AC in {iters} iterations.", flush=True)
+    out = ac.cpu().numpy() if numpy_io else ac
+    return (out, {"iterations": iters}) if return_info else out

@@ -1,0 +1,675 @@
+// Conjugate-gradient autocorrelation solve on the device.
+//
+// Normal equations of cmtip/autocorrelation/autocorrelation.py:113-173 (setup_linops):
+//   W x = a * S . conv_{2M}(T, S x)        (Toeplitz data term, core_problem_convolution :32-63)
+//       + r * x                            (Tikhonov)
+//       + f * S . Re(IFFT(FFT(S x) . A))   (Fourier antisupport, fourier_reg :88-110)
+// with T = Re(type-1 of ones onto 2M modes) / (2M)^3 (:141-148).  The data term can instead
+// be applied as the explicit fused type-2 then type-1 pair on the points (cmt_execute_pair).
+// Both FFT convolutions use real-to-complex transforms: the operands are real and the
+// multipliers Hermitian, which is what the reference's .real projections compute.
+//
+// The iteration is scipy's cg (scipy/sparse/linalg/_isolve/iterative.py, called at
+// autocorrelation.py:239): no preconditioner, convergence test ||r|| < max(atol, rtol ||b||)
+// at the top of each iteration, r0 = b - W x0 only if x0 has a nonzero entry.  Vectors
+// live in the solver precision (float for the mixed form, double for the FP64 form);
+// every inner product, residual norm and the alpha/beta scalars are FP64.  One iteration
+// is a fixed launch sequence with no host synchronisation, so it is captured once into a
+// CUDA graph and replayed; a device-side flag turns the updates into no-ops after
+// convergence.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "cmt_common.cuh"
+
+namespace cmt {
+
+struct CgScalars {
+    double rho, rho_prev, pq, alpha, atol, bnorm;
+    int it, done;
+    unsigned ticket[4];
+};
+
+constexpr int RED_THREADS = 256;
+constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
+
+struct Cg {
+    int M = 0, prec = 32, op = 0;  // op 0 Toeplitz, 1 explicit pair
+    cudaStream_t stream = nullptr;
+    double alambda = 1, rlambda = 0, flambda = 0;
+    int64_t m3 = 0, m2 = 0;  // M^3, (2M)^3
+    // device buffers
+    void *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *b = nullptr;
+    void *sx = nullptr, *pad = nullptr, *conv = nullptr, *spec = nullptr, *spec2 = nullptr, *reg = nullptr;
+    void *kern_hat = nullptr;  // (2M)x(2M)x(M+1) complex: FFT of T / (2M)^3
+    void *mask_hat = nullptr;  // M x M x (M/2+1) real: Hermitian part of ifftshift(antisupport) / M^3
+    float *support = nullptr;  // M^3
+    double *partial = nullptr;
+    CgScalars *sc = nullptr;
+    cufftHandle r2c_big = 0, c2r_big = 0, r2c_small = 0, c2r_small = 0;
+    bool have_big = false, have_small = false;
+    cmt_plan *pair_plan = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    bool ready = false;
+};
+
+}  // namespace cmt
+
+struct cmt_cg : cmt::Cg {};
+
+namespace cmt {
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block partial of a sum; the last block to finish reduces all partials in a fixed
+// order (deterministic) and returns true in thread 0 with the total in *out.
+__device__ bool block_reduce_last(double v, double *partial, unsigned *ticket, double *out)
+{
+    __shared__ double s[RED_THREADS / 32];
+    __shared__ bool last;
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < RED_THREADS / 32 ? s[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+        if (threadIdx.x == 0) {
+            partial[blockIdx.x] = t;
+            __threadfence();
+            unsigned k = atomicAdd(ticket, 1u);
+            last = (k == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double t = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += ((volatile double *)partial)[i];
+    // fixed-order tree over the block
+    t = warp_sum(t);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int i = 0; i < RED_THREADS / 32; ++i) tot += s[i];
+        *out = tot;
+        *ticket = 0u;
+    }
+    return threadIdx.x == 0;
+}
+
+// dot(a, b) (or |a|^2) -> sc->field, plus optional companion sum of b^2 (for ||b||)
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_dot(const T *a, const T *b, int64_t n, double *partial,
+                                                     unsigned *ticket, double *out)
+{
+    double v = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v += (double)a[i] * (double)b[i];
+    block_reduce_last(v, partial, ticket, out);
+}
+
+// Start of an iteration: convergence test, p = r (+ beta p), S p into the padded corner
+// (Toeplitz) and into the M^3 buffer for the Fourier regulariser.
+template <typename T>
+__global__ void k_iter_begin(CgScalars *sc, const T *r, T *p, const float *support, int M, int use_pad, T *pad,
+                             T *sx)
+{
+    if (sc->done) return;
+    double rho = sc->rho;
+    if (sqrt(rho) < sc->atol) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
+        return;
+    }
+    int64_t m3 = (int64_t)M * M * M;
+    double beta = sc->it > 0 ? rho / sc->rho_prev : 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += (int64_t)gridDim.x * blockDim.x) {
+        T pv = sc->it > 0 ? (T)((double)r[i] + beta * (double)p[i]) : r[i];
+        p[i] = pv;
+        T v = pv * (T)support[i];
+        sx[i] = v;
+        if (use_pad) {
+            int64_t a = i / ((int64_t)M * M), rem = i - a * M * M, bb = rem / M, c = rem - bb * M;
+            int64_t M2 = 2 * M;
+            pad[(a * M2 + bb) * M2 + c] = v;
+        }
+    }
+}
+
+// S x for a given vector (matvec outside the iteration)
+template <typename T>
+__global__ void k_apply_support(const T *v, const float *support, int M, int use_pad, T *pad, T *sx)
+{
+    int64_t m3 = (int64_t)M * M * M;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += (int64_t)gridDim.x * blockDim.x) {
+        T s = v[i] * (T)support[i];
+        sx[i] = s;
+        if (use_pad) {
+            int64_t a = i / ((int64_t)M * M), rem = i - a * M * M, bb = rem / M, c = rem - bb * M;
+            int64_t M2 = 2 * M;
+            pad[(a * M2 + bb) * M2 + c] = s;
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_mul_complex(cplx_t<T> *a, const cplx_t<T> *b, int64_t n, const CgScalars *sc)
+{
+    if (sc && sc->done) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        cplx_t<T> u = a[i], v = b[i];
+        a[i] = {u.x * v.x - u.y * v.y, u.x * v.y + u.y * v.x};
+    }
+}
+
+template <typename T>
+__global__ void k_mul_real(cplx_t<T> *a, const T *m, int64_t n, const CgScalars *sc)
+{
+    if (sc && sc->done) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        cplx_t<T> u = a[i];
+        T s = m[i];
+        a[i] = {u.x * s, u.y * s};
+    }
+}
+
+// q = a S conv + r v + f S reg; conv read from the (2M)^3 corner (stride 2M) or an M^3 grid.
+// With dot: pq = v . q -> alpha = rho / pq.
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_combine(CgScalars *sc, const T *v, const T *conv, int conv_pad,
+                                                         const T *reg, const float *support, int M, double al,
+                                                         double rl, double fl, T *q, int with_dot, double *partial)
+{
+    if (with_dot && sc->done) return;
+    int64_t m3 = (int64_t)M * M * M;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += (int64_t)gridDim.x * blockDim.x) {
+        T cv;
+        if (conv_pad) {
+            int64_t a = i / ((int64_t)M * M), rem = i - a * M * M, bb = rem / M, c = rem - bb * M;
+            int64_t M2 = 2 * M;
+            cv = conv[(a * M2 + bb) * M2 + c];
+        } else {
+            cv = conv[i];
+        }
+        T s = (T)support[i];
+        T out = (T)al * s * cv + (T)rl * v[i] + (T)fl * s * reg[i];
+        q[i] = out;
+        acc += (double)v[i] * (double)out;
+    }
+    if (!with_dot) return;
+    double tot;
+    if (block_reduce_last(acc, partial, &sc->ticket[0], &tot)) {
+        sc->pq = tot;
+        sc->alpha = sc->rho / tot;
+    }
+}
+
+// x += alpha p ; r -= alpha q ; rho_new = r . r
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_update(CgScalars *sc, T *x, T *r, const T *p, const T *q, int M,
+                                                        double *partial)
+{
+    if (sc->done) return;
+    int64_t m3 = (int64_t)M * M * M;
+    double alpha = sc->alpha;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+        T rn = (T)((double)r[i] - alpha * (double)q[i]);
+        r[i] = rn;
+        acc += (double)rn * (double)rn;
+    }
+    double tot;
+    if (block_reduce_last(acc, partial, &sc->ticket[1], &tot)) {
+        sc->rho_prev = sc->rho;
+        sc->rho = tot;
+        sc->it += 1;
+    }
+}
+
+// r = b - q  (q = W x0)
+template <typename T>
+__global__ void k_residual(const T *b, const T *q, T *r, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = (T)((double)b[i] - (double)q[i]);
+}
+
+template <typename T>
+__global__ void k_scale(T *a, int64_t n, double s)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = (T)((double)a[i] * s);
+}
+
+// Hermitian part of a real M^3 multiplier in FFT order, stored as the R2C half (M x M x (M/2+1)),
+// times s.  For a real-even multiplier (odd M, symmetric antisupport) this is just the half.
+template <typename T>
+__global__ void k_mask_half(const float *m_fft, int M, double s, T *half)
+{
+    int hz = M / 2 + 1;
+    int64_t n = (int64_t)M * M * hz;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = (int)(i % hz);
+    int64_t r = i / hz;
+    int b = (int)(r % M), a = (int)(r / M);
+    int na = (M - a) % M, nb = (M - b) % M, nc = (M - c) % M;
+    double v = 0.5 * ((double)m_fft[((int64_t)a * M + b) * M + c] + (double)m_fft[((int64_t)na * M + nb) * M + nc]);
+    half[i] = (T)(v * s);
+}
+
+// scipy.ndimage.gaussian_filter(est, sigma=0.5) > 1e-12 (truncate 4 -> radius 2, mode
+// 'reflect'), one axis per pass with the float32 rounding of each pass, taps combined
+// symmetrically in float64 as ndimage's correlate1d does.
+__global__ void k_gauss_axis(const float *in, float *out, int M, int axis, double w0, double w1, double w2)
+{
+    int64_t m3 = (int64_t)M * M * M;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m3) return;
+    int64_t c[3] = {i / ((int64_t)M * M), (i / M) % M, i % M};
+    int64_t stride = axis == 0 ? (int64_t)M * M : (axis == 1 ? M : 1);
+    int64_t pos = c[axis];
+    auto refl = [&](int64_t k) -> int64_t {
+        // half-sample symmetric reflection: d c b a | a b c d | d c b a
+        int64_t period = 2 * M;
+        k %= period;
+        if (k < 0) k += period;
+        return k < M ? k : period - 1 - k;
+    };
+    const float *base = in + (i - pos * stride);
+    double v0 = base[pos * stride];
+    double a1 = (double)base[refl(pos - 1) * stride] + (double)base[refl(pos + 1) * stride];
+    double a2 = (double)base[refl(pos - 2) * stride] + (double)base[refl(pos + 2) * stride];
+    double t = v0 * w0;
+    t += a1 * w1;
+    t += a2 * w2;
+    out[i] = (float)t;
+}
+
+__global__ void k_threshold(const float *sm, float *support, float *est, int64_t n, double thr)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = sm[i] > thr ? 1.0f : 0.0f;
+    support[i] = s;
+    if (est) est[i] *= s;
+}
+
+// ---------------------------------------------------------------- host
+
+static size_t esz(const Cg &c) { return c.prec == 64 ? 8 : 4; }
+
+static int grid_elems(int64_t n) { return (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), 152 * 8); }
+
+template <typename T>
+static int matvec_impl(Cg &c, const T *v, T *out, bool in_iteration)
+{
+    cudaStream_t st = c.stream;
+    int M = c.M;
+    bool toe = c.op == 0;
+    int g = grid_elems(c.m3);
+    if (!in_iteration) {
+        k_apply_support<T><<<g, 256, 0, st>>>(v, c.support, M, toe, (T *)c.pad, (T *)c.sx);
+        CMT_LAUNCH_CHECK();
+    }
+    CgScalars *sc = in_iteration ? c.sc : nullptr;
+    int64_t hbig = (int64_t)(2 * M) * (2 * M) * (M + 1);
+    int64_t hsmall = (int64_t)M * M * (M / 2 + 1);
+    if (toe) {
+        if (c.prec == 64) {
+            CMT_TRY_CUFFT(cufftExecD2Z(c.r2c_big, (double *)c.pad, (cufftDoubleComplex *)c.spec));
+        } else {
+            CMT_TRY_CUFFT(cufftExecR2C(c.r2c_big, (float *)c.pad, (cufftComplex *)c.spec));
+        }
+        k_mul_complex<T><<<grid_elems(hbig), 256, 0, st>>>((cplx_t<T> *)c.spec, (const cplx_t<T> *)c.kern_hat, hbig, sc);
+        CMT_LAUNCH_CHECK();
+        if (c.prec == 64) {
+            CMT_TRY_CUFFT(cufftExecZ2D(c.c2r_big, (cufftDoubleComplex *)c.spec, (double *)c.conv));
+        } else {
+            CMT_TRY_CUFFT(cufftExecC2R(c.c2r_big, (cufftComplex *)c.spec, (float *)c.conv));
+        }
+    } else {
+        // explicit pair: conv = Re(A^H A (S v)) S / (2M)^3 on the M^3 grid
+        CMT_TRY(cmt_execute_pair(c.pair_plan, in_iteration ? c.p : v, c.conv, c.support,
+                                 1.0 / ((double)(2 * M) * (2 * M) * (2 * M))));
+    }
+    if (c.flambda != 0.0) {
+        if (c.prec == 64) {
+            CMT_TRY_CUFFT(cufftExecD2Z(c.r2c_small, (double *)c.sx, (cufftDoubleComplex *)c.spec2));
+        } else {
+            CMT_TRY_CUFFT(cufftExecR2C(c.r2c_small, (float *)c.sx, (cufftComplex *)c.spec2));
+        }
+        k_mul_real<T><<<grid_elems(hsmall), 256, 0, st>>>((cplx_t<T> *)c.spec2, (const T *)c.mask_hat, hsmall, sc);
+        CMT_LAUNCH_CHECK();
+        if (c.prec == 64) {
+            CMT_TRY_CUFFT(cufftExecZ2D(c.c2r_small, (cufftDoubleComplex *)c.spec2, (double *)c.reg));
+        } else {
+            CMT_TRY_CUFFT(cufftExecC2R(c.c2r_small, (cufftComplex *)c.spec2, (float *)c.reg));
+        }
+    } else {
+        CMT_TRY_CUDA(cudaMemsetAsync(c.reg, 0, esz(c) * c.m3, st));
+    }
+    // the pair already applied S and the 1/(2M)^3; the Toeplitz conv is unscaled (kern_hat holds it)
+    k_combine<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>(c.sc, in_iteration ? (const T *)c.p : v, (const T *)c.conv,
+                                                     toe ? 1 : 0, (const T *)c.reg, c.support, M, c.alambda,
+                                                     c.rlambda, c.flambda, out, in_iteration ? 1 : 0, c.partial);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+template <typename T>
+static int iteration(Cg &c)
+{
+    cudaStream_t st = c.stream;
+    int g = grid_elems(c.m3);
+    k_iter_begin<T><<<g, 256, 0, st>>>(c.sc, (const T *)c.r, (T *)c.p, c.support, c.M, c.op == 0, (T *)c.pad,
+                                       (T *)c.sx);
+    CMT_LAUNCH_CHECK();
+    CMT_TRY(matvec_impl<T>(c, (const T *)c.p, (T *)c.q, true));
+    k_update<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>(c.sc, (T *)c.x, (T *)c.r, (const T *)c.p, (const T *)c.q, c.M,
+                                                    c.partial);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+static void cg_destroy(Cg *c)
+{
+    if (!c) return;
+    void *bufs[] = {c->x, c->r, c->p, c->q, c->b, c->sx, c->pad, c->conv, c->spec, c->spec2, c->reg,
+                    c->kern_hat, c->mask_hat, c->support, c->partial, c->sc};
+    for (void *b : bufs) cudaFree(b);
+    if (c->have_big) {
+        cufftDestroy(c->r2c_big);
+        cufftDestroy(c->c2r_big);
+    }
+    if (c->have_small) {
+        cufftDestroy(c->r2c_small);
+        cufftDestroy(c->c2r_small);
+    }
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+}
+
+}  // namespace cmt
+
+using namespace cmt;
+
+extern "C" int cmt_cg_create(int M, int prec, int op, void *stream, cmt_cg **out)
+{
+    CMT_CHECK_ARG(out, "null output pointer");
+    *out = nullptr;
+    CMT_CHECK_ARG(M >= 2 && M <= 512, "M must be in [2, 512]");
+    CMT_CHECK_ARG(prec == 32 || prec == 64, "prec must be 32 or 64");
+    CMT_CHECK_ARG(op == 0 || op == 1, "op must be 0 (Toeplitz) or 1 (explicit pair)");
+    cmt_cg *c = new (std::nothrow) cmt_cg();
+    if (!c) return CMT_ERR_OOM;
+    c->M = M;
+    c->prec = prec;
+    c->op = op;
+    c->stream = (cudaStream_t)stream;
+    c->m3 = (int64_t)M * M * M;
+    c->m2 = (int64_t)(2 * M) * (2 * M) * (2 * M);
+    size_t e = esz(*c);
+    int64_t hbig = (int64_t)(2 * M) * (2 * M) * (M + 1), hsmall = (int64_t)M * M * (M / 2 + 1);
+    auto fail = [&](int code) {
+        cg_destroy(c);
+        delete c;
+        return code;
+    };
+    struct A {
+        void **p;
+        size_t n;
+    } allocs[] = {{&c->x, e * c->m3},       {&c->r, e * c->m3},         {&c->p, e * c->m3},
+                  {&c->q, e * c->m3},       {&c->b, e * c->m3},         {&c->sx, e * c->m3},
+                  {&c->reg, e * c->m3},     {&c->spec2, 2 * e * hsmall}, {&c->mask_hat, e * hsmall},
+                  {(void **)&c->support, (size_t)(4 * c->m3)}, {(void **)&c->partial, (size_t)8 * RED_BLOCKS},
+                  {(void **)&c->sc, sizeof(CgScalars)}};
+    for (auto &a : allocs) {
+        cudaError_t err = cudaMalloc(a.p, a.n);
+        if (err != cudaSuccess) {
+            set_error("cg allocation of %zu bytes: %s", a.n, cudaGetErrorString(err));
+            return fail(CMT_ERR_OOM);
+        }
+    }
+    if (op == 0) {
+        struct A big[] = {{&c->pad, e * c->m2}, {&c->conv, e * c->m2}, {&c->spec, 2 * e * hbig}, {&c->kern_hat, 2 * e * hbig}};
+        for (auto &a : big) {
+            cudaError_t err = cudaMalloc(a.p, a.n);
+            if (err != cudaSuccess) {
+                set_error("cg allocation of %zu bytes: %s", a.n, cudaGetErrorString(err));
+                return fail(CMT_ERR_OOM);
+            }
+        }
+        cudaMemset(c->pad, 0, e * c->m2);
+        int n2 = 2 * M;
+        if (cufftPlan3d(&c->r2c_big, n2, n2, n2, prec == 64 ? CUFFT_D2Z : CUFFT_R2C) != CUFFT_SUCCESS ||
+            cufftPlan3d(&c->c2r_big, n2, n2, n2, prec == 64 ? CUFFT_Z2D : CUFFT_C2R) != CUFFT_SUCCESS) {
+            set_error("cuFFT plan (2M)^3 failed");
+            return fail(CMT_ERR_CUFFT);
+        }
+        c->have_big = true;
+        cufftSetStream(c->r2c_big, c->stream);
+        cufftSetStream(c->c2r_big, c->stream);
+    } else {
+        cudaError_t err = cudaMalloc(&c->conv, e * c->m3);
+        if (err != cudaSuccess) return fail(CMT_ERR_OOM);
+    }
+    if (cufftPlan3d(&c->r2c_small, M, M, M, prec == 64 ? CUFFT_D2Z : CUFFT_R2C) != CUFFT_SUCCESS ||
+        cufftPlan3d(&c->c2r_small, M, M, M, prec == 64 ? CUFFT_Z2D : CUFFT_C2R) != CUFFT_SUCCESS) {
+        set_error("cuFFT plan M^3 failed");
+        return fail(CMT_ERR_CUFFT);
+    }
+    c->have_small = true;
+    cufftSetStream(c->r2c_small, c->stream);
+    cufftSetStream(c->c2r_small, c->stream);
+    cudaMemsetAsync(c->sc, 0, sizeof(CgScalars), c->stream);
+    *out = c;
+    return CMT_OK;
+}
+
+// Toeplitz kernel from its real circular (FFT-ordered) values T_circ on the (2M)^3 grid
+// (already divided by (2M)^3, the adjoint's scale, autocorrelation.py:141-147); stores
+// FFT(T_circ) / (2M)^3, the second factor being numpy's ifftn normalisation (:54).
+extern "C" int cmt_cg_set_kernel(cmt_cg *c, const void *t_circ)
+{
+    CMT_CHECK_ARG(c && t_circ, "null argument");
+    CMT_CHECK_ARG(c->op == 0, "the kernel belongs to the Toeplitz operator");
+    int64_t hbig = (int64_t)(2 * c->M) * (2 * c->M) * (c->M + 1);
+    if (c->prec == 64) {
+        CMT_TRY_CUFFT(cufftExecD2Z(c->r2c_big, (double *)t_circ, (cufftDoubleComplex *)c->kern_hat));
+        k_scale<double><<<grid_elems(2 * hbig), 256, 0, c->stream>>>((double *)c->kern_hat, 2 * hbig, 1.0 / c->m2);
+    } else {
+        CMT_TRY_CUFFT(cufftExecR2C(c->r2c_big, (float *)t_circ, (cufftComplex *)c->kern_hat));
+        k_scale<float><<<grid_elems(2 * hbig), 256, 0, c->stream>>>((float *)c->kern_hat, 2 * hbig, 1.0 / c->m2);
+    }
+    CMT_LAUNCH_CHECK();
+    c->ready = false;
+    return CMT_OK;
+}
+
+// Fourier-space multiplier of the regulariser: ifftshift(F_antisupport) as float M^3
+// (FFT order, autocorrelation.py:105), support S (M^3 float) and the three lambdas
+// (alambda, rlambda, flambda of autocorrelation.py:223-225).
+extern "C" int cmt_cg_set_operator(cmt_cg *c, const float *mask_fft, const float *support, double alambda,
+                                   double rlambda, double flambda)
+{
+    CMT_CHECK_ARG(c && support, "null argument");
+    CMT_CHECK_ARG(mask_fft || flambda == 0.0, "mask required when flambda != 0");
+    int M = c->M;
+    int64_t hsmall = (int64_t)M * M * (M / 2 + 1);
+    if (mask_fft) {
+        double s = 1.0 / (double)c->m3;  // numpy ifftn normalisation of fourier_reg (:106)
+        if (c->prec == 64)
+            k_mask_half<double><<<ceil_div(hsmall, 256), 256, 0, c->stream>>>(mask_fft, M, s, (double *)c->mask_hat);
+        else
+            k_mask_half<float><<<ceil_div(hsmall, 256), 256, 0, c->stream>>>(mask_fft, M, s, (float *)c->mask_hat);
+        CMT_LAUNCH_CHECK();
+    }
+    CMT_TRY_CUDA(cudaMemcpyAsync(c->support, support, 4 * c->m3, cudaMemcpyDeviceToDevice, c->stream));
+    c->alambda = alambda;
+    c->rlambda = rlambda;
+    c->flambda = flambda;
+    c->ready = false;
+    return CMT_OK;
+}
+
+// Explicit-pair data term: the plan (type 1, M modes, same precision) holds the points.
+extern "C" int cmt_cg_set_pair_plan(cmt_cg *c, cmt_plan *plan)
+{
+    CMT_CHECK_ARG(c && plan, "null argument");
+    CMT_CHECK_ARG(c->op == 1, "pair plan applies to the explicit-pair operator");
+    c->pair_plan = plan;
+    c->ready = false;
+    return CMT_OK;
+}
+
+// y = W x (solver precision vectors of M^3 elements)
+extern "C" int cmt_cg_matvec(cmt_cg *c, const void *x, void *y)
+{
+    CMT_CHECK_ARG(c && x && y, "null argument");
+    CMT_CHECK_ARG(c->op == 0 || c->pair_plan, "pair operator without a plan");
+    if (c->prec == 64) return matvec_impl<double>(*c, (const double *)x, (double *)y, false);
+    return matvec_impl<float>(*c, (const float *)x, (float *)y, false);
+}
+
+template <typename T>
+static int solve_impl(Cg &c, const T *d, T *x, int maxiter, double rtol, double atol, int use_graph, int *iters,
+                      double *final_rho)
+{
+    cudaStream_t st = c.stream;
+    size_t bytes = sizeof(T) * c.m3;
+    int g = grid_elems(c.m3);
+    CMT_TRY_CUDA(cudaMemsetAsync(c.sc, 0, sizeof(CgScalars), st));
+    CMT_TRY_CUDA(cudaMemcpyAsync(c.b, d, bytes, cudaMemcpyDeviceToDevice, st));
+    CMT_TRY_CUDA(cudaMemcpyAsync(c.x, x, bytes, cudaMemcpyDeviceToDevice, st));
+    // ||b||, x0.any()
+    CgScalars *sc = c.sc;
+    k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.b, (const T *)c.b, c.m3, c.partial, &sc->ticket[2],
+                                                 &sc->bnorm);
+    CMT_LAUNCH_CHECK();
+    double xx_host = 0.0;
+    {
+        k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.x, (const T *)c.x, c.m3, c.partial,
+                                                     &sc->ticket[3], &sc->pq);
+        CMT_LAUNCH_CHECK();
+        CgScalars h;
+        CMT_TRY_CUDA(cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st));
+        CMT_TRY_CUDA(cudaStreamSynchronize(st));
+        xx_host = h.pq;
+        double bnorm = sqrt(h.bnorm);
+        if (bnorm == 0.0) {  // scipy returns b itself
+            CMT_TRY_CUDA(cudaMemcpyAsync(x, c.b, bytes, cudaMemcpyDeviceToDevice, st));
+            if (iters) *iters = 0;
+            if (final_rho) *final_rho = 0.0;
+            return CMT_OK;
+        }
+        CgScalars init = h;
+        init.bnorm = bnorm;
+        init.atol = std::max(atol, rtol * bnorm);
+        init.it = 0;
+        init.done = 0;
+        init.pq = 0.0;
+        memset(init.ticket, 0, sizeof init.ticket);
+        CMT_TRY_CUDA(cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st));
+        CMT_TRY_CUDA(cudaStreamSynchronize(st));
+    }
+    if (xx_host != 0.0) {
+        CMT_TRY(matvec_impl<T>(c, (const T *)c.x, (T *)c.q, false));
+        k_residual<T><<<g, 256, 0, st>>>((const T *)c.b, (const T *)c.q, (T *)c.r, c.m3);
+    } else {
+        CMT_TRY_CUDA(cudaMemcpyAsync(c.r, c.b, bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.r, (const T *)c.r, c.m3, c.partial, &sc->ticket[2],
+                                                 &sc->rho);
+    CMT_LAUNCH_CHECK();
+    if (use_graph) {
+        if (!c.ready) {
+            if (c.graph) {
+                cudaGraphExecDestroy(c.graph);
+                c.graph = nullptr;
+            }
+            cudaGraph_t graph;
+            CMT_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = iteration<T>(c);
+            cudaError_t e = cudaStreamEndCapture(st, &graph);
+            if (rc != CMT_OK) return rc;
+            CMT_TRY_CUDA(e);
+            CMT_TRY_CUDA(cudaGraphInstantiate(&c.graph, graph, 0));
+            cudaGraphDestroy(graph);
+            c.ready = true;
+        }
+        for (int it = 0; it < maxiter; ++it) CMT_TRY_CUDA(cudaGraphLaunch(c.graph, st));
+    } else {
+        for (int it = 0; it < maxiter; ++it) CMT_TRY(iteration<T>(c));
+    }
+    CMT_TRY_CUDA(cudaMemcpyAsync(x, c.x, bytes, cudaMemcpyDeviceToDevice, st));
+    if (iters || final_rho) {
+        CgScalars h;
+        CMT_TRY_CUDA(cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st));
+        CMT_TRY_CUDA(cudaStreamSynchronize(st));
+        if (iters) *iters = h.it;
+        if (final_rho) *final_rho = h.rho;
+    }
+    return CMT_OK;
+}
+
+// Solve W x = d from x (in: x0, out: solution) with at most maxiter iterations,
+// scipy's stopping rule ||r|| < max(atol, rtol ||d||).  use_graph replays one captured
+// iteration (the first call captures; capture happens outside any user capture).
+extern "C" int cmt_cg_solve(cmt_cg *c, const void *d, void *x, int maxiter, double rtol, double atol, int use_graph,
+                            int *iters, double *final_rho)
+{
+    CMT_CHECK_ARG(c && d && x, "null argument");
+    CMT_CHECK_ARG(maxiter >= 0, "maxiter must be >= 0");
+    CMT_CHECK_ARG(c->op == 0 || c->pair_plan, "pair operator without a plan");
+    if (c->prec == 64)
+        return solve_impl<double>(*c, (const double *)d, (double *)x, maxiter, rtol, atol, use_graph, iters, final_rho);
+    return solve_impl<float>(*c, (const float *)d, (float *)x, maxiter, rtol, atol, use_graph, iters, final_rho);
+}
+
+extern "C" int cmt_cg_destroy(cmt_cg *c)
+{
+    if (!c) return CMT_OK;
+    cg_destroy(c);
+    delete c;
+    return CMT_OK;
+}
+
+// support = gaussian_filter(est, 0.5) > 1e-12 (float 0/1), est *= support in place when
+// est_inplace is non-zero (autocorrelation.py:217-220).  scratch: 2 M^3 floats.
+extern "C" int cmt_support_from_estimate(float *est, int M, float *support, float *scratch, int est_inplace,
+                                         void *stream)
+{
+    CMT_CHECK_ARG(est && support && scratch && M > 0, "bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    int64_t m3 = (int64_t)M * M * M;
+    // ndimage _gaussian_kernel1d(sigma=0.5, radius=2)
+    double w[3];
+    double sum = 0.0;
+    for (int k = 0; k <= 2; ++k) {
+        w[k] = exp(-0.5 / (0.5 * 0.5) * k * k);
+        sum += k == 0 ? w[k] : 2 * w[k];
+    }
+    double phi[5];
+    for (int k = -2; k <= 2; ++k) phi[k + 2] = exp(-0.5 / (0.5 * 0.5) * k * k);
+    double tot = 0.0;
+    for (double v : phi) tot += v;
+    for (int k = 0; k <= 2; ++k) w[k] = phi[k + 2] / tot;
+    (void)sum;
+    float *a = scratch, *b = scratch + m3;
+    unsigned gb = (unsigned)ceil_div(m3, 256);
+    k_gauss_axis<<<gb, 256, 0, st>>>(est, a, M, 0, w[0], w[1], w[2]);
+    k_gauss_axis<<<gb, 256, 0, st>>>(a, b, M, 1, w[0], w[1], w[2]);
+    k_gauss_axis<<<gb, 256, 0, st>>>(b, a, M, 2, w[0], w[1], w[2]);
+    k_threshold<<<gb, 256, 0, st>>>(a, support, est_inplace ? est : nullptr, m3, 1e-12);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}

@@ -1,0 +1,1198 @@
+// 3D type-1 / type-2 NUFFT for sm_103a with an exponential-of-semicircle kernel.
+//
+// Points are counting-sorted into cubic bins of the upsampled ("fine") grid once per
+// set_pts; the plan keeps, in bin order, each point's coordinates relative to its
+// bin origin (fine-grid units) and the permutation back to caller order.  Execution:
+//   type 1: spread   -> one CTA per subproblem (a bin or a <= maxsub slice of it)
+//                       accumulates into a shared-memory subgrid, then flushes it
+//                       once to the fine grid; cuFFT; deconvolve + crop (fused).
+//   type 2: deconvolve + zero-pad (fused, one pass over the fine grid); cuFFT;
+//                       interpolate from a shared-memory copy of the bin's subgrid.
+//   pair  : type 2 then type 1 on the same points with the interpolated value
+//           spread straight back from registers (no N-sized intermediate).
+// Real-valued strengths (type 1) and real-part outputs (type 2) use R2C / C2R
+// transforms on a real fine grid, halving spreading/interpolation work.
+//
+// The reference calls cufinufft/finufft for these transforms
+// (cmtip/nufft/forward.py:40,77-79; cmtip/nufft/adjoint.py:33,73-75).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "cmt_common.cuh"
+
+namespace cmt {
+
+static constexpr double kPi = 3.14159265358979323846;
+
+static thread_local char g_err[2048] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+// ------------------------------------------------------------------ host helpers
+
+// Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_n.
+static void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w)
+{
+    x.resize(n);
+    w.resize(n);
+    for (int i = 0; i < n; ++i) {
+        double z = cos(kPi * (i + 0.75) / (n + 0.5));
+        double dp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; ++k) {
+                double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+            double dz = p1 / dp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        x[i] = z;
+        w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+// psi_hat(xi) = int_{-w/2}^{w/2} phi(t) cos(xi t) dt
+static double kernel_ft(double xi, int w, double beta, const std::vector<double> &gx,
+                        const std::vector<double> &gw)
+{
+    double s = 0.0, half = 0.5 * w;
+    for (size_t i = 0; i < gx.size(); ++i) {
+        double t = 0.5 * half * (gx[i] + 1.0);  // [0, w/2]
+        double z = 2.0 * t / w;
+        double a = 1.0 - z * z;
+        double phi = a > 0 ? exp(beta * (sqrt(a) - 1.0)) : 0.0;
+        s += 0.5 * half * gw[i] * phi * cos(xi * t);
+    }
+    return 2.0 * s;
+}
+
+static int next_nice(int n)
+{
+    int m = std::max(n, 2);
+    for (;; ++m) {
+        if (m & 1) continue;
+        int r = m;
+        for (int p : {2, 3, 5, 7})
+            while (r % p == 0) r /= p;
+        if (r == 1) return m;
+    }
+}
+
+// ------------------------------------------------------------------ plan
+
+struct Plan {
+    int type = 1, prec = 32, M = 0, isign = 1;
+    double eps = 1e-6, sigma = 2.0;
+    int n = 0, w = 0, bs = 8, nb = 0, S = 0;  // fine size, width, bin size, bins/dim, subgrid size
+    double beta = 0.0;
+    int maxsub = 2048;
+    cudaStream_t stream = nullptr;
+
+    int64_t N = 0;
+    int64_t nsub = 0;
+    int *bin_count = nullptr, *bin_start = nullptr, *bin_fill = nullptr;
+    int *sub_bin = nullptr, *sub_off = nullptr;
+    int *perm = nullptr;
+    void *ux = nullptr, *uy = nullptr, *uz = nullptr;  // bin-relative sorted coordinates
+    int64_t cap_pts = 0, cap_sub = 0;
+    int *dflag = nullptr;      // device: range error flag, totals
+    long long *dtot = nullptr; // device: [total subproblems]
+
+    void *fine = nullptr;   // 2 n^3 elements of prec (complex n^3 or padded real)
+    void *fine2 = nullptr;  // second grid for the pair operator
+    void *deconv = nullptr; // |k| -> 1/psi_hat(k h), k = 0 .. M/2 + 1
+    cufftHandle fft_c2c = 0, fft_r2c = 0, fft_c2r = 0;
+    bool has_c2c = false, has_r2c = false, has_c2r = false;
+};
+
+}  // namespace cmt
+
+struct cmt_plan : cmt::Plan {};
+
+namespace cmt {
+
+// ------------------------------------------------------------------ device helpers
+
+// Split u (fine-grid units, any real) into the integer cell and the fraction.
+template <typename T>
+__device__ __forceinline__ void cell_and_frac(T x, T s_hi, T s_lo, int n, int &cell, T &frac)
+{
+    // u = x * (s_hi + s_lo) carried as p + lo with p = fl(x s_hi) and lo its exact error
+    T p = x * s_hi;
+    T lo = fma(x, s_hi, -p);
+    lo = fma(x, s_lo, lo);
+    T fp = floor(p);
+    T f = (p - fp) + lo;
+    int c = (int)fp;
+    if (f >= T(1)) { f -= T(1); c += 1; }
+    if (f < T(0)) { f += T(1); c -= 1; }
+    c %= n;
+    if (c < 0) c += n;
+    cell = c;
+    frac = f;
+}
+
+// Coordinates of point j.  MODE 0: arrays of the plan's precision; MODE 1: rotation.
+struct QuatSrc {
+    const double *inv_rot;
+    const double *ppr;
+    int64_t n_pix;
+    double rext;
+};
+
+template <typename T>
+__device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, const T *y, const T *z,
+                                             QuatSrc q, T &px, T &py, T &pz, bool &bad)
+{
+    if (mode == 0) {
+        px = x[j];
+        py = y[j];
+        pz = z[j];
+    } else {
+        // float32(inv(R) . p) / reciprocal_extent * pi, as in align.py:52-57 and
+        // autocorrelation.py:27,210 + setup_linops :133-135 (products not fused).
+        int64_t img = j / q.n_pix, pix = j - img * q.n_pix;
+        const double *R = q.inv_rot + 9 * img;
+        double p0 = q.ppr[pix], p1 = q.ppr[q.n_pix + pix], p2 = q.ppr[2 * q.n_pix + pix];
+        double h = __dadd_rn(__dadd_rn(__dmul_rn(R[0], p0), __dmul_rn(R[1], p1)), __dmul_rn(R[2], p2));
+        double k = __dadd_rn(__dadd_rn(__dmul_rn(R[3], p0), __dmul_rn(R[4], p1)), __dmul_rn(R[5], p2));
+        double l = __dadd_rn(__dadd_rn(__dmul_rn(R[6], p0), __dmul_rn(R[7], p1)), __dmul_rn(R[8], p2));
+        const double pi = 3.141592653589793;
+        double xh = __dmul_rn(__ddiv_rn((double)__double2float_rn(h), q.rext), pi);
+        double xk = __dmul_rn(__ddiv_rn((double)__double2float_rn(k), q.rext), pi);
+        double xl = __dmul_rn(__ddiv_rn((double)__double2float_rn(l), q.rext), pi);
+        px = (T)xh;
+        py = (T)xk;
+        pz = (T)xl;
+    }
+    const T lim = T(3.0 * 3.141592653589793);
+    bad = !(fabs(px) < lim && fabs(py) < lim && fabs(pz) < lim);
+}
+
+template <typename T>
+__device__ __forceinline__ int bin_of(T px, T py, T pz, T s_hi, T s_lo, int n, int bs, int nb, T &rx, T &ry,
+                                      T &rz)
+{
+    int cx, cy, cz;
+    T fx, fy, fz;
+    cell_and_frac(px, s_hi, s_lo, n, cx, fx);
+    cell_and_frac(py, s_hi, s_lo, n, cy, fy);
+    cell_and_frac(pz, s_hi, s_lo, n, cz, fz);
+    int bx = cx / bs, by = cy / bs, bz = cz / bs;
+    rx = T(cx - bx * bs) + fx;
+    ry = T(cy - by * bs) + fy;
+    rz = T(cz - bz * bs) + fz;
+    return (bx * nb + by) * nb + bz;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Pass 1: per-bin counts (warp-aggregated atomics), range check.
+template <typename T>
+__global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q, T s_hi, T s_lo,
+                            int n, int bs, int nb, int *count, int *flag)
+{
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t base = (int64_t)blockIdx.x * blockDim.x;
+    for (; base < N; base += stride) {
+        int64_t j = base + threadIdx.x;
+        int b = -1;
+        if (j < N) {
+            T px, py, pz, rx, ry, rz;
+            bool bad;
+            point_coords<T>(mode, j, x, y, z, q, px, py, pz, bad);
+            if (bad) {
+                atomicOr(flag, 1);
+            } else {
+                b = bin_of<T>(px, py, pz, s_hi, s_lo, n, bs, nb, rx, ry, rz);
+            }
+        }
+        unsigned peers = __match_any_sync(0xffffffffu, b);
+        int leader = __ffs(peers) - 1;
+        if (b >= 0 && (int)(threadIdx.x & 31) == leader) atomicAdd(&count[b], __popc(peers));
+    }
+}
+
+// Pass 2: scatter permutation and bin-relative coordinates into bin order.
+template <typename T>
+__global__ void k_bin_scatter(int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q, T s_hi,
+                              T s_lo, int n, int bs, int nb, const int *start, const int *count, int *fill,
+                              int *perm, T *ux, T *uy, T *uz, int *flag)
+{
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t base = (int64_t)blockIdx.x * blockDim.x;
+    for (; base < N; base += stride) {
+        int64_t j = base + threadIdx.x;
+        int b = -1;
+        T rx = 0, ry = 0, rz = 0;
+        if (j < N) {
+            T px, py, pz;
+            bool bad;
+            point_coords<T>(mode, j, x, y, z, q, px, py, pz, bad);
+            if (!bad) b = bin_of<T>(px, py, pz, s_hi, s_lo, n, bs, nb, rx, ry, rz);
+        }
+        unsigned peers = __match_any_sync(0xffffffffu, b);
+        int lane = threadIdx.x & 31;
+        int leader = __ffs(peers) - 1;
+        int off = 0;
+        if (b >= 0 && lane == leader) off = atomicAdd(&fill[b], __popc(peers));
+        off = __shfl_sync(peers, off, leader);
+        if (b >= 0) {
+            int rank = off + __popc(peers & lanemask_lt());
+            if (rank >= count[b]) {  // pass 1 and 2 disagree: never write out of the bin
+                atomicOr(flag, 2);
+                continue;
+            }
+            int pos = start[b] + rank;
+            perm[pos] = (int)j;
+            ux[pos] = rx;
+            uy[pos] = ry;
+            uz[pos] = rz;
+        }
+    }
+}
+
+// Exclusive scan of bin counts and of per-bin subproblem counts (one CTA).
+__global__ void k_scan_bins(int nbins, const int *count, int *start, int *sub_start, int maxsub, long long *tot)
+{
+    __shared__ long long s_pts[1024], s_sub[1024];
+    int t = threadIdx.x, T = blockDim.x;
+    int per = (nbins + T - 1) / T;
+    int lo = min(t * per, nbins), hi = min(lo + per, nbins);
+    long long a = 0, b = 0;
+    for (int i = lo; i < hi; ++i) {
+        a += count[i];
+        b += (count[i] + maxsub - 1) / maxsub;
+    }
+    s_pts[t] = a;
+    s_sub[t] = b;
+    __syncthreads();
+    for (int off = 1; off < T; off <<= 1) {
+        long long va = t >= off ? s_pts[t - off] : 0, vb = t >= off ? s_sub[t - off] : 0;
+        __syncthreads();
+        s_pts[t] += va;
+        s_sub[t] += vb;
+        __syncthreads();
+    }
+    long long ra = s_pts[t] - a, rb = s_sub[t] - b;
+    for (int i = lo; i < hi; ++i) {
+        start[i] = (int)ra;
+        sub_start[i] = (int)rb;
+        ra += count[i];
+        rb += (count[i] + maxsub - 1) / maxsub;
+    }
+    if (t == T - 1) {
+        tot[0] = s_sub[t];
+        tot[1] = s_pts[t];
+    }
+}
+
+__global__ void k_sub_list(int nbins, const int *count, const int *sub_start, int maxsub, int *sub_bin, int *sub_off)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbins) return;
+    int c = count[b];
+    int s0 = sub_start[b];
+    for (int s = 0; s * maxsub < c; ++s) {
+        sub_bin[s0 + s] = b;
+        sub_off[s0 + s] = s * maxsub;
+    }
+}
+
+// inv(R(q)) per quaternion: float32 element products (skopi, float32 quaternions),
+// inverse by the adjugate in float64.
+__global__ void k_inverse_rotations(const float *quat, int64_t n, double *out)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float w = quat[4 * i], x = quat[4 * i + 1], y = quat[4 * i + 2], z = quat[4 * i + 3];
+    float q01 = __fmul_rn(w, x), q02 = __fmul_rn(w, y), q03 = __fmul_rn(w, z);
+    float q11 = __fmul_rn(x, x), q12 = __fmul_rn(x, y), q13 = __fmul_rn(x, z);
+    float q22 = __fmul_rn(y, y), q23 = __fmul_rn(y, z), q33 = __fmul_rn(z, z);
+    double r[9];
+    r[0] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(q22, q33)));
+    r[1] = __fmul_rn(2.f, __fsub_rn(q12, q03));
+    r[2] = __fmul_rn(2.f, __fadd_rn(q13, q02));
+    r[3] = __fmul_rn(2.f, __fadd_rn(q12, q03));
+    r[4] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(q11, q33)));
+    r[5] = __fmul_rn(2.f, __fsub_rn(q23, q01));
+    r[6] = __fmul_rn(2.f, __fsub_rn(q13, q02));
+    r[7] = __fmul_rn(2.f, __fadd_rn(q23, q01));
+    r[8] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(q11, q22)));
+    double c00 = r[4] * r[8] - r[5] * r[7], c01 = r[5] * r[6] - r[3] * r[8], c02 = r[3] * r[7] - r[4] * r[6];
+    double det = r[0] * c00 + r[1] * c01 + r[2] * c02;
+    double id = 1.0 / det;
+    double *o = out + 9 * i;
+    o[0] = c00 * id;
+    o[1] = (r[2] * r[7] - r[1] * r[8]) * id;
+    o[2] = (r[1] * r[5] - r[2] * r[4]) * id;
+    o[3] = c01 * id;
+    o[4] = (r[0] * r[8] - r[2] * r[6]) * id;
+    o[5] = (r[2] * r[3] - r[0] * r[5]) * id;
+    o[6] = c02 * id;
+    o[7] = (r[1] * r[6] - r[0] * r[7]) * id;
+    o[8] = (r[0] * r[4] - r[1] * r[3]) * id;
+}
+
+// Kernel values phi((l0 + a) - u) for the w grid points of one dimension; returns the
+// window start relative to the bin origin (>= -floor(w/2)).
+template <typename T>
+__device__ __forceinline__ int kernel_vals(T u, int w, T beta, T *k)
+{
+    int l0 = (int)ceil(u - T(0.5) * T(w));
+    T inv = T(2) / T(w);
+#pragma unroll
+    for (int a = 0; a < MAXW; ++a) {
+        if (a < w) {
+            T t = (T(l0 + a) - u) * inv;
+            k[a] = es_eval(t * t, beta);
+        }
+    }
+    return l0;
+}
+
+template <typename T> struct Vec2Ops;
+
+// ------------------------------------------------------------------ spread (type 1)
+
+// One CTA per subproblem.  CPLX: complex strengths (interleaved), else real.
+// Fine grid: complex n^3 (CPLX) or real with row stride rs (in-place R2C layout).
+template <typename T, bool CPLX>
+__global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *sub_off, const int *bin_count,
+                                                const int *bin_start, const int *perm, const T *ux, const T *uy,
+                                                const T *uz, const T *c, const T *weight, int n, int rs, int bs,
+                                                int nb, int w, int S, T beta, int maxsub, T *fine)
+{
+    extern __shared__ unsigned char smem_raw[];
+    T *sg = reinterpret_cast<T *>(smem_raw);
+    const int nc = CPLX ? 2 : 1;
+    const int cells = S * S * S;
+    for (int i = threadIdx.x; i < cells * nc; i += blockDim.x) sg[i] = T(0);
+    __syncthreads();
+
+    int b = sub_bin[blockIdx.x];
+    int off = sub_off[blockIdx.x];
+    int cnt = min(maxsub, bin_count[b] - off);
+    int p0 = bin_start[b] + off;
+    const int h = w / 2;
+    const T tb = beta;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+        int pos = p0 + t;
+        int j = perm[pos];
+        T vr, vi = T(0);
+        if (CPLX) {
+            vr = c[2 * (int64_t)j];
+            vi = c[2 * (int64_t)j + 1];
+        } else {
+            vr = c ? c[j] : T(1);
+        }
+        if (weight) {
+            T wj = weight[j];
+            vr *= wj;
+            vi *= wj;
+        }
+        T kx[MAXW], ky[MAXW], kz[MAXW];
+        int lx = kernel_vals<T>(ux[pos], w, tb, kx) + h;
+        int ly = kernel_vals<T>(uy[pos], w, tb, ky) + h;
+        int lz = kernel_vals<T>(uz[pos], w, tb, kz) + h;
+        for (int a = 0; a < w; ++a) {
+            for (int bb = 0; bb < w; ++bb) {
+                T kab = kx[a] * ky[bb];
+                int row = ((lx + a) * S + (ly + bb)) * S + lz;
+                T ar = kab * vr, ai = kab * vi;
+#pragma unroll
+                for (int e = 0; e < MAXW; ++e) {
+                    if (e < w) {
+                        if (CPLX) {
+                            atomicAdd(&sg[2 * (row + e)], ar * kz[e]);
+                            atomicAdd(&sg[2 * (row + e) + 1], ai * kz[e]);
+                        } else {
+                            atomicAdd(&sg[row + e], ar * kz[e]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // flush: bin origin minus halo, periodic wrap
+    int bx = b / (nb * nb), by = (b / nb) % nb, bz = b % nb;
+    int ox = bx * bs - h, oy = by * bs - h, oz = bz * bs - h;
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+        int a = i / (S * S), r = i - a * S * S, bb = r / S, e = r - bb * S;
+        int gx = ox + a, gy = oy + bb, gz = oz + e;
+        gx += gx < 0 ? n : (gx >= n ? -n : 0);
+        gy += gy < 0 ? n : (gy >= n ? -n : 0);
+        gz += gz < 0 ? n : (gz >= n ? -n : 0);
+        if (CPLX) {
+            T vr = sg[2 * i], vi = sg[2 * i + 1];
+            if (vr != T(0) || vi != T(0)) {
+                int64_t g = ((int64_t)gx * n + gy) * n + gz;
+                atomicAdd(&fine[2 * g], vr);
+                atomicAdd(&fine[2 * g + 1], vi);
+            }
+        } else {
+            T v = sg[i];
+            if (v != T(0)) atomicAdd(&fine[((int64_t)gx * n + gy) * rs + gz], v);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ interp (type 2)
+
+// OUT: 0 complex values, 1 real part of complex grid, 2 real grid (values real)
+template <typename T, int OUT>
+__global__ void __launch_bounds__(256) k_interp(const int *sub_bin, const int *sub_off, const int *bin_count,
+                                                const int *bin_start, const int *perm, const T *ux, const T *uy,
+                                                const T *uz, const T *fine, int n, int rs, int bs, int nb, int w,
+                                                int S, T beta, int maxsub, T *out)
+{
+    extern __shared__ unsigned char smem_raw[];
+    T *sg = reinterpret_cast<T *>(smem_raw);
+    const bool cgrid = OUT != 2;
+    const int cells = S * S * S;
+    int b = sub_bin[blockIdx.x];
+    int bx = b / (nb * nb), by = (b / nb) % nb, bz = b % nb;
+    const int h = w / 2;
+    int ox = bx * bs - h, oy = by * bs - h, oz = bz * bs - h;
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+        int a = i / (S * S), r = i - a * S * S, bb = r / S, e = r - bb * S;
+        int gx = ox + a, gy = oy + bb, gz = oz + e;
+        gx += gx < 0 ? n : (gx >= n ? -n : 0);
+        gy += gy < 0 ? n : (gy >= n ? -n : 0);
+        gz += gz < 0 ? n : (gz >= n ? -n : 0);
+        if (cgrid) {
+            int64_t g = ((int64_t)gx * n + gy) * n + gz;
+            sg[2 * i] = fine[2 * g];
+            sg[2 * i + 1] = fine[2 * g + 1];
+        } else {
+            sg[i] = fine[((int64_t)gx * n + gy) * rs + gz];
+        }
+    }
+    __syncthreads();
+    int off = sub_off[blockIdx.x];
+    int cnt = min(maxsub, bin_count[b] - off);
+    int p0 = bin_start[b] + off;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+        int pos = p0 + t;
+        T kx[MAXW], ky[MAXW], kz[MAXW];
+        int lx = kernel_vals<T>(ux[pos], w, beta, kx) + h;
+        int ly = kernel_vals<T>(uy[pos], w, beta, ky) + h;
+        int lz = kernel_vals<T>(uz[pos], w, beta, kz) + h;
+        T sr = T(0), si = T(0);
+        for (int a = 0; a < w; ++a) {
+            T ar = T(0), ai = T(0);
+            for (int bb = 0; bb < w; ++bb) {
+                int row = ((lx + a) * S + (ly + bb)) * S + lz;
+                T rr = T(0), ri = T(0);
+#pragma unroll
+                for (int e = 0; e < MAXW; ++e) {
+                    if (e < w) {
+                        if (cgrid) {
+                            rr += kz[e] * sg[2 * (row + e)];
+                            if (OUT == 0) ri += kz[e] * sg[2 * (row + e) + 1];
+                        } else {
+                            rr += kz[e] * sg[row + e];
+                        }
+                    }
+                }
+                ar += ky[bb] * rr;
+                ai += ky[bb] * ri;
+            }
+            sr += kx[a] * ar;
+            si += kx[a] * ai;
+        }
+        int j = perm[pos];
+        if (OUT == 0) {
+            out[2 * (int64_t)j] = sr;
+            out[2 * (int64_t)j + 1] = si;
+        } else {
+            out[j] = sr;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ fused pair
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub_off, const int *bin_count,
+                                              const int *bin_start, const T *ux, const T *uy, const T *uz,
+                                              const T *g1, int n, int bs, int nb, int w, int S, T beta, int maxsub,
+                                              T *g2)
+{
+    extern __shared__ unsigned char smem_raw[];
+    const int cells = S * S * S;
+    T *sa = reinterpret_cast<T *>(smem_raw);
+    T *sb = sa + 2 * cells;
+    int b = sub_bin[blockIdx.x];
+    int bx = b / (nb * nb), by = (b / nb) % nb, bz = b % nb;
+    const int h = w / 2;
+    int ox = bx * bs - h, oy = by * bs - h, oz = bz * bs - h;
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+        int a = i / (S * S), r = i - a * S * S, bb = r / S, e = r - bb * S;
+        int gx = ox + a, gy = oy + bb, gz = oz + e;
+        gx += gx < 0 ? n : (gx >= n ? -n : 0);
+        gy += gy < 0 ? n : (gy >= n ? -n : 0);
+        gz += gz < 0 ? n : (gz >= n ? -n : 0);
+        int64_t g = ((int64_t)gx * n + gy) * n + gz;
+        sa[2 * i] = g1[2 * g];
+        sa[2 * i + 1] = g1[2 * g + 1];
+        sb[2 * i] = T(0);
+        sb[2 * i + 1] = T(0);
+    }
+    __syncthreads();
+    int off = sub_off[blockIdx.x];
+    int cnt = min(maxsub, bin_count[b] - off);
+    int p0 = bin_start[b] + off;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+        int pos = p0 + t;
+        T kx[MAXW], ky[MAXW], kz[MAXW];
+        int lx = kernel_vals<T>(ux[pos], w, beta, kx) + h;
+        int ly = kernel_vals<T>(uy[pos], w, beta, ky) + h;
+        int lz = kernel_vals<T>(uz[pos], w, beta, kz) + h;
+        T sr = T(0), si = T(0);
+        for (int a = 0; a < w; ++a) {
+            T ar = T(0), ai = T(0);
+            for (int bb = 0; bb < w; ++bb) {
+                int row = ((lx + a) * S + (ly + bb)) * S + lz;
+                T rr = T(0), ri = T(0);
+#pragma unroll
+                for (int e = 0; e < MAXW; ++e) {
+                    if (e < w) {
+                        rr += kz[e] * sa[2 * (row + e)];
+                        ri += kz[e] * sa[2 * (row + e) + 1];
+                    }
+                }
+                ar += ky[bb] * rr;
+                ai += ky[bb] * ri;
+            }
+            sr += kx[a] * ar;
+            si += kx[a] * ai;
+        }
+        for (int a = 0; a < w; ++a) {
+            for (int bb = 0; bb < w; ++bb) {
+                T kab = kx[a] * ky[bb];
+                int row = ((lx + a) * S + (ly + bb)) * S + lz;
+                T vr = kab * sr, vi = kab * si;
+#pragma unroll
+                for (int e = 0; e < MAXW; ++e) {
+                    if (e < w) {
+                        atomicAdd(&sb[2 * (row + e)], vr * kz[e]);
+                        atomicAdd(&sb[2 * (row + e) + 1], vi * kz[e]);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+        T vr = sb[2 * i], vi = sb[2 * i + 1];
+        if (vr == T(0) && vi == T(0)) continue;
+        int a = i / (S * S), r = i - a * S * S, bb = r / S, e = r - bb * S;
+        int gx = ox + a, gy = oy + bb, gz = oz + e;
+        gx += gx < 0 ? n : (gx >= n ? -n : 0);
+        gy += gy < 0 ? n : (gy >= n ? -n : 0);
+        gz += gz < 0 ? n : (gz >= n ? -n : 0);
+        int64_t g = ((int64_t)gx * n + gy) * n + gz;
+        atomicAdd(&g2[2 * g], vr);
+        atomicAdd(&g2[2 * g + 1], vi);
+    }
+}
+
+// ------------------------------------------------------------------ deconvolution stages
+
+__device__ __forceinline__ int freq_of(int i, int n) { return i <= n / 2 ? i : i - n; }
+
+// Type 2 (and the first half of the pair): fine-grid spectrum from the modes.
+// HERM: write the half spectrum (n x n x (n/2+1)) of the Hermitian part of the modes for
+// a C2R transform (real-part output); else the full n^3 spectrum for C2C.
+// f: modes (complex or real), centred unless fftord.  support multiplies the modes.
+template <typename T, bool REAL_IN, bool HERM>
+__global__ void k_pad_deconv(const T *f, const float *support, const T *deconv, int M, int n, int fftord,
+                             int conj_out, T *spec)
+{
+    const int nz = HERM ? n / 2 + 1 : n;
+    int64_t total = (int64_t)n * n * nz;
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    int i3 = (int)(idx % nz);
+    int64_t r = idx / nz;
+    int i2 = (int)(r % n), i1 = (int)(r / n);
+    int k1 = freq_of(i1, n), k2 = freq_of(i2, n), k3 = HERM ? i3 : freq_of(i3, n);
+    const int kmin = -(M / 2), kmax = M - 1 - M / 2;
+    T vr = T(0), vi = T(0);
+    auto load = [&](int a, int b, int c, T &re, T &im) {
+        re = T(0);
+        im = T(0);
+        if (a < kmin || a > kmax || b < kmin || b > kmax || c < kmin || c > kmax) return;
+        int ia, ib, ic;
+        if (fftord) {
+            ia = a < 0 ? a + M : a;
+            ib = b < 0 ? b + M : b;
+            ic = c < 0 ? c + M : c;
+        } else {
+            ia = a - kmin;
+            ib = b - kmin;
+            ic = c - kmin;
+        }
+        int64_t m = ((int64_t)ia * M + ib) * M + ic;
+        T s = support ? (T)support[m] : T(1);
+        if (REAL_IN) {
+            re = f[m] * s;
+        } else {
+            re = f[2 * m] * s;
+            im = f[2 * m + 1] * s;
+        }
+    };
+    int lim = M / 2;
+    if (abs(k1) <= lim && abs(k2) <= lim && abs(k3) <= lim) {
+        if (HERM) {
+            T ar, ai, br, bi;
+            load(k1, k2, k3, ar, ai);
+            load(-k1, -k2, -k3, br, bi);
+            vr = T(0.5) * (ar + br);
+            vi = T(0.5) * (ai - bi);
+        } else {
+            load(k1, k2, k3, vr, vi);
+        }
+        T p = deconv[abs(k1)] * deconv[abs(k2)] * deconv[abs(k3)];
+        vr *= p;
+        vi *= p;
+        if (conj_out) vi = -vi;
+    }
+    spec[2 * idx] = vr;
+    spec[2 * idx + 1] = vi;
+}
+
+// Type 1: modes from the transformed fine grid.  HALF: the grid is an R2C half spectrum
+// (n x n x (n/2+1)), else a full C2C spectrum.  The transform computed
+// sum_l b_l e^{-i k l h} (HALF, or C2C forward) or e^{+i k l h} (C2C inverse); sgn_flip
+// says the requested isign is the opposite one, which for a real grid is a conjugation.
+template <typename T, bool HALF, bool REAL_OUT>
+__global__ void k_crop_deconv(const T *spec, const float *support, const T *deconv, int M, int n, int fftord,
+                              int sgn_flip, T scale, T *f)
+{
+    int64_t total = (int64_t)M * M * M;
+    int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= total) return;
+    int ic = (int)(m % M);
+    int64_t r = m / M;
+    int ib = (int)(r % M), ia = (int)(r / M);
+    int k1, k2, k3;
+    if (fftord) {
+        k1 = ia <= (M - 1) / 2 ? ia : ia - M;
+        k2 = ib <= (M - 1) / 2 ? ib : ib - M;
+        k3 = ic <= (M - 1) / 2 ? ic : ic - M;
+        // FFT ordering with even M: index M/2 holds mode -M/2
+        if (!(M & 1)) {
+            if (ia == M / 2) k1 = -M / 2;
+            if (ib == M / 2) k2 = -M / 2;
+            if (ic == M / 2) k3 = -M / 2;
+        }
+    } else {
+        k1 = ia - M / 2;
+        k2 = ib - M / 2;
+        k3 = ic - M / 2;
+    }
+    T vr, vi;
+    if (HALF) {
+        bool neg = k3 < 0;
+        int a = neg ? -k1 : k1, b = neg ? -k2 : k2, c = neg ? -k3 : k3;
+        a = a < 0 ? a + n : a;
+        b = b < 0 ? b + n : b;
+        int64_t g = ((int64_t)a * n + b) * (n / 2 + 1) + c;
+        vr = spec[2 * g];
+        vi = spec[2 * g + 1];
+        // B(k) stored for k3 >= 0; B(-k) = conj(B(k)) for a real grid
+        bool conj = neg != (bool)sgn_flip;
+        if (conj) vi = -vi;
+    } else {
+        int a = k1 < 0 ? k1 + n : k1, b = k2 < 0 ? k2 + n : k2, c = k3 < 0 ? k3 + n : k3;
+        int64_t g = ((int64_t)a * n + b) * n + c;
+        vr = spec[2 * g];
+        vi = spec[2 * g + 1];
+    }
+    T p = deconv[abs(k1)] * deconv[abs(k2)] * deconv[abs(k3)] * scale;
+    if (support) p *= (T)support[m];
+    if (REAL_OUT) {
+        f[m] = vr * p;
+    } else {
+        f[2 * m] = vr * p;
+        f[2 * m + 1] = vi * p;
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+static size_t elem(const Plan &p) { return p.prec == 64 ? sizeof(double) : sizeof(float); }
+
+static int choose_params(Plan &p)
+{
+    double eps = p.eps;
+    double floor_eps = p.prec == 32 ? 1e-7 : 1e-14;
+    if (!(eps > 0) || eps < floor_eps) eps = floor_eps;
+    double sigma = p.sigma > 1.0 ? p.sigma : 2.0;
+    int w;
+    if (sigma == 2.0)
+        w = (int)ceil(log10(1.0 / eps)) + 1;
+    else
+        w = (int)ceil(log(1.0 / eps) / (kPi * sqrt(1.0 - 1.0 / sigma)));
+    w = std::max(2, std::min(w, MAXW));
+    p.w = w;
+    p.sigma = sigma;
+    p.beta = 0.97 * kPi * w * (1.0 - 0.5 / sigma);
+    p.n = next_nice(std::max((int)ceil(sigma * p.M), 2 * w));
+    // bin size: subgrid (bs + w)^3 complex fits two CTAs per SM for the pair kernel
+    size_t e2 = 2 * elem(p);
+    int bs = 16;
+    while (bs > 4 && (size_t)(bs + w) * (bs + w) * (bs + w) * e2 * 2 > 100 * 1024) bs /= 2;
+    p.bs = std::min(bs, p.n);
+    p.nb = (p.n + p.bs - 1) / p.bs;
+    p.S = p.bs + w;
+    return CMT_OK;
+}
+
+template <typename T>
+static int upload_deconv(Plan &p)
+{
+    std::vector<double> gx, gw;
+    gauss_legendre(std::max(64, 4 * p.w), gx, gw);
+    int K = p.M / 2 + 2;
+    std::vector<T> h(K);
+    for (int k = 0; k < K; ++k) h[k] = (T)(1.0 / kernel_ft(k * 2.0 * kPi / p.n, p.w, p.beta, gx, gw));
+    CMT_TRY_CUDA(cudaMalloc(&p.deconv, K * sizeof(T)));
+    CMT_TRY_CUDA(cudaMemcpy(p.deconv, h.data(), K * sizeof(T), cudaMemcpyHostToDevice));
+    return CMT_OK;
+}
+
+static int ensure_fft(Plan &p, int kind)
+{
+    int n = p.n;
+    bool dbl = p.prec == 64;
+    if (kind == 0 && !p.has_c2c) {
+        CMT_TRY_CUFFT(cufftPlan3d(&p.fft_c2c, n, n, n, dbl ? CUFFT_Z2Z : CUFFT_C2C));
+        CMT_TRY_CUFFT(cufftSetStream(p.fft_c2c, p.stream));
+        p.has_c2c = true;
+    }
+    if (kind == 1 && !p.has_r2c) {
+        CMT_TRY_CUFFT(cufftPlan3d(&p.fft_r2c, n, n, n, dbl ? CUFFT_D2Z : CUFFT_R2C));
+        CMT_TRY_CUFFT(cufftSetStream(p.fft_r2c, p.stream));
+        p.has_r2c = true;
+    }
+    if (kind == 2 && !p.has_c2r) {
+        CMT_TRY_CUFFT(cufftPlan3d(&p.fft_c2r, n, n, n, dbl ? CUFFT_Z2D : CUFFT_C2R));
+        CMT_TRY_CUFFT(cufftSetStream(p.fft_c2r, p.stream));
+        p.has_c2r = true;
+    }
+    return CMT_OK;
+}
+
+static int grid_for(int64_t N)
+{
+    int64_t blocks = (N + 255) / 256;
+    return (int)std::min<int64_t>(std::max<int64_t>(blocks, 1), 152 * 16);
+}
+
+template <typename T>
+static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q)
+{
+    p.N = 0;
+    CMT_CHECK_ARG(N > 0 && N <= 0x7fffffffLL, "number of points %lld outside [1, 2^31-1]", (long long)N);
+    int nbins = p.nb * p.nb * p.nb;
+    if (!p.bin_count) {
+        CMT_TRY_CUDA(cudaMalloc(&p.bin_count, sizeof(int) * nbins));
+        CMT_TRY_CUDA(cudaMalloc(&p.bin_fill, sizeof(int) * nbins));
+        CMT_TRY_CUDA(cudaMalloc(&p.bin_start, sizeof(int) * nbins));
+        CMT_TRY_CUDA(cudaMalloc(&p.dflag, sizeof(int) * 4));
+        CMT_TRY_CUDA(cudaMalloc(&p.dtot, sizeof(long long) * 2));
+    }
+    if (N > p.cap_pts) {
+        cudaFree(p.perm);
+        cudaFree(p.ux);
+        cudaFree(p.uy);
+        cudaFree(p.uz);
+        p.perm = nullptr;
+        p.ux = p.uy = p.uz = nullptr;
+        p.cap_pts = 0;
+        CMT_TRY_CUDA(cudaMalloc(&p.perm, sizeof(int) * N));
+        CMT_TRY_CUDA(cudaMalloc(&p.ux, sizeof(T) * N));
+        CMT_TRY_CUDA(cudaMalloc(&p.uy, sizeof(T) * N));
+        CMT_TRY_CUDA(cudaMalloc(&p.uz, sizeof(T) * N));
+        p.cap_pts = N;
+    }
+    cudaStream_t st = p.stream;
+    CMT_TRY_CUDA(cudaMemsetAsync(p.bin_count, 0, sizeof(int) * nbins, st));
+    CMT_TRY_CUDA(cudaMemsetAsync(p.bin_fill, 0, sizeof(int) * nbins, st));
+    CMT_TRY_CUDA(cudaMemsetAsync(p.dflag, 0, sizeof(int) * 4, st));
+    double s = p.n / (2.0 * kPi);
+    T s_hi = (T)s, s_lo = (T)(s - (double)s_hi);
+    int g = grid_for(N);
+    k_bin_count<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, p.n, p.bs, p.nb, p.bin_count, p.dflag);
+    CMT_LAUNCH_CHECK();
+    int *sub_start = p.bin_fill;  // reuse as scratch for the subproblem scan
+    k_scan_bins<<<1, 1024, 0, st>>>(nbins, p.bin_count, p.bin_start, sub_start, p.maxsub, p.dtot);
+    CMT_LAUNCH_CHECK();
+    long long tot[2];
+    int flag = 0;
+    CMT_TRY_CUDA(cudaMemcpyAsync(tot, p.dtot, sizeof tot, cudaMemcpyDeviceToHost, st));
+    CMT_TRY_CUDA(cudaMemcpyAsync(&flag, p.dflag, sizeof flag, cudaMemcpyDeviceToHost, st));
+    CMT_TRY_CUDA(cudaStreamSynchronize(st));
+    if (flag) {
+        set_error("nonuniform point outside (-3 pi, 3 pi) (cmtip asserts |x| < 3 pi)");
+        return CMT_ERR_RANGE;
+    }
+    p.nsub = tot[0];
+    if (p.nsub > p.cap_sub) {
+        cudaFree(p.sub_bin);
+        cudaFree(p.sub_off);
+        p.sub_bin = p.sub_off = nullptr;
+        p.cap_sub = 0;
+        CMT_TRY_CUDA(cudaMalloc(&p.sub_bin, sizeof(int) * p.nsub));
+        CMT_TRY_CUDA(cudaMalloc(&p.sub_off, sizeof(int) * p.nsub));
+        p.cap_sub = p.nsub;
+    }
+    k_sub_list<<<ceil_div(nbins, 256), 256, 0, st>>>(nbins, p.bin_count, sub_start, p.maxsub, p.sub_bin, p.sub_off);
+    CMT_LAUNCH_CHECK();
+    CMT_TRY_CUDA(cudaMemsetAsync(p.bin_fill, 0, sizeof(int) * nbins, st));
+    k_bin_scatter<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, p.n, p.bs, p.nb, p.bin_start, p.bin_count,
+                                        p.bin_fill, p.perm, (T *)p.ux, (T *)p.uy, (T *)p.uz, p.dflag);
+    CMT_LAUNCH_CHECK();
+    CMT_TRY_CUDA(cudaMemcpyAsync(&flag, p.dflag, sizeof flag, cudaMemcpyDeviceToHost, st));
+    CMT_TRY_CUDA(cudaStreamSynchronize(st));
+    if (flag) {
+        set_error("internal error: bin assignment differs between counting passes");
+        return CMT_ERR_STATE;
+    }
+    p.N = N;
+    return CMT_OK;
+}
+
+static int smem_bytes(const Plan &p, int grids, bool cplx)
+{
+    return p.S * p.S * p.S * (cplx ? 2 : 1) * (int)elem(p) * grids;
+}
+
+template <typename K>
+static int prep_smem(K kernel, int bytes)
+{
+    if (bytes > 48 * 1024) CMT_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return CMT_OK;
+}
+
+template <typename T>
+static int exec_type1(Plan &p, const T *c, T *f, const float *support, double scale, int flags)
+{
+    bool real_in = flags & CMT_REAL_IN, real_out = flags & CMT_REAL_OUT, fftord = flags & CMT_MODEORD_FFT;
+    cudaStream_t st = p.stream;
+    int n = p.n;
+    int64_t nsub = p.nsub;
+    T beta = (T)p.beta;
+    int M = p.M;
+    int64_t mt = (int64_t)M * M * M;
+    if (real_in) {
+        CMT_TRY(ensure_fft(p, 1));
+        int rs = n + 2;
+        CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * (size_t)n * n * rs, st));
+        int sm = smem_bytes(p, 1, false);
+        CMT_TRY(prep_smem(k_spread<T, false>, sm));
+        k_spread<T, false><<<(unsigned)nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
+                                                            (T *)p.ux, (T *)p.uy, (T *)p.uz, c, nullptr, n, rs, p.bs,
+                                                            p.nb, p.w, p.S, beta, p.maxsub, (T *)p.fine);
+        CMT_LAUNCH_CHECK();
+        if (p.prec == 64)
+            CMT_TRY_CUFFT(cufftExecD2Z(p.fft_r2c, (double *)p.fine, (cufftDoubleComplex *)p.fine));
+        else
+            CMT_TRY_CUFFT(cufftExecR2C(p.fft_r2c, (float *)p.fine, (cufftComplex *)p.fine));
+        int sgn_flip = p.isign > 0;  // R2C computed e^{-i}
+        unsigned gb = (unsigned)ceil_div(mt, 256);
+        if (real_out)
+            k_crop_deconv<T, true, true><<<gb, 256, 0, st>>>((T *)p.fine, support, (T *)p.deconv, M, n, fftord,
+                                                             sgn_flip, (T)scale, f);
+        else
+            k_crop_deconv<T, true, false><<<gb, 256, 0, st>>>((T *)p.fine, support, (T *)p.deconv, M, n, fftord,
+                                                              sgn_flip, (T)scale, f);
+        CMT_LAUNCH_CHECK();
+    } else {
+        CMT_TRY(ensure_fft(p, 0));
+        CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * 2 * (size_t)n * n * n, st));
+        int sm = smem_bytes(p, 1, true);
+        CMT_TRY(prep_smem(k_spread<T, true>, sm));
+        k_spread<T, true><<<(unsigned)nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
+                                                           (T *)p.ux, (T *)p.uy, (T *)p.uz, c, nullptr, n, n, p.bs,
+                                                           p.nb, p.w, p.S, beta, p.maxsub, (T *)p.fine);
+        CMT_LAUNCH_CHECK();
+        int dir = p.isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
+        if (p.prec == 64)
+            CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
+        else
+            CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, dir));
+        unsigned gb = (unsigned)ceil_div(mt, 256);
+        if (real_out)
+            k_crop_deconv<T, false, true><<<gb, 256, 0, st>>>((T *)p.fine, support, (T *)p.deconv, M, n, fftord, 0,
+                                                              (T)scale, f);
+        else
+            k_crop_deconv<T, false, false><<<gb, 256, 0, st>>>((T *)p.fine, support, (T *)p.deconv, M, n, fftord, 0,
+                                                               (T)scale, f);
+        CMT_LAUNCH_CHECK();
+    }
+    return CMT_OK;
+}
+
+template <typename T>
+static int exec_type2(Plan &p, T *c, const T *f, const float *support, double scale, int flags)
+{
+    bool real_in = flags & CMT_REAL_IN, real_out = flags & CMT_REAL_OUT, fftord = flags & CMT_MODEORD_FFT;
+    CMT_CHECK_ARG(scale == 1.0, "type-2 execute takes scale = 1");
+    cudaStream_t st = p.stream;
+    int n = p.n;
+    T beta = (T)p.beta;
+    int M = p.M;
+    if (real_out) {
+        // Re(c) = sum_k g_k e^{isign i k.x} with g the Hermitian part of f: real fine grid
+        CMT_TRY(ensure_fft(p, 2));
+        int64_t tot = (int64_t)n * n * (n / 2 + 1);
+        unsigned gb = (unsigned)ceil_div(tot, 256);
+        int conj_out = p.isign < 0;  // C2R computes e^{+i}
+        if (real_in)
+            k_pad_deconv<T, true, true><<<gb, 256, 0, st>>>(f, support, (T *)p.deconv, M, n, fftord, conj_out,
+                                                            (T *)p.fine);
+        else
+            k_pad_deconv<T, false, true><<<gb, 256, 0, st>>>(f, support, (T *)p.deconv, M, n, fftord, conj_out,
+                                                             (T *)p.fine);
+        CMT_LAUNCH_CHECK();
+        if (p.prec == 64)
+            CMT_TRY_CUFFT(cufftExecZ2D(p.fft_c2r, (cufftDoubleComplex *)p.fine, (double *)p.fine));
+        else
+            CMT_TRY_CUFFT(cufftExecC2R(p.fft_c2r, (cufftComplex *)p.fine, (float *)p.fine));
+        int sm = smem_bytes(p, 1, false);
+        CMT_TRY(prep_smem(k_interp<T, 2>, sm));
+        k_interp<T, 2><<<(unsigned)p.nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
+                                                          (T *)p.ux, (T *)p.uy, (T *)p.uz, (T *)p.fine, n, n + 2, p.bs,
+                                                          p.nb, p.w, p.S, beta, p.maxsub, c);
+        CMT_LAUNCH_CHECK();
+    } else {
+        CMT_TRY(ensure_fft(p, 0));
+        int64_t tot = (int64_t)n * n * n;
+        unsigned gb = (unsigned)ceil_div(tot, 256);
+        if (real_in)
+            k_pad_deconv<T, true, false><<<gb, 256, 0, st>>>(f, support, (T *)p.deconv, M, n, fftord, 0, (T *)p.fine);
+        else
+            k_pad_deconv<T, false, false><<<gb, 256, 0, st>>>(f, support, (T *)p.deconv, M, n, fftord, 0,
+                                                              (T *)p.fine);
+        CMT_LAUNCH_CHECK();
+        int dir = p.isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
+        if (p.prec == 64)
+            CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
+        else
+            CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, dir));
+        int sm = smem_bytes(p, 1, true);
+        CMT_TRY(prep_smem(k_interp<T, 0>, sm));
+        k_interp<T, 0><<<(unsigned)p.nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
+                                                          (T *)p.ux, (T *)p.uy, (T *)p.uz, (T *)p.fine, n, n, p.bs,
+                                                          p.nb, p.w, p.S, beta, p.maxsub, c);
+        CMT_LAUNCH_CHECK();
+    }
+    return CMT_OK;
+}
+
+template <typename T>
+static int exec_pair(Plan &p, const T *fin, T *fout, const float *support, double scale)
+{
+    cudaStream_t st = p.stream;
+    int n = p.n;
+    int M = p.M;
+    CMT_TRY(ensure_fft(p, 0));
+    if (!p.fine2) CMT_TRY_CUDA(cudaMalloc(&p.fine2, 2 * elem(p) * (size_t)n * n * n));
+    int64_t tot = (int64_t)n * n * n;
+    unsigned gb = (unsigned)ceil_div(tot, 256);
+    // A: modes -> fine grid, isign -1 (cmtip's forward, forward.py:40)
+    k_pad_deconv<T, true, false><<<gb, 256, 0, st>>>(fin, support, (T *)p.deconv, M, n, 0, 0, (T *)p.fine);
+    CMT_LAUNCH_CHECK();
+    if (p.prec == 64)
+        CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, CUFFT_FORWARD));
+    else
+        CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, CUFFT_FORWARD));
+    CMT_TRY_CUDA(cudaMemsetAsync(p.fine2, 0, 2 * elem(p) * (size_t)n * n * n, st));
+    int sm = smem_bytes(p, 2, true);
+    CMT_TRY(prep_smem(k_pair<T>, sm));
+    k_pair<T><<<(unsigned)p.nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, (T *)p.ux,
+                                                 (T *)p.uy, (T *)p.uz, (T *)p.fine, n, p.bs, p.nb, p.w, p.S,
+                                                 (T)p.beta, p.maxsub, (T *)p.fine2);
+    CMT_LAUNCH_CHECK();
+    // A^H: isign +1 (cmtip's adjoint, adjoint.py:33)
+    if (p.prec == 64)
+        CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine2, (cufftDoubleComplex *)p.fine2, CUFFT_INVERSE));
+    else
+        CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine2, (cufftComplex *)p.fine2, CUFFT_INVERSE));
+    unsigned gm = (unsigned)ceil_div((int64_t)M * M * M, 256);
+    k_crop_deconv<T, false, true><<<gm, 256, 0, st>>>((T *)p.fine2, support, (T *)p.deconv, M, n, 0, 0, (T)scale, fout);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+static void destroy(Plan *p)
+{
+    if (!p) return;
+    cudaFree(p->bin_count);
+    cudaFree(p->bin_fill);
+    cudaFree(p->bin_start);
+    cudaFree(p->sub_bin);
+    cudaFree(p->sub_off);
+    cudaFree(p->perm);
+    cudaFree(p->ux);
+    cudaFree(p->uy);
+    cudaFree(p->uz);
+    cudaFree(p->dflag);
+    cudaFree(p->dtot);
+    cudaFree(p->fine);
+    cudaFree(p->fine2);
+    cudaFree(p->deconv);
+    if (p->has_c2c) cufftDestroy(p->fft_c2c);
+    if (p->has_r2c) cufftDestroy(p->fft_r2c);
+    if (p->has_c2r) cufftDestroy(p->fft_c2r);
+}
+
+}  // namespace cmt
+
+// ====================================================================== C ABI
+
+using namespace cmt;
+
+extern "C" const char *cmt_last_error(void) { return cmt::g_err; }
+
+extern "C" const char *cmt_version(void) { return "cmtip_gb300 0.1 (sm_103a)"; }
+
+extern "C" int cmt_plan_create(int type, int M, int prec, double eps, int isign, double upsampfac, void *stream,
+                               cmt_plan **out)
+{
+    CMT_CHECK_ARG(out, "null plan pointer");
+    *out = nullptr;
+    CMT_CHECK_ARG(type == 1 || type == 2, "type must be 1 or 2 (got %d)", type);
+    CMT_CHECK_ARG(prec == 32 || prec == 64, "prec must be 32 or 64 (got %d)", prec);
+    CMT_CHECK_ARG(M >= 1 && M <= 1024, "M must be in [1, 1024] (got %d)", M);
+    CMT_CHECK_ARG(isign == 1 || isign == -1, "isign must be +1 or -1");
+    cmt_plan *p = new (std::nothrow) cmt_plan();
+    if (!p) {
+        set_error("host allocation failed");
+        return CMT_ERR_OOM;
+    }
+    p->type = type;
+    p->M = M;
+    p->prec = prec;
+    p->eps = eps;
+    p->isign = isign;
+    p->sigma = upsampfac > 1.0 ? upsampfac : 2.0;
+    p->stream = (cudaStream_t)stream;
+    choose_params(*p);
+    int rc = CMT_OK;
+    size_t bytes = 2 * elem(*p) * (size_t)p->n * p->n * p->n;
+    cudaError_t e = cudaMalloc(&p->fine, bytes);
+    if (e != cudaSuccess) {
+        set_error("fine grid allocation (%zu bytes): %s", bytes, cudaGetErrorString(e));
+        rc = CMT_ERR_OOM;
+    }
+    if (rc == CMT_OK) rc = prec == 64 ? upload_deconv<double>(*p) : upload_deconv<float>(*p);
+    if (rc != CMT_OK) {
+        destroy(p);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return CMT_OK;
+}
+
+extern "C" int cmt_plan_info(const cmt_plan *p, int *n_fine, int *width, double *beta, int *bin_size,
+                             int64_t *n_sub)
+{
+    CMT_CHECK_ARG(p, "null plan");
+    if (n_fine) *n_fine = p->n;
+    if (width) *width = p->w;
+    if (beta) *beta = p->beta;
+    if (bin_size) *bin_size = p->bs;
+    if (n_sub) *n_sub = p->nsub;
+    return CMT_OK;
+}
+
+extern "C" int cmt_set_pts(cmt_plan *p, int64_t N, const void *x, const void *y, const void *z)
+{
+    CMT_CHECK_ARG(p && x && y && z, "null argument");
+    QuatSrc q{nullptr, nullptr, 1, 1.0};
+    if (p->prec == 64) return set_pts_impl<double>(*p, 0, N, (const double *)x, (const double *)y, (const double *)z, q);
+    return set_pts_impl<float>(*p, 0, N, (const float *)x, (const float *)y, (const float *)z, q);
+}
+
+extern "C" int cmt_set_pts_quat(cmt_plan *p, int64_t n_img, const double *inv_rot, int64_t n_pix, const double *ppr,
+                                double rext)
+{
+    CMT_CHECK_ARG(p && inv_rot && ppr, "null argument");
+    CMT_CHECK_ARG(n_img > 0 && n_pix > 0, "empty image set");
+    CMT_CHECK_ARG(rext > 0, "reciprocal_extent must be positive");
+    QuatSrc q{inv_rot, ppr, n_pix, rext};
+    int64_t N = n_img * n_pix;
+    if (p->prec == 64) return set_pts_impl<double>(*p, 1, N, nullptr, nullptr, nullptr, q);
+    return set_pts_impl<float>(*p, 1, N, nullptr, nullptr, nullptr, q);
+}
+
+extern "C" int cmt_execute(cmt_plan *p, void *c, void *f, const float *support, double scale, int flags)
+{
+    // type 1 with real strengths accepts c == NULL: every strength is 1 (the Toeplitz
+    // kernel's adjoint of ones, autocorrelation.py:141-147)
+    CMT_CHECK_ARG(p && f && (c || (p->type == 1 && (flags & CMT_REAL_IN))), "null argument");
+    if (p->N <= 0) {
+        set_error("execute before set_pts");
+        return CMT_ERR_STATE;
+    }
+    if (p->type == 1) {
+        if (p->prec == 64) return exec_type1<double>(*p, (const double *)c, (double *)f, support, scale, flags);
+        return exec_type1<float>(*p, (const float *)c, (float *)f, support, scale, flags);
+    }
+    if (p->prec == 64) return exec_type2<double>(*p, (double *)c, (const double *)f, support, scale, flags);
+    return exec_type2<float>(*p, (float *)c, (const float *)f, support, scale, flags);
+}
+
+extern "C" int cmt_execute_pair(cmt_plan *p, const void *fin, void *fout, const float *support, double scale)
+{
+    CMT_CHECK_ARG(p && fin && fout, "null argument");
+    if (p->N <= 0) {
+        set_error("execute before set_pts");
+        return CMT_ERR_STATE;
+    }
+    if (p->prec == 64) return exec_pair<double>(*p, (const double *)fin, (double *)fout, support, scale);
+    return exec_pair<float>(*p, (const float *)fin, (float *)fout, support, scale);
+}
+
+extern "C" int cmt_plan_destroy(cmt_plan *p)
+{
+    if (!p) return CMT_OK;
+    destroy(p);
+    delete p;
+    return CMT_OK;
+}
+
+extern "C" int cmt_inverse_rotations(const float *quat, int64_t n, double *out, void *stream)
+{
+    CMT_CHECK_ARG(quat && out && n >= 0, "bad argument");
+    if (n == 0) return CMT_OK;
+    k_inverse_rotations<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(quat, n, out);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}

@@ -1,0 +1,153 @@
+/*
+ * cmtip_gb300 -- C ABI of the GB300 (sm_103a) reconstruction hot path of cartesian
+ * MTIP: 3D type-1/type-2 NUFFT, the conjugate-gradient autocorrelation solve and
+ * orientation matching.
+ *
+ * All array pointers are DEVICE pointers owned by the caller (PyTorch tensors in
+ * the Python layer); every call is stream-ordered on the stream given at creation
+ * (a cudaStream_t passed as void*, NULL = legacy default stream).  Objects own only
+ * their workspace.  Every function returns a status code (CMT_OK = 0);
+ * cmt_last_error() returns a thread-local description of the last failure.
+ *
+ * Reference interfaces replaced (paths inside the cmtip project):
+ *   cmt_plan_create / cmt_set_pts / cmt_execute / cmt_plan_destroy
+ *       -> cmtip/nufft/forward.py:45-82 forward_gpu (cufinufft type 2, isign -1,
+ *          set_pts at :77-79, execute :79) and cmtip/nufft/adjoint.py:46-86
+ *          adjoint_gpu (cufinufft type 1, isign +1, set_pts :74, execute :75,
+ *          *support / .real / M**3 at :79-86), and the CPU twins forward_cpu
+ *          (:13-42, finufft nufft3d2) / adjoint_cpu (:13-43, finufft nufft3d1).
+ *   cmt_set_pts_quat / cmt_inverse_rotations
+ *       -> cmtip/autocorrelation/autocorrelation.py:12-29 gen_nonuniform_positions and
+ *          cmtip/alignment/align.py:50-57 (rotate pixel q-vectors by inv(R(q)), cast to
+ *          float32, scale by pi / reciprocal_extent).
+ *   cmt_execute_pair
+ *       -> the data term of W in cmtip/autocorrelation/autocorrelation.py:150-155
+ *          (core_problem_convolution, :32-63) applied as an explicit type-2 then
+ *          type-1 pair instead of the Toeplitz embedding.
+ *   cmt_cg_*
+ *       -> cmtip/autocorrelation/autocorrelation.py:113-173 setup_linops and the
+ *          scipy cg call of solve_ac (:234-239).
+ *   cmt_match_*
+ *       -> cmtip/alignment/align.py:68-132 match_orientations (compute_slices :39-65,
+ *          std scaling :122-124, calc_eudist :27-36, argmin :131).
+ */
+#ifndef CMTIP_GB300_H
+#define CMTIP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CMT_OK 0
+#define CMT_ERR_ARG 1      /* bad argument (shape, type, size, null pointer) */
+#define CMT_ERR_RANGE 2    /* a nonuniform point has |x| >= 3 pi (forward.py:27, adjoint.py:29) */
+#define CMT_ERR_OOM 3      /* device allocation failed */
+#define CMT_ERR_CUDA 4     /* CUDA runtime error */
+#define CMT_ERR_TIMEOUT 5  /* a bounded device wait gave up */
+#define CMT_ERR_CUFFT 6    /* cuFFT error */
+#define CMT_ERR_STATE 7    /* call out of order (e.g. execute before set_pts) */
+
+/* cmt_execute flags */
+#define CMT_REAL_IN 1      /* type 1: strengths c are real; type 2: modes f are real */
+#define CMT_REAL_OUT 2     /* type 1: write Re(f) (M^3 reals); type 2: write Re(c) (N reals) */
+#define CMT_MODEORD_FFT 4  /* modes stored FFT-style (k at index k mod M) instead of centred */
+
+typedef struct cmt_plan cmt_plan;
+
+/* Create a cubic 3D NUFFT plan.
+ * type   1 (nonuniform -> M^3 modes) or 2 (M^3 modes -> nonuniform)
+ * M      modes per dimension; mode k in [-floor(M/2), (M-1)-floor(M/2)],
+ *        stored centred (index k + floor(M/2)) unless CMT_MODEORD_FFT
+ * prec   32 (float / complex64) or 64 (double / complex128)
+ * eps    requested relative tolerance (sets kernel width); clamped to what prec can reach
+ * isign  sign of the exponent: -1 for cmtip's forward, +1 for its adjoint
+ * upsampfac  fine grid / M ratio (0 = automatic choice)
+ * Replaces cufinufft(type, shape, isign=, eps=, dtype=, gpu_method=1) at forward.py:77 / adjoint.py:73. */
+int cmt_plan_create(int type, int M, int prec, double eps, int isign, double upsampfac,
+                    void *stream, cmt_plan **plan);
+
+/* Query the chosen fine-grid size, kernel width, ES shape parameter and bin size. */
+int cmt_plan_info(const cmt_plan *plan, int *n_fine, int *width, double *beta, int *bin_size,
+                  int64_t *n_subproblems);
+
+/* Set nonuniform points from coordinate arrays (device, prec-typed, length N, radians,
+ * |x| < 3 pi).  Points are counting-sorted into spatial bins of the fine grid; the plan
+ * keeps the sorted coordinates and the permutation.  Replaces plan.set_pts (forward.py:77-79:
+ * cufinufft is given (L, K, H) so that H pairs with array axis 0; here x pairs with axis 0). */
+int cmt_set_pts(cmt_plan *plan, int64_t N, const void *x, const void *y, const void *z);
+
+/* Set points from per-image inverse rotation matrices (device, n_img x 3 x 3 float64) and
+ * detector q-vectors (device, 3 x n_pix float64): point (i, p) has coordinates
+ * float32(inv_rot[i] . ppr[:, p]) * pi / reciprocal_extent, point index i * n_pix + p. */
+int cmt_set_pts_quat(cmt_plan *plan, int64_t n_img, const double *inv_rot, int64_t n_pix,
+                     const double *ppr, double reciprocal_extent);
+
+/* Execute.  type 1: c (N strengths) -> f (M^3 modes); type 2: f -> c.
+ * support  optional M^3 float mask multiplied into the modes (type 1: output; type 2: input)
+ * scale    multiplies the output (cmtip's adjoint divides by M**3, adjoint.py:43)
+ * flags    CMT_REAL_IN / CMT_REAL_OUT / CMT_MODEORD_FFT
+ * For type 1 with CMT_REAL_IN, c may be NULL: all strengths are 1. */
+int cmt_execute(cmt_plan *plan, void *c, void *f, const float *support, double scale, int flags);
+
+/* Fused type-2 then type-1 pair on the plan's points (the normal operator A^H A):
+ * f_out = scale * S . Re( sum_j e^{+i k.x_j} sum_k' e^{-i k'.x_j} (S . f_in)_k' )
+ * with S the optional support.  f_in / f_out are real M^3 grids of the plan's precision. */
+int cmt_execute_pair(cmt_plan *plan, const void *f_in, void *f_out, const float *support, double scale);
+
+int cmt_plan_destroy(cmt_plan *plan);
+
+/* ---------------------------------------------------------------- CG solve
+ * Solver of W x = d, W = alambda * S.conv(T, S x) + rlambda * x + flambda * S.Re(IFFT(FFT(S x).A))
+ * (cmtip/autocorrelation/autocorrelation.py:113-173 setup_linops, :150-155 W_matvec) with
+ * scipy's cg iteration (autocorrelation.py:239).  prec 32: float vectors, FP64 dots / norms /
+ * alpha / beta; prec 64: all double.  op 0: Toeplitz data term on the (2M)^3 grid (the
+ * reference's form); op 1: explicit fused type-2 then type-1 pair (cmt_execute_pair). */
+typedef struct cmt_cg cmt_cg;
+
+int cmt_cg_create(int M, int prec, int op, void *stream, cmt_cg **cg);
+
+/* Toeplitz kernel: T_circ = (2M)^3 real grid (prec), FFT order, already / (2M)^3 as cmtip's
+ * adjoint returns it (autocorrelation.py:141-147); stored as FFT(T_circ) / (2M)^3 (:148, :54). */
+int cmt_cg_set_kernel(cmt_cg *cg, const void *t_circ);
+
+/* mask_fft: ifftshift(gen_F_antisupport(M)) as float M^3 (autocorrelation.py:66-85, :105);
+ * support: M^3 float; lambdas as in autocorrelation.py:223-225. */
+int cmt_cg_set_operator(cmt_cg *cg, const float *mask_fft, const float *support, double alambda,
+                        double rlambda, double flambda);
+
+/* op 1: type-1 plan (M modes, same prec) whose points define A. */
+int cmt_cg_set_pair_plan(cmt_cg *cg, cmt_plan *plan);
+
+/* y = W x (M^3 vectors of the solver precision). */
+int cmt_cg_matvec(cmt_cg *cg, const void *x, void *y);
+
+/* x (in: x0, out: solution) after at most maxiter iterations; stops when
+ * ||r|| < max(atol, rtol ||d||) (scipy semantics).  use_graph: replay a captured iteration.
+ * iters / final_rho (optional, host) receive the iteration count and r.r. */
+int cmt_cg_solve(cmt_cg *cg, const void *d, void *x, int maxiter, double rtol, double atol,
+                 int use_graph, int *iters, double *final_rho);
+
+int cmt_cg_destroy(cmt_cg *cg);
+
+/* support = gaussian_filter(est, 0.5) > 1e-12 as 0/1 floats, and est *= support when
+ * est_inplace (autocorrelation.py:217-220).  scratch: 2 M^3 floats. */
+int cmt_support_from_estimate(float *est, int M, float *support, float *scratch, int est_inplace,
+                              void *stream);
+
+/* inv(R(q)) for n float32 quaternions (w, x, y, z), skopi convention (element products
+ * rounded to float32 as with float32 quaternions), into n x 3 x 3 float64. */
+int cmt_inverse_rotations(const float *quat, int64_t n, double *inv_rot, void *stream);
+
+const char *cmt_last_error(void);
+
+/* library version string */
+const char *cmt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CMTIP_GB300_H */

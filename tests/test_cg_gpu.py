@@ -1,0 +1,105 @@
+"""CUDA CG autocorrelation solve against the reference's fixtures and the FP64 oracle.
+
+Bars: the mixed-precision solver (FP32 vectors and NUFFT at eps 1e-6, FP64 dots) reaches
+relative L2 <= 1e-4 on the solved autocorrelation; the FP64 form at eps 1e-12 agrees with
+the reference's own CG (complex128 numpy/scipy) to <= 1e-7."""
+import numpy as np
+import pytest
+import torch
+from scipy.ndimage import gaussian_filter
+
+from conftest import rel_l2
+from oracle import reference_port as rp
+
+pytestmark = pytest.mark.gpu
+
+TOL_AC = 1e-4
+
+
+@pytest.fixture(scope="module")
+def ac_mod():
+    import cmtip_gb300.autocorrelation as ac
+    return ac
+
+
+def _linops(ac_mod, g, prec, operator="toeplitz"):
+    M = int(g["M"])
+    s = rp.solve_ac_inputs(g["ppr"], g["slices"], M, g["quats"], g["estimate"].copy())
+    eps = 1e-6 if prec == 32 else 1e-12
+    W, d = ac_mod.setup_linops(s["H"], s["K"], s["L"], s["data"], s["ac_support"], s["weights"], s["x0"], M,
+                               s["Mtot"], s["N"], g["rext"], s["alambda"], s["rlambda"], s["flambda"],
+                               prec=prec, operator=operator, eps=eps)
+    return W, d, s
+
+
+@pytest.mark.parametrize("prec,tol", [(64, 1e-9), (32, 1e-5)])
+def test_rhs_and_matvec_match_reference(ac_mod, golden, prec, tol):
+    g = golden("autocorrelation")
+    W, d, _ = _linops(ac_mod, g, prec)
+    assert rel_l2(d, g["d"]) < tol
+    for p, wp in zip(g["probe"], g["W_probe"]):
+        assert rel_l2(W.matvec(p), wp.real) < tol
+
+
+@pytest.mark.parametrize("prec,tol", [(64, 1e-9), (32, 1e-5)])
+def test_pair_operator_equals_toeplitz(ac_mod, golden, prec, tol):
+    g = golden("autocorrelation")
+    Wt, _, _ = _linops(ac_mod, g, prec, "toeplitz")
+    Wp, _, _ = _linops(ac_mod, g, prec, "pair")
+    for p in g["probe"]:
+        assert rel_l2(Wp.matvec(p), Wt.matvec(p)) < 10 * tol
+
+
+@pytest.mark.parametrize("prec,tol", [(64, 1e-7), (32, TOL_AC)])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_fixed_iterations_match_reference(ac_mod, golden, prec, tol, use_graph):
+    g = golden("autocorrelation")
+    W, d, s = _linops(ac_mod, g, prec)
+    x, it = W.solver.solve(torch.from_numpy(d), torch.from_numpy(s["x0"].astype(np.float64)), maxiter=10,
+                           rtol=0.0, use_graph=use_graph)
+    assert it == 10
+    assert rel_l2(x.cpu().numpy(), g["x_cg10"].real) < tol
+
+
+@pytest.mark.parametrize("prec,tol", [(64, 1e-6), (32, TOL_AC)])
+@pytest.mark.parametrize("operator", ["toeplitz", "pair"])
+def test_solve_ac_matches_reference(ac_mod, golden, prec, tol, operator):
+    g = golden("autocorrelation")
+    M = int(g["M"])
+    eps = 1e-6 if prec == 32 else 1e-12
+    est = g["estimate"].copy()
+    ac, info = ac_mod.solve_ac(1, g["ppr"], g["rext"], g["slices"], M, orientations=g["quats"], ac_estimate=est,
+                               prec=prec, operator=operator, eps=eps, return_info=True)
+    assert ac.dtype == np.float64 and ac.shape == (M,) * 3
+    assert rel_l2(ac, g["ac_solved"]) < tol
+    # the reference masks the estimate in place (autocorrelation.py:220)
+    assert np.array_equal(est, g["estimate"] * g["ac_support"])
+    ac0 = ac_mod.solve_ac(0, g["ppr"], g["rext"], g["slices"], M, orientations=g["quats"], ac_estimate=None,
+                          prec=prec, operator=operator, eps=eps)
+    assert rel_l2(ac0, g["ac_gen0"]) < tol
+
+
+def test_support_matches_ndimage(ac_mod):
+    rng = np.random.default_rng(2)
+    for M in (9, 20, 33):
+        est = (rng.standard_normal((M,) * 3) * (rng.random((M,) * 3) > 0.5)).astype(np.float32)
+        est[rng.random((M,) * 3) > 0.7] = 1e-13
+        ref = (gaussian_filter(est, 0.5) > 1e-12).astype(np.float32)
+        t = torch.from_numpy(est).cuda()
+        sup = ac_mod.support_from_estimate(t, inplace=True)
+        assert np.array_equal(sup.cpu().numpy(), ref)
+        assert np.array_equal(t.cpu().numpy(), est * ref)
+
+
+def test_converged_early_stops_like_scipy(ac_mod, golden):
+    g = golden("autocorrelation")
+    W, d, s = _linops(ac_mod, g, 64)
+    from scipy.sparse.linalg import LinearOperator, cg
+    n = int(g["M"]) ** 3
+    count = [0]
+    Wr = LinearOperator(dtype=np.float64, shape=(n, n), matvec=W.matvec)
+    xr, _ = cg(Wr, d, x0=s["x0"].astype(np.float64), maxiter=200, rtol=1e-3,
+               callback=lambda xk: count.__setitem__(0, count[0] + 1))
+    x, it = W.solver.solve(torch.from_numpy(d), torch.from_numpy(s["x0"].astype(np.float64)), maxiter=200, rtol=1e-3)
+    assert it == count[0]
+    assert rel_l2(x.cpu().numpy(), xr) < 1e-9
