@@ -1,0 +1,928 @@
+// Orientation matching: weighted euclidean distances between data images and model slices
+// with a running top-k / argmin epilogue (cmtip/alignment/align.py:68-132).
+//
+//   d(r, i)^2 = || w . (s_r m_r - x_i) ||^2 = s_r^2 |w m_r|^2 + |w x_i|^2 - 2 s_r (w m_r).(w x_i)
+//
+// (weights w multiply both operands as in align.py:127-128; s_r = std(data) / std(model batch)
+// of the reference batch holding r, align.py:122-124).  For the argmin over r only
+// g(r, i) = s_r^2 |w m_r|^2 - 2 s_r (w m_r).(w x_i) matters, so the kernels compute the
+// cross term as a GEMM and keep, per image, the TOPK best g in registers; the distance
+// matrix never reaches HBM.  A merge kernel then re-scores those candidates exactly
+// (FP64 accumulation of the FP32 inputs) and picks the argmin (first index on ties, as
+// numpy's argmin), counting near-ties whose best two distances differ by less than one
+// FP32 rounding.
+//
+// Forms: BF16 operands on the 5th-generation tensor cores (tcgen05.mma, TMEM accumulators,
+// TMA loads with 128B swizzle, warp-specialised pipeline); plain FP32 and plain FP64
+// SIMT kernels (the comparison forms).
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "cmt_common.cuh"
+
+namespace cmt {
+
+constexpr int TOPK = 8;
+constexpr float SCORE_INF = 3.0e38f;
+
+__device__ __forceinline__ void topk_insert(float (&s)[TOPK], int (&id)[TOPK], float g, int r)
+{
+    if (!(g < s[TOPK - 1])) return;
+    s[TOPK - 1] = g;
+    id[TOPK - 1] = r;
+#pragma unroll
+    for (int k = TOPK - 1; k > 0; --k) {
+        if (s[k] < s[k - 1]) {
+            float ts = s[k];
+            s[k] = s[k - 1];
+            s[k - 1] = ts;
+            int ti = id[k];
+            id[k] = id[k - 1];
+            id[k - 1] = ti;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ operand preparation
+
+// One CTA per row: u = w . v (FP64), operand row (padded with zeros to Kp), |u|^2, and the
+// row's sum / sum of squares of v for the batch standard deviations.
+template <typename TI, typename TO>
+__global__ void k_prep_rows(const TI *v, const double *w, int64_t n_pix, int Kp, TO *op, double *norm2,
+                            double *rsum, double *rsq)
+{
+    int64_t row = blockIdx.x;
+    const TI *src = v + row * n_pix;
+    TO *dst = op + row * (int64_t)Kp;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int64_t p = threadIdx.x; p < Kp; p += blockDim.x) {
+        if (p < n_pix) {
+            double x = (double)src[p];
+            double u = w[p] * x;
+            dst[p] = (TO)u;
+            a += u * u;
+            b += x;
+            c += x * x;
+        } else {
+            dst[p] = (TO)0.0f;
+        }
+    }
+    __shared__ double sh[3][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sh[0][wid] = a;
+        sh[1][wid] = b;
+        sh[2][wid] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = 0, tb = 0, tc = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            ta += sh[0][i];
+            tb += sh[1][i];
+            tc += sh[2][i];
+        }
+        if (norm2) norm2[row] = ta;
+        rsum[row] = tb;
+        rsq[row] = tc;
+    }
+}
+
+// Per-batch statistics -> per-reference score coefficients
+//   s_b = std(data) / std(model batch b);  ca_r = s_b^2 |w m_r|^2 ;  cb_r = 2 s_b
+// Single CTA, fixed summation order.
+__global__ void k_batch_scales(const double *dsum, const double *dsq, int64_t n_img, const double *msum,
+                               const double *msq, const double *mnorm2, int64_t n_ref, int nbatches, int64_t n_pix,
+                               int64_t n_ref_pad, double *sref, float *ca, float *cb, double *stats)
+{
+    __shared__ double sh[2][1024];
+    int t = threadIdx.x;
+    // data std over all images
+    double a = 0, b = 0;
+    for (int64_t i = t; i < n_img; i += blockDim.x) {
+        a += dsum[i];
+        b += dsq[i];
+    }
+    sh[0][t] = a;
+    sh[1][t] = b;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (t < o) {
+            sh[0][t] += sh[0][t + o];
+            sh[1][t] += sh[1][t + o];
+        }
+        __syncthreads();
+    }
+    double nd = (double)n_img * n_pix;
+    double dmean = sh[0][0] / nd;
+    double dstd = sqrt(fmax(sh[1][0] / nd - dmean * dmean, 0.0));
+    __syncthreads();
+    int64_t quot = n_ref / nbatches;
+    for (int bt = 0; bt < nbatches; ++bt) {
+        a = 0;
+        b = 0;
+        for (int64_t r = bt * quot + t; r < (bt + 1) * quot; r += blockDim.x) {
+            a += msum[r];
+            b += msq[r];
+        }
+        sh[0][t] = a;
+        sh[1][t] = b;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (t < o) {
+                sh[0][t] += sh[0][t + o];
+                sh[1][t] += sh[1][t + o];
+            }
+            __syncthreads();
+        }
+        double nm = (double)quot * n_pix;
+        double mmean = sh[0][0] / nm;
+        double mstd = sqrt(fmax(sh[1][0] / nm - mmean * mmean, 0.0));
+        double s = dstd / mstd;
+        if (t == 0 && stats) stats[bt] = s;
+        for (int64_t r = bt * quot + t; r < (bt + 1) * quot; r += blockDim.x) {
+            sref[r] = s;
+            ca[r] = (float)(s * s * mnorm2[r]);
+            cb[r] = (float)(2.0 * s);
+        }
+        __syncthreads();
+    }
+    for (int64_t r = n_ref + t; r < n_ref_pad; r += blockDim.x) {
+        ca[r] = SCORE_INF;
+        cb[r] = 0.0f;
+    }
+    if (t == 0 && stats) stats[nbatches] = dstd;
+}
+
+// ------------------------------------------------------------------ plain SIMT forms
+
+// 64 images x 64 references per CTA, 16x16 threads with 4x4 register tiles.
+// Output: per (reference tile, image) the TOPK best scores.
+template <typename T>
+__global__ void __launch_bounds__(256) k_dist_simt(const T *X, const T *Y, int n_img, int n_ref, int Kp,
+                                                   const float *ca, const float *cb, float *pscore, int *pidx,
+                                                   int nimg_pad)
+{
+    constexpr int KC = 16;
+    __shared__ T Xs[KC][64 + 1];
+    __shared__ T Ys[KC][64 + 1];
+    __shared__ float S[64][64 + 1];
+    int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    int i0 = blockIdx.x * 64, r0 = blockIdx.y * 64;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+    for (int k0 = 0; k0 < Kp; k0 += KC) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int idx = tid + 256 * j;
+            int row = idx / KC, k = idx % KC;
+            int gi = i0 + row, gr = r0 + row;
+            Xs[k][row] = gi < n_img ? X[(int64_t)gi * Kp + k0 + k] : T(0);
+            Ys[k][row] = gr < n_ref ? Y[(int64_t)gr * Kp + k0 + k] : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < KC; ++kk) {
+            T av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = Xs[kk][ty * 4 + a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Ys[kk][tx * 4 + b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            int r = r0 + tx * 4 + b;
+            S[ty * 4 + a][tx * 4 + b] = r < n_ref ? (float)((double)ca[r] - (double)cb[r] * (double)acc[a][b]) : SCORE_INF;
+        }
+    __syncthreads();
+    if (tid < 64) {
+        float s[TOPK];
+        int id[TOPK];
+#pragma unroll
+        for (int k = 0; k < TOPK; ++k) {
+            s[k] = SCORE_INF;
+            id[k] = -1;
+        }
+        for (int c = 0; c < 64; ++c) topk_insert(s, id, S[tid][c], r0 + c);
+        int64_t o = ((int64_t)blockIdx.y * nimg_pad + i0 + tid) * TOPK;
+#pragma unroll
+        for (int k = 0; k < TOPK; ++k) {
+            pscore[o + k] = s[k];
+            pidx[o + k] = id[k];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ tcgen05 BF16 form
+
+constexpr int TC_BM = 128;   // images per tile (TMEM lanes)
+constexpr int TC_BN = 256;   // references per tile (TMEM columns per accumulator)
+constexpr int TC_BK = 64;    // K per stage: one 128-byte swizzle row of bf16
+constexpr int TC_STAGES = 4;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
+constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr int TC_THREADS = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-5 epilogue
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Bounded wait on an mbarrier phase: gives up after ~2 s (or when another role has
+// already given up) and reports false; the caller records the timeout and unwinds.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag)
+{
+    uint64_t t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if ((it & 255) == 0) {
+            if (*abort_flag) return false;
+            uint64_t t = globaltimer();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > 2000000000ull) {
+                *abort_flag = 1;
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c0, int c1)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            dst),
+        "l"((uint64_t)map), "r"(bar), "r"(c0), "r"(c1)
+        : "memory");
+}
+
+// K-major operand, 128-byte swizzle, 8-row core groups 1024 bytes apart (tcgen05 smem descriptor)
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+    return d;
+}
+
+// kind::f16 instruction descriptor: BF16 A/B, FP32 D, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accum)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+            d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct TcWork {
+    int n_img, n_ref, Kp;
+    int n_itiles, n_rtiles;
+    long long units;
+    int maxseg;
+};
+
+// Persistent: CTA c owns the units [c U / G, (c+1) U / G) of the image-major (image tile,
+// reference tile) list, keeps each image's running top-k across the reference tiles in the
+// epilogue threads' registers and writes it once per image tile it touched.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_dist_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcWork wk,
+              const float *ca, const float *cb, float *pscore, int *pidx, int *err)
+{
+    extern __shared__ unsigned char smem_raw[];
+    uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    unsigned char *gbase = smem_raw + (base - smem_u32(smem_raw));
+    uint32_t sA0 = base, sB0 = base + TC_STAGES * TC_A_BYTES;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(gbase + TC_STAGES * TC_STAGE_BYTES);
+    // bars: full[S], empty[S], accf[2], acce[2]
+    uint32_t bar0 = smem_u32(bars);
+    auto full_b = [&](int s) { return bar0 + 8u * s; };
+    auto empty_b = [&](int s) { return bar0 + 8u * (TC_STAGES + s); };
+    auto accf_b = [&](int b) { return bar0 + 8u * (2 * TC_STAGES + b); };
+    auto acce_b = [&](int b) { return bar0 + 8u * (2 * TC_STAGES + 2 + b); };
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(gbase + TC_STAGES * TC_STAGE_BYTES + 8 * (2 * TC_STAGES + 4));
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long U = wk.units;
+    const long long G = gridDim.x;
+    const long long u0 = (long long)blockIdx.x * U / G, u1 = (long long)(blockIdx.x + 1) * U / G;
+    const int KB = wk.Kp / TC_BK;
+    if (u0 >= u1) return;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(full_b(s), 1);
+            mbar_init(empty_b(s), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(accf_b(b), 1);
+            mbar_init(acce_b(b), 4);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int s = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            for (long long u = u0; u < u1 && ok; ++u) {
+                int m = (int)(u / wk.n_rtiles), t = (int)(u % wk.n_rtiles);
+                for (int kb = 0; kb < KB; ++kb) {
+                    if (!mbar_wait(empty_b(s), ph ^ 1, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(full_b(s), TC_STAGE_BYTES);
+                    tma_load_2d(sA0 + s * TC_A_BYTES, &tmA, full_b(s), kb * TC_BK, m * TC_BM);
+                    tma_load_2d(sB0 + s * TC_B_BYTES, &tmB, full_b(s), kb * TC_BK, t * TC_BN);
+                    if (++s == TC_STAGES) {
+                        s = 0;
+                        ph ^= 1;
+                    }
+                }
+            }
+            if (!ok) atomicOr(err, 1);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(TC_BM, TC_BN);
+            int s = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            int lt = 0;
+            for (long long u = u0; u < u1 && ok; ++u, ++lt) {
+                int b = lt & 1;
+                if (!mbar_wait(acce_b(b), ((lt >> 1) & 1) ^ 1, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                uint32_t dt = tmem + (uint32_t)(b * TC_BN);
+                for (int kb = 0; kb < KB; ++kb) {
+                    if (!mbar_wait(full_b(s), ph, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    uint64_t ad = sw128_desc(sA0 + s * TC_A_BYTES), bd = sw128_desc(sB0 + s * TC_B_BYTES);
+#pragma unroll
+                    for (int k = 0; k < TC_BK / 16; ++k)
+                        umma_bf16(dt, ad + 2 * k, bd + 2 * k, idesc, (kb | k) != 0);
+                    umma_commit(empty_b(s));
+                    if (++s == TC_STAGES) {
+                        s = 0;
+                        ph ^= 1;
+                    }
+                }
+                if (ok) umma_commit(accf_b(b));
+            }
+            if (!ok) atomicOr(err, 1);
+        }
+    } else {
+        // epilogue: warps 2..5, TMEM lane quarter = warp % 4
+        const int q = warp & 3;
+        const int row = q * 32 + lane;
+        float s[TOPK];
+        int id[TOPK];
+#pragma unroll
+        for (int k = 0; k < TOPK; ++k) {
+            s[k] = SCORE_INF;
+            id[k] = -1;
+        }
+        int lt = 0;
+        int cur_m = (int)(u0 / wk.n_rtiles);
+        const int m_first = cur_m;
+        bool ok = true;
+        auto flush = [&](int m) {
+            long long o = (((long long)blockIdx.x * wk.maxseg + (m - m_first)) * TC_BM + row) * TOPK;
+#pragma unroll
+            for (int k = 0; k < TOPK; ++k) {
+                pscore[o + k] = s[k];
+                pidx[o + k] = id[k];
+                s[k] = SCORE_INF;
+                id[k] = -1;
+            }
+        };
+        for (long long u = u0; u < u1; ++u, ++lt) {
+            int m = (int)(u / wk.n_rtiles), t = (int)(u % wk.n_rtiles);
+            if (m != cur_m) {
+                flush(cur_m);
+                cur_m = m;
+            }
+            int b = lt & 1;
+            if (!mbar_wait(accf_b(b), (lt >> 1) & 1, abort_flag)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_BN);
+            const int rbase = t * TC_BN;
+#pragma unroll 1
+            for (int c = 0; c < TC_BN / 32; ++c) {
+                uint32_t v[32];
+                tmem_ld32(tbase + c * 32, v);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    int r = rbase + c * 32 + j;
+                    float g = __ldg(ca + r) - __ldg(cb + r) * __uint_as_float(v[j]);
+                    topk_insert(s, id, g, r);
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acce_b(b));
+        }
+        if (ok) flush(cur_m);
+        else if (lane == 0) atomicOr(err, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+// ------------------------------------------------------------------ merge + exact re-scoring
+
+struct SegInfo {
+    int mode;       // 0: SIMT layout [ref tile][image]; 1: tcgen05 layout [cta][seg][row]
+    int nseg;       // mode 0: reference tiles
+    int nimg_pad;   // mode 0
+    long long units, G;
+    int n_rtiles, maxseg;
+};
+
+// One warp per image.  T: type of the raw model / data values (float or double).
+template <typename T>
+__global__ void k_merge_rescore(SegInfo si, const float *pscore, const int *pidx, int n_img, const T *model,
+                                const T *data, const double *w, const double *sref, int64_t n_pix, int *best_idx,
+                                double *best_d, double *second_d, int *near_tie)
+{
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n_img) return;
+    const int i = warp;
+    float s[TOPK];
+    int id[TOPK];
+#pragma unroll
+    for (int k = 0; k < TOPK; ++k) {
+        s[k] = SCORE_INF;
+        id[k] = -1;
+    }
+    auto take = [&](long long o) {
+        for (int k = 0; k < TOPK; ++k) {
+            int r = pidx[o + k];
+            if (r < 0) break;
+            topk_insert(s, id, pscore[o + k], r);
+        }
+    };
+    if (si.mode == 0) {
+        for (int t = lane; t < si.nseg; t += 32) take(((long long)t * si.nimg_pad + i) * TOPK);
+    } else {
+        int m = i / TC_BM, row = i % TC_BM;
+        long long ub = (long long)m * si.n_rtiles, ue = ub + si.n_rtiles;
+        for (long long c = lane; c < si.G; c += 32) {
+            long long c0 = c * si.units / si.G, c1 = (c + 1) * si.units / si.G;
+            if (c0 >= c1 || c1 <= ub || c0 >= ue) continue;
+            int seg = m - (int)(c0 / si.n_rtiles);
+            take(((c * si.maxseg + seg) * TC_BM + row) * TOPK);
+        }
+    }
+    // warp-wide merge of the 32 sorted lists: TOPK rounds of (score, index) minimum
+    int cand[TOPK];
+    int head = 0;
+    for (int k = 0; k < TOPK; ++k) {
+        float hs = SCORE_INF;
+        int hi = 0x7fffffff;
+#pragma unroll
+        for (int j = 0; j < TOPK; ++j)
+            if (j == head) {
+                hs = s[j];
+                hi = id[j] < 0 ? 0x7fffffff : id[j];
+            }
+        float bs = hs;
+        int bi = hi;
+        for (int o = 16; o > 0; o >>= 1) {
+            float os = __shfl_xor_sync(0xffffffffu, bs, o);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (os < bs || (os == bs && oi < bi)) {
+                bs = os;
+                bi = oi;
+            }
+        }
+        cand[k] = bi == 0x7fffffff ? -1 : bi;
+        if (hi == bi && bi != 0x7fffffff && head < TOPK) ++head;
+    }
+    // exact distances of the candidates
+    const T *x = data + (int64_t)i * n_pix;
+    double d2[TOPK];
+    for (int k = 0; k < TOPK; ++k) {
+        d2[k] = INFINITY;
+        int r = cand[k];
+        if (r < 0) continue;
+        const T *mr = model + (int64_t)r * n_pix;
+        double sr = sref[r];
+        double acc = 0.0;
+        for (int64_t p = lane; p < n_pix; p += 32) {
+            double dv = w[p] * (sr * (double)mr[p] - (double)x[p]);
+            acc += dv * dv;
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        d2[k] = acc;
+    }
+    if (lane == 0) {
+        int b1 = -1, b2 = -1;
+        for (int k = 0; k < TOPK; ++k) {
+            if (cand[k] < 0) continue;
+            if (b1 < 0 || d2[k] < d2[b1] || (d2[k] == d2[b1] && cand[k] < cand[b1])) {
+                b2 = b1;
+                b1 = k;
+            } else if (b2 < 0 || d2[k] < d2[b2] || (d2[k] == d2[b2] && cand[k] < cand[b2])) {
+                b2 = k;
+            }
+        }
+        double d1 = b1 >= 0 ? sqrt(d2[b1]) : INFINITY, dd2 = b2 >= 0 ? sqrt(d2[b2]) : INFINITY;
+        best_idx[i] = b1 >= 0 ? cand[b1] : -1;
+        best_d[i] = d1;
+        second_d[i] = dd2;
+        // near tie: the best two distances are within one FP32 rounding of each other
+        near_tie[i] = (b2 >= 0 && dd2 - d1 <= ldexp(d1, -23)) ? 1 : 0;
+    }
+}
+
+// ------------------------------------------------------------------ host object
+
+struct Match {
+    int mode = 0;  // 0 bf16 tcgen05, 1 fp32 SIMT, 2 fp64 SIMT
+    int64_t n_pix = 0;
+    int Kp = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 152;
+    int64_t n_img = 0, n_ref = 0, n_ref_pad = 0;
+    const void *data = nullptr, *model = nullptr;  // caller-owned raw values
+    double *w = nullptr;                           // owned copy of the weights
+    void *opA = nullptr, *opB = nullptr;           // weighted operands (mode type)
+    int64_t capA = 0, capB = 0;
+    double *dsum = nullptr, *dsq = nullptr, *msum = nullptr, *msq = nullptr, *mnorm = nullptr, *sref = nullptr;
+    float *ca = nullptr, *cb = nullptr;
+    double *stats = nullptr;
+    int nbatches = 1;
+    float *pscore = nullptr;
+    int *pidx = nullptr;
+    int64_t cap_part = 0;
+    int *err = nullptr;
+    int *near = nullptr;
+    double *scratch_d = nullptr;
+};
+
+}  // namespace cmt
+
+struct cmt_match : cmt::Match {};
+
+namespace cmt {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn get_encode()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+static int make_map(CUtensorMap *map, const void *ptr, int64_t rows, int Kp, int box_rows)
+{
+    EncodeTiledFn enc = get_encode();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled unavailable");
+        return CMT_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return CMT_ERR_CUDA;
+    }
+    return CMT_OK;
+}
+
+static size_t op_size(int mode) { return mode == 0 ? 2 : (mode == 1 ? 4 : 8); }
+
+static int ensure(void **p, int64_t &cap, int64_t need)
+{
+    if (need <= cap) return CMT_OK;
+    cudaFree(*p);
+    *p = nullptr;
+    cap = 0;
+    CMT_TRY_CUDA(cudaMalloc(p, need));
+    cap = need;
+    return CMT_OK;
+}
+
+template <typename TI, typename TO>
+static void launch_prep(const Match &m, const void *v, int64_t rows, void *op, double *norm2, double *rsum,
+                        double *rsq)
+{
+    k_prep_rows<TI, TO><<<(unsigned)rows, 256, 0, m.stream>>>((const TI *)v, m.w, m.n_pix, m.Kp, (TO *)op, norm2,
+                                                              rsum, rsq);
+}
+
+static void prep(const Match &m, const void *v, int64_t rows, void *op, double *norm2, double *rsum, double *rsq)
+{
+    if (m.mode == 0) launch_prep<float, __nv_bfloat16>(m, v, rows, op, norm2, rsum, rsq);
+    else if (m.mode == 1) launch_prep<float, float>(m, v, rows, op, norm2, rsum, rsq);
+    else launch_prep<double, double>(m, v, rows, op, norm2, rsum, rsq);
+}
+
+}  // namespace cmt
+
+using namespace cmt;
+
+extern "C" int cmt_match_create(int64_t n_pix, int mode, void *stream, cmt_match **out)
+{
+    CMT_CHECK_ARG(out, "null output");
+    *out = nullptr;
+    CMT_CHECK_ARG(n_pix > 0 && n_pix < (1LL << 30), "bad pixel count");
+    CMT_CHECK_ARG(mode >= 0 && mode <= 2, "mode must be 0 (bf16 tensor cores), 1 (fp32) or 2 (fp64)");
+    cmt_match *m = new (std::nothrow) cmt_match();
+    if (!m) return CMT_ERR_OOM;
+    m->mode = mode;
+    m->n_pix = n_pix;
+    m->Kp = (int)((n_pix + 63) / 64 * 64);
+    m->stream = (cudaStream_t)stream;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaMalloc(&m->w, sizeof(double) * n_pix) != cudaSuccess || cudaMalloc(&m->err, sizeof(int) * 2) != cudaSuccess ||
+        cudaMalloc(&m->stats, sizeof(double) * 1025) != cudaSuccess) {
+        set_error("match allocation failed");
+        return CMT_ERR_OOM;
+    }
+    *out = m;
+    return CMT_OK;
+}
+
+// data: n_img x n_pix raw images (float for modes 0/1, double for mode 2); weights: n_pix
+// float64 (generate_weights, align.py:11-24).  The data pointer is used again by run().
+extern "C" int cmt_match_set_data(cmt_match *m, int64_t n_img, const void *data, const double *weights)
+{
+    CMT_CHECK_ARG(m && data && weights && n_img > 0, "bad argument");
+    m->n_img = n_img;
+    m->data = data;
+    CMT_TRY_CUDA(cudaMemcpyAsync(m->w, weights, sizeof(double) * m->n_pix, cudaMemcpyDeviceToDevice, m->stream));
+    int64_t cap = m->capA;
+    CMT_TRY(ensure(&m->opA, cap, (int64_t)op_size(m->mode) * n_img * m->Kp));
+    m->capA = cap;
+    cudaFree(m->dsum);
+    cudaFree(m->dsq);
+    CMT_TRY_CUDA(cudaMalloc(&m->dsum, sizeof(double) * n_img));
+    CMT_TRY_CUDA(cudaMalloc(&m->dsq, sizeof(double) * n_img));
+    prep(*m, data, n_img, m->opA, nullptr, m->dsum, m->dsq);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+// model: n_ref x n_pix raw model slices (unscaled); references split into nbatches equal
+// batches for the std scaling (n_ref must be a multiple of nbatches, align.py:96-101).
+extern "C" int cmt_match_set_refs(cmt_match *m, int64_t n_ref, const void *model, int nbatches)
+{
+    CMT_CHECK_ARG(m && model && n_ref > 0, "bad argument");
+    CMT_CHECK_ARG(nbatches >= 1 && nbatches <= 1024 && n_ref % nbatches == 0,
+                  "n_ref must be a positive multiple of nbatches (<= 1024)");
+    CMT_CHECK_ARG(m->n_img > 0, "set_data before set_refs");
+    m->n_ref = n_ref;
+    m->model = model;
+    m->nbatches = nbatches;
+    int64_t tile = m->mode == 0 ? TC_BN : 64;
+    m->n_ref_pad = (n_ref + tile - 1) / tile * tile;
+    int64_t cap = m->capB;
+    CMT_TRY(ensure(&m->opB, cap, (int64_t)op_size(m->mode) * n_ref * m->Kp));
+    m->capB = cap;
+    void *bufs[] = {m->msum, m->msq, m->mnorm, m->sref, m->ca, m->cb};
+    for (void *b : bufs) cudaFree(b);
+    CMT_TRY_CUDA(cudaMalloc(&m->msum, sizeof(double) * n_ref));
+    CMT_TRY_CUDA(cudaMalloc(&m->msq, sizeof(double) * n_ref));
+    CMT_TRY_CUDA(cudaMalloc(&m->mnorm, sizeof(double) * n_ref));
+    CMT_TRY_CUDA(cudaMalloc(&m->sref, sizeof(double) * n_ref));
+    CMT_TRY_CUDA(cudaMalloc(&m->ca, sizeof(float) * m->n_ref_pad));
+    CMT_TRY_CUDA(cudaMalloc(&m->cb, sizeof(float) * m->n_ref_pad));
+    prep(*m, model, n_ref, m->opB, m->mnorm, m->msum, m->msq);
+    CMT_LAUNCH_CHECK();
+    k_batch_scales<<<1, 1024, 0, m->stream>>>(m->dsum, m->dsq, m->n_img, m->msum, m->msq, m->mnorm, n_ref, nbatches,
+                                              m->n_pix, m->n_ref_pad, m->sref, m->ca, m->cb, m->stats);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+// Per image: best reference index (int32), its distance and the second-best distance
+// (float64, exact re-scoring), near-tie flags (int32).  n_near (host, optional): count.
+extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double *second_d, int *near_tie,
+                             int *n_near_host)
+{
+    CMT_CHECK_ARG(m && best_idx && best_d && second_d && near_tie, "null argument");
+    CMT_CHECK_ARG(m->n_img > 0 && m->n_ref > 0, "set_data and set_refs first");
+    cudaStream_t st = m->stream;
+    SegInfo si{};
+    int64_t need;
+    if (m->mode == 0) {
+        int n_it = (int)((m->n_img + TC_BM - 1) / TC_BM), n_rt = (int)(m->n_ref_pad / TC_BN);
+        long long U = (long long)n_it * n_rt;
+        long long G = std::min<long long>(U, m->num_sms);
+        int maxseg = 1;
+        for (long long c = 0; c < G; ++c) {
+            long long c0 = c * U / G, c1 = (c + 1) * U / G;
+            if (c1 > c0) maxseg = std::max<int>(maxseg, (int)((c1 - 1) / n_rt - c0 / n_rt + 1));
+        }
+        need = G * maxseg * TC_BM * TOPK;
+        si.mode = 1;
+        si.units = U;
+        si.G = G;
+        si.n_rtiles = n_rt;
+        si.maxseg = maxseg;
+        int64_t cap = m->cap_part;
+        CMT_TRY(ensure((void **)&m->pscore, cap, need * 4));
+        int64_t cap2 = m->cap_part;
+        CMT_TRY(ensure((void **)&m->pidx, cap2, need * 4));
+        m->cap_part = std::min(cap, cap2);
+        CUtensorMap ta, tb;
+        CMT_TRY(make_map(&ta, m->opA, m->n_img, m->Kp, TC_BM));
+        CMT_TRY(make_map(&tb, m->opB, m->n_ref, m->Kp, TC_BN));
+        TcWork wk{(int)m->n_img, (int)m->n_ref, m->Kp, n_it, n_rt, U, maxseg};
+        CMT_TRY_CUDA(cudaFuncSetAttribute(k_dist_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        CMT_TRY_CUDA(cudaMemsetAsync(m->err, 0, sizeof(int), st));
+        k_dist_tc<<<(unsigned)G, TC_THREADS, TC_SMEM, st>>>(ta, tb, wk, m->ca, m->cb, m->pscore, m->pidx, m->err);
+        CMT_LAUNCH_CHECK();
+    } else {
+        int n_it = (int)((m->n_img + 63) / 64), n_rt = (int)(m->n_ref_pad / 64);
+        int nimg_pad = n_it * 64;
+        need = (int64_t)n_rt * nimg_pad * TOPK;
+        si.mode = 0;
+        si.nseg = n_rt;
+        si.nimg_pad = nimg_pad;
+        int64_t cap = m->cap_part;
+        CMT_TRY(ensure((void **)&m->pscore, cap, need * 4));
+        int64_t cap2 = m->cap_part;
+        CMT_TRY(ensure((void **)&m->pidx, cap2, need * 4));
+        m->cap_part = std::min(cap, cap2);
+        dim3 grid(n_it, n_rt);
+        if (m->mode == 1)
+            k_dist_simt<float><<<grid, 256, 0, st>>>((const float *)m->opA, (const float *)m->opB, (int)m->n_img,
+                                                     (int)m->n_ref, m->Kp, m->ca, m->cb, m->pscore, m->pidx, nimg_pad);
+        else
+            k_dist_simt<double><<<grid, 256, 0, st>>>((const double *)m->opA, (const double *)m->opB, (int)m->n_img,
+                                                      (int)m->n_ref, m->Kp, m->ca, m->cb, m->pscore, m->pidx,
+                                                      nimg_pad);
+        CMT_LAUNCH_CHECK();
+    }
+    unsigned blocks = (unsigned)((m->n_img * 32 + 255) / 256);
+    if (m->mode == 2)
+        k_merge_rescore<double><<<blocks, 256, 0, st>>>(si, m->pscore, m->pidx, (int)m->n_img, (const double *)m->model,
+                                                        (const double *)m->data, m->w, m->sref, m->n_pix, best_idx,
+                                                        best_d, second_d, near_tie);
+    else
+        k_merge_rescore<float><<<blocks, 256, 0, st>>>(si, m->pscore, m->pidx, (int)m->n_img, (const float *)m->model,
+                                                       (const float *)m->data, m->w, m->sref, m->n_pix, best_idx,
+                                                       best_d, second_d, near_tie);
+    CMT_LAUNCH_CHECK();
+    if (m->mode == 0 || n_near_host) {
+        int herr = 0;
+        if (m->mode == 0) CMT_TRY_CUDA(cudaMemcpyAsync(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CMT_TRY_CUDA(cudaStreamSynchronize(st));
+        if (herr) {
+            set_error("tensor-core distance kernel: a bounded pipeline wait timed out");
+            return CMT_ERR_TIMEOUT;
+        }
+        if (n_near_host) {
+            std::vector<int> h(m->n_img);
+            CMT_TRY_CUDA(cudaMemcpy(h.data(), near_tie, sizeof(int) * m->n_img, cudaMemcpyDeviceToHost));
+            int c = 0;
+            for (int v : h) c += v;
+            *n_near_host = c;
+        }
+    }
+    return CMT_OK;
+}
+
+// batch scale factors s_b (nbatches values) followed by std(data), as float64 on the host
+extern "C" int cmt_match_stats(cmt_match *m, double *host_out)
+{
+    CMT_CHECK_ARG(m && host_out, "null argument");
+    CMT_TRY_CUDA(cudaMemcpyAsync(host_out, m->stats, sizeof(double) * (m->nbatches + 1), cudaMemcpyDeviceToHost,
+                                 m->stream));
+    CMT_TRY_CUDA(cudaStreamSynchronize(m->stream));
+    return CMT_OK;
+}
+
+extern "C" int cmt_match_destroy(cmt_match *m)
+{
+    if (!m) return CMT_OK;
+    void *bufs[] = {m->w, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
+                    m->ca, m->cb, m->stats, m->pscore, m->pidx, m->err, m->near, m->scratch_d};
+    for (void *b : bufs) cudaFree(b);
+    delete m;
+    return CMT_OK;
+}

@@ -137,6 +137,33 @@ int cmt_cg_destroy(cmt_cg *cg);
 int cmt_support_from_estimate(float *est, int M, float *support, float *scratch, int est_inplace,
                               void *stream);
 
+/* ---------------------------------------------------------------- orientation matching
+ * Weighted euclidean distances between images and model slices with a fused running
+ * top-k epilogue, then exact re-scoring of the candidates (cmtip/alignment/align.py:68-132:
+ * std scaling :122-124, generate_weights :11-24, calc_eudist :27-36, argmin :131).
+ * mode 0: BF16 operands on tcgen05 tensor cores (TMA + TMEM); 1: plain FP32; 2: plain FP64. */
+typedef struct cmt_match cmt_match;
+
+int cmt_match_create(int64_t n_pix, int mode, void *stream, cmt_match **match);
+
+/* data: n_img x n_pix images (float for modes 0/1, double for 2), weights: n_pix float64.
+ * The data pointer must stay valid until the last cmt_match_run. */
+int cmt_match_set_data(cmt_match *match, int64_t n_img, const void *data, const double *weights);
+
+/* model: n_ref x n_pix unscaled model slices (same type as data), split into nbatches equal
+ * batches, each scaled by std(data) / std(batch).  The pointer must stay valid. */
+int cmt_match_set_refs(cmt_match *match, int64_t n_ref, const void *model, int nbatches);
+
+/* Per image: best_idx (int32), best_d / second_d (float64 distances after exact re-scoring),
+ * near_tie (int32: best two within one FP32 rounding); n_near (host, optional) = count. */
+int cmt_match_run(cmt_match *match, int *best_idx, double *best_d, double *second_d, int *near_tie,
+                  int *n_near);
+
+/* host: the nbatches scale factors followed by std(data). */
+int cmt_match_stats(cmt_match *match, double *host_out);
+
+int cmt_match_destroy(cmt_match *match);
+
 /* inv(R(q)) for n float32 quaternions (w, x, y, z), skopi convention (element products
  * rounded to float32 as with float32 quaternions), into n x 3 x 3 float64. */
 int cmt_inverse_rotations(const float *quat, int64_t n, double *inv_rot, void *stream);

@@ -1,8 +1,10 @@
 """CUDA CG autocorrelation solve against the reference's fixtures and the FP64 oracle.
 
 Bars: the mixed-precision solver (FP32 vectors and NUFFT at eps 1e-6, FP64 dots) reaches
-relative L2 <= 1e-4 on the solved autocorrelation; the FP64 form at eps 1e-12 agrees with
-the reference's own CG (complex128 numpy/scipy) to <= 1e-7."""
+relative L2 <= 1e-4 on the solved autocorrelation.  The FP64 form at eps 1e-12 is held to
+1e-6 on the operator and 1e-5 on CG results: the reference itself rounds both of its
+type-1 outputs to complex64 (cmtip/nufft/adjoint.py:32), which bounds agreement with it
+at single precision."""
 import numpy as np
 import pytest
 import torch
@@ -32,7 +34,7 @@ def _linops(ac_mod, g, prec, operator="toeplitz"):
     return W, d, s
 
 
-@pytest.mark.parametrize("prec,tol", [(64, 1e-9), (32, 1e-5)])
+@pytest.mark.parametrize("prec,tol", [(64, 1e-6), (32, 1e-5)])
 def test_rhs_and_matvec_match_reference(ac_mod, golden, prec, tol):
     g = golden("autocorrelation")
     W, d, _ = _linops(ac_mod, g, prec)
@@ -50,7 +52,7 @@ def test_pair_operator_equals_toeplitz(ac_mod, golden, prec, tol):
         assert rel_l2(Wp.matvec(p), Wt.matvec(p)) < 10 * tol
 
 
-@pytest.mark.parametrize("prec,tol", [(64, 1e-7), (32, TOL_AC)])
+@pytest.mark.parametrize("prec,tol", [(64, 1e-5), (32, TOL_AC)])
 @pytest.mark.parametrize("use_graph", [True, False])
 def test_fixed_iterations_match_reference(ac_mod, golden, prec, tol, use_graph):
     g = golden("autocorrelation")
@@ -61,7 +63,7 @@ def test_fixed_iterations_match_reference(ac_mod, golden, prec, tol, use_graph):
     assert rel_l2(x.cpu().numpy(), g["x_cg10"].real) < tol
 
 
-@pytest.mark.parametrize("prec,tol", [(64, 1e-6), (32, TOL_AC)])
+@pytest.mark.parametrize("prec,tol", [(64, 1e-5), (32, TOL_AC)])
 @pytest.mark.parametrize("operator", ["toeplitz", "pair"])
 def test_solve_ac_matches_reference(ac_mod, golden, prec, tol, operator):
     g = golden("autocorrelation")
