@@ -21,7 +21,7 @@ from . import _lib
 from .geometry import uniform_quaternions
 from .nufft import DEFAULT_EPS, Plan, _ptr, _stream_ptr, inverse_rotations
 
-MODES = {"bf16": 0, "fp32": 1, "fp64": 2}
+MODES = {"bf16": 0, "fp32": 1, "fp64": 2, "bf16x3": 3}
 
 
 def generate_weights(pixel_position_reciprocal, order=0):

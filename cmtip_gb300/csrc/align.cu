@@ -51,28 +51,8 @@ __device__ __forceinline__ void topk_insert(float (&s)[TOPK], int (&id)[TOPK], f
 
 // ------------------------------------------------------------------ operand preparation
 
-// One CTA per row: u = w . v (FP64), operand row (padded with zeros to Kp), |u|^2, and the
-// row's sum / sum of squares of v for the batch standard deviations.
-template <typename TI, typename TO>
-__global__ void k_prep_rows(const TI *v, const double *w, int64_t n_pix, int Kp, TO *op, double *norm2,
-                            double *rsum, double *rsq)
+__device__ __forceinline__ void block_sum3(double &a, double &b, double &c)
 {
-    int64_t row = blockIdx.x;
-    const TI *src = v + row * n_pix;
-    TO *dst = op + row * (int64_t)Kp;
-    double a = 0.0, b = 0.0, c = 0.0;
-    for (int64_t p = threadIdx.x; p < Kp; p += blockDim.x) {
-        if (p < n_pix) {
-            double x = (double)src[p];
-            double u = w[p] * x;
-            dst[p] = (TO)u;
-            a += u * u;
-            b += x;
-            c += x * x;
-        } else {
-            dst[p] = (TO)0.0f;
-        }
-    }
     __shared__ double sh[3][32];
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(0xffffffffu, a, o);
@@ -93,18 +73,98 @@ __global__ void k_prep_rows(const TI *v, const double *w, int64_t n_pix, int Kp,
             tb += sh[1][i];
             tc += sh[2][i];
         }
-        if (norm2) norm2[row] = ta;
-        rsum[row] = tb;
-        rsq[row] = tc;
+        a = ta;
+        b = tb;
+        c = tc;
     }
 }
 
-// Per-batch statistics -> per-reference score coefficients
-//   s_b = std(data) / std(model batch b);  ca_r = s_b^2 |w m_r|^2 ;  cb_r = 2 s_b
+// One CTA per row: sum and sum of squares of the raw values (batch standard deviations).
+template <typename TI>
+__global__ void k_row_stats(const TI *v, int64_t n_pix, double *rsum, double *rsq)
+{
+    int64_t row = blockIdx.x;
+    const TI *src = v + row * n_pix;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int64_t p = threadIdx.x; p < n_pix; p += blockDim.x) {
+        double x = (double)src[p];
+        a += x;
+        b += x * x;
+    }
+    block_sum3(a, b, c);
+    if (threadIdx.x == 0) {
+        rsum[row] = a;
+        rsq[row] = b;
+    }
+}
+
+// Centre: c_p = mean_i w_p x_ip.  Distances are unchanged when both operands are shifted by
+// the same vector; shifting by the mean weighted image removes the component all images
+// share (the radial intensity fall-off), so the cross term no longer cancels against
+// |x|^2 and reduced-precision operands keep their accuracy on the distance itself.
+template <typename TI>
+__global__ void k_col_mean(const TI *x, const double *w, int64_t n_img, int64_t n_pix, double *c)
+{
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pix) return;
+    double s = 0.0;
+    for (int64_t i = 0; i < n_img; ++i) s += (double)x[i * n_pix + p];
+    c[p] = w[p] * s / (double)n_img;
+}
+
+template <typename TO> __device__ __forceinline__ TO to_op(double v) { return (TO)v; }
+template <> __device__ __forceinline__ __nv_bfloat16 to_op<__nv_bfloat16>(double v) { return __double2bfloat16(v); }
+template <typename TO> __device__ __forceinline__ double from_op(TO v) { return (double)v; }
+template <> __device__ __forceinline__ double from_op<__nv_bfloat16>(__nv_bfloat16 v) { return (double)__bfloat162float(v); }
+
+// One CTA per row: u = scale_row * w . v - c (FP64), written as the GEMM operand row.
+// terms == 1: [u] (Kp wide).  terms == 3 (bf16 only): the split u = hi + lo in bf16 laid
+// out along K so that one GEMM yields hi.hi' + hi.lo' + lo.hi':
+//   side 0 (images):     [hi, hi, lo]      side 1 (references): [hi, lo, hi]
+// Also |u|^2 (of the unrounded values) when norm2 is given.
+template <typename TI, typename TO>
+__global__ void k_build_op(const TI *v, const double *w, const double *c, const double *scale, int64_t n_pix, int Kp,
+                           int terms, int side, TO *op, double *norm2)
+{
+    int64_t row = blockIdx.x;
+    const TI *src = v + row * n_pix;
+    const int64_t ld = (int64_t)Kp * terms;
+    TO *dst = op + row * ld;
+    double sr = scale ? scale[row] : 1.0;
+    double a = 0.0, b = 0.0, cc = 0.0;
+    for (int64_t p = threadIdx.x; p < Kp; p += blockDim.x) {
+        double u = 0.0;
+        if (p < n_pix) u = sr * w[p] * (double)src[p] - c[p];
+        a += u * u;
+        TO hi = to_op<TO>(u);
+        if (terms == 1) {
+            dst[p] = hi;
+        } else {
+            TO lo = to_op<TO>(u - from_op<TO>(hi));
+            dst[p] = hi;
+            dst[Kp + p] = side == 0 ? hi : lo;
+            dst[2 * (int64_t)Kp + p] = side == 0 ? lo : hi;
+        }
+    }
+    block_sum3(a, b, cc);
+    if (threadIdx.x == 0 && norm2) norm2[row] = a;
+}
+
+// score coefficients: g = ca_r - cb_r * (a_r . b_i) with ca_r = |a_r|^2, cb_r = 2; padding
+// columns get +inf so they never enter a candidate list
+__global__ void k_score_coeffs(const double *norm2, int64_t n_ref, int64_t n_ref_pad, float *ca, float *cb)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_ref_pad) return;
+    ca[r] = r < n_ref ? (float)norm2[r] : SCORE_INF;
+    cb[r] = r < n_ref ? 2.0f : 0.0f;
+}
+
+// Per-batch scale s_b = std(data) / std(model batch b) (numpy std, ddof 0), per reference.
 // Single CTA, fixed summation order.
 __global__ void k_batch_scales(const double *dsum, const double *dsq, int64_t n_img, const double *msum,
-                               const double *msq, const double *mnorm2, int64_t n_ref, int nbatches, int64_t n_pix,
-                               int64_t n_ref_pad, double *sref, float *ca, float *cb, double *stats)
+                               const double *msq, int64_t n_ref, int nbatches, int64_t n_pix, double *sref,
+                               double *stats)
 {
     __shared__ double sh[2][1024];
     int t = threadIdx.x;
@@ -151,16 +211,8 @@ __global__ void k_batch_scales(const double *dsum, const double *dsq, int64_t n_
         double mstd = sqrt(fmax(sh[1][0] / nm - mmean * mmean, 0.0));
         double s = dstd / mstd;
         if (t == 0 && stats) stats[bt] = s;
-        for (int64_t r = bt * quot + t; r < (bt + 1) * quot; r += blockDim.x) {
-            sref[r] = s;
-            ca[r] = (float)(s * s * mnorm2[r]);
-            cb[r] = (float)(2.0 * s);
-        }
+        for (int64_t r = bt * quot + t; r < (bt + 1) * quot; r += blockDim.x) sref[r] = s;
         __syncthreads();
-    }
-    for (int64_t r = n_ref + t; r < n_ref_pad; r += blockDim.x) {
-        ca[r] = SCORE_INF;
-        cb[r] = 0.0f;
     }
     if (t == 0 && stats) stats[nbatches] = dstd;
 }
@@ -643,9 +695,11 @@ __global__ void k_merge_rescore(SegInfo si, const float *pscore, const int *pidx
 // ------------------------------------------------------------------ host object
 
 struct Match {
-    int mode = 0;  // 0 bf16 tcgen05, 1 fp32 SIMT, 2 fp64 SIMT
+    int mode = 0;  // 0 bf16 tcgen05, 1 fp32 SIMT, 2 fp64 SIMT, 3 bf16x3 tcgen05
+    int terms = 1; // bf16 terms per product (3: hi.hi + hi.lo + lo.hi laid out along K)
     int64_t n_pix = 0;
     int Kp = 0;
+    double *cen = nullptr;                         // mean weighted image (operand centre)
     cudaStream_t stream = nullptr;
     int num_sms = 152;
     int64_t n_img = 0, n_ref = 0, n_ref_pad = 0;
@@ -689,15 +743,15 @@ static EncodeTiledFn get_encode()
     return fn;
 }
 
-static int make_map(CUtensorMap *map, const void *ptr, int64_t rows, int Kp, int box_rows)
+static int make_map(CUtensorMap *map, const void *ptr, int64_t rows, int64_t Kld, int box_rows)
 {
     EncodeTiledFn enc = get_encode();
     if (!enc) {
         set_error("cuTensorMapEncodeTiled unavailable");
         return CMT_ERR_CUDA;
     }
-    cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+    cuuint64_t dims[2] = {(cuuint64_t)Kld, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)Kld * 2};
     cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, es,
@@ -710,7 +764,7 @@ static int make_map(CUtensorMap *map, const void *ptr, int64_t rows, int Kp, int
     return CMT_OK;
 }
 
-static size_t op_size(int mode) { return mode == 0 ? 2 : (mode == 1 ? 4 : 8); }
+static size_t op_size(int mode) { return (mode == 0 || mode == 3) ? 2 : (mode == 1 ? 4 : 8); }
 
 static int ensure(void **p, int64_t &cap, int64_t need)
 {
@@ -723,19 +777,28 @@ static int ensure(void **p, int64_t &cap, int64_t need)
     return CMT_OK;
 }
 
-template <typename TI, typename TO>
-static void launch_prep(const Match &m, const void *v, int64_t rows, void *op, double *norm2, double *rsum,
-                        double *rsq)
+// operand rows u = scale . w . v - centre for the mode's operand type
+static void build_op(const Match &m, const void *v, int64_t rows, const double *scale, int side, void *op,
+                     double *norm2)
 {
-    k_prep_rows<TI, TO><<<(unsigned)rows, 256, 0, m.stream>>>((const TI *)v, m.w, m.n_pix, m.Kp, (TO *)op, norm2,
-                                                              rsum, rsq);
+    unsigned g = (unsigned)rows;
+    if (m.mode == 0 || m.mode == 3)
+        k_build_op<float, __nv_bfloat16><<<g, 256, 0, m.stream>>>((const float *)v, m.w, m.cen, scale, m.n_pix, m.Kp,
+                                                                  m.terms, side, (__nv_bfloat16 *)op, norm2);
+    else if (m.mode == 1)
+        k_build_op<float, float><<<g, 256, 0, m.stream>>>((const float *)v, m.w, m.cen, scale, m.n_pix, m.Kp, 1, side,
+                                                          (float *)op, norm2);
+    else
+        k_build_op<double, double><<<g, 256, 0, m.stream>>>((const double *)v, m.w, m.cen, scale, m.n_pix, m.Kp, 1,
+                                                            side, (double *)op, norm2);
 }
 
-static void prep(const Match &m, const void *v, int64_t rows, void *op, double *norm2, double *rsum, double *rsq)
+static void row_stats(const Match &m, const void *v, int64_t rows, double *rsum, double *rsq)
 {
-    if (m.mode == 0) launch_prep<float, __nv_bfloat16>(m, v, rows, op, norm2, rsum, rsq);
-    else if (m.mode == 1) launch_prep<float, float>(m, v, rows, op, norm2, rsum, rsq);
-    else launch_prep<double, double>(m, v, rows, op, norm2, rsum, rsq);
+    if (m.mode == 2)
+        k_row_stats<double><<<(unsigned)rows, 256, 0, m.stream>>>((const double *)v, m.n_pix, rsum, rsq);
+    else
+        k_row_stats<float><<<(unsigned)rows, 256, 0, m.stream>>>((const float *)v, m.n_pix, rsum, rsq);
 }
 
 }  // namespace cmt
@@ -747,17 +810,19 @@ extern "C" int cmt_match_create(int64_t n_pix, int mode, void *stream, cmt_match
     CMT_CHECK_ARG(out, "null output");
     *out = nullptr;
     CMT_CHECK_ARG(n_pix > 0 && n_pix < (1LL << 30), "bad pixel count");
-    CMT_CHECK_ARG(mode >= 0 && mode <= 2, "mode must be 0 (bf16 tensor cores), 1 (fp32) or 2 (fp64)");
+    CMT_CHECK_ARG(mode >= 0 && mode <= 3, "mode must be 0 (bf16 tensor cores), 1 (fp32), 2 (fp64) or 3 (bf16x3)");
     cmt_match *m = new (std::nothrow) cmt_match();
     if (!m) return CMT_ERR_OOM;
     m->mode = mode;
+    m->terms = mode == 3 ? 3 : 1;
     m->n_pix = n_pix;
     m->Kp = (int)((n_pix + 63) / 64 * 64);
     m->stream = (cudaStream_t)stream;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaMalloc(&m->w, sizeof(double) * n_pix) != cudaSuccess || cudaMalloc(&m->err, sizeof(int) * 2) != cudaSuccess ||
+    if (cudaMalloc(&m->w, sizeof(double) * n_pix) != cudaSuccess || cudaMalloc(&m->cen, sizeof(double) * n_pix) != cudaSuccess ||
+        cudaMalloc(&m->err, sizeof(int) * 2) != cudaSuccess ||
         cudaMalloc(&m->stats, sizeof(double) * 1025) != cudaSuccess) {
         set_error("match allocation failed");
         return CMT_ERR_OOM;
@@ -775,13 +840,19 @@ extern "C" int cmt_match_set_data(cmt_match *m, int64_t n_img, const void *data,
     m->data = data;
     CMT_TRY_CUDA(cudaMemcpyAsync(m->w, weights, sizeof(double) * m->n_pix, cudaMemcpyDeviceToDevice, m->stream));
     int64_t cap = m->capA;
-    CMT_TRY(ensure(&m->opA, cap, (int64_t)op_size(m->mode) * n_img * m->Kp));
+    CMT_TRY(ensure(&m->opA, cap, (int64_t)op_size(m->mode) * n_img * m->Kp * m->terms));
     m->capA = cap;
     cudaFree(m->dsum);
     cudaFree(m->dsq);
     CMT_TRY_CUDA(cudaMalloc(&m->dsum, sizeof(double) * n_img));
     CMT_TRY_CUDA(cudaMalloc(&m->dsq, sizeof(double) * n_img));
-    prep(*m, data, n_img, m->opA, nullptr, m->dsum, m->dsq);
+    unsigned gp = (unsigned)ceil_div(m->n_pix, 256);
+    if (m->mode == 2)
+        k_col_mean<double><<<gp, 256, 0, m->stream>>>((const double *)data, m->w, n_img, m->n_pix, m->cen);
+    else
+        k_col_mean<float><<<gp, 256, 0, m->stream>>>((const float *)data, m->w, n_img, m->n_pix, m->cen);
+    row_stats(*m, data, n_img, m->dsum, m->dsq);
+    build_op(*m, data, n_img, nullptr, 0, m->opA, nullptr);
     CMT_LAUNCH_CHECK();
     return CMT_OK;
 }
@@ -797,10 +868,10 @@ extern "C" int cmt_match_set_refs(cmt_match *m, int64_t n_ref, const void *model
     m->n_ref = n_ref;
     m->model = model;
     m->nbatches = nbatches;
-    int64_t tile = m->mode == 0 ? TC_BN : 64;
+    int64_t tile = (m->mode == 0 || m->mode == 3) ? TC_BN : 64;
     m->n_ref_pad = (n_ref + tile - 1) / tile * tile;
     int64_t cap = m->capB;
-    CMT_TRY(ensure(&m->opB, cap, (int64_t)op_size(m->mode) * n_ref * m->Kp));
+    CMT_TRY(ensure(&m->opB, cap, (int64_t)op_size(m->mode) * n_ref * m->Kp * m->terms));
     m->capB = cap;
     void *bufs[] = {m->msum, m->msq, m->mnorm, m->sref, m->ca, m->cb};
     for (void *b : bufs) cudaFree(b);
@@ -810,10 +881,11 @@ extern "C" int cmt_match_set_refs(cmt_match *m, int64_t n_ref, const void *model
     CMT_TRY_CUDA(cudaMalloc(&m->sref, sizeof(double) * n_ref));
     CMT_TRY_CUDA(cudaMalloc(&m->ca, sizeof(float) * m->n_ref_pad));
     CMT_TRY_CUDA(cudaMalloc(&m->cb, sizeof(float) * m->n_ref_pad));
-    prep(*m, model, n_ref, m->opB, m->mnorm, m->msum, m->msq);
-    CMT_LAUNCH_CHECK();
-    k_batch_scales<<<1, 1024, 0, m->stream>>>(m->dsum, m->dsq, m->n_img, m->msum, m->msq, m->mnorm, n_ref, nbatches,
-                                              m->n_pix, m->n_ref_pad, m->sref, m->ca, m->cb, m->stats);
+    row_stats(*m, model, n_ref, m->msum, m->msq);
+    k_batch_scales<<<1, 1024, 0, m->stream>>>(m->dsum, m->dsq, m->n_img, m->msum, m->msq, n_ref, nbatches, m->n_pix,
+                                              m->sref, m->stats);
+    build_op(*m, model, n_ref, m->sref, 1, m->opB, m->mnorm);
+    k_score_coeffs<<<ceil_div(m->n_ref_pad, 256), 256, 0, m->stream>>>(m->mnorm, n_ref, m->n_ref_pad, m->ca, m->cb);
     CMT_LAUNCH_CHECK();
     return CMT_OK;
 }
@@ -828,7 +900,7 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
     cudaStream_t st = m->stream;
     SegInfo si{};
     int64_t need;
-    if (m->mode == 0) {
+    if (m->mode == 0 || m->mode == 3) {
         int n_it = (int)((m->n_img + TC_BM - 1) / TC_BM), n_rt = (int)(m->n_ref_pad / TC_BN);
         long long U = (long long)n_it * n_rt;
         long long G = std::min<long long>(U, m->num_sms);
@@ -849,9 +921,10 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
         CMT_TRY(ensure((void **)&m->pidx, cap2, need * 4));
         m->cap_part = std::min(cap, cap2);
         CUtensorMap ta, tb;
-        CMT_TRY(make_map(&ta, m->opA, m->n_img, m->Kp, TC_BM));
-        CMT_TRY(make_map(&tb, m->opB, m->n_ref, m->Kp, TC_BN));
-        TcWork wk{(int)m->n_img, (int)m->n_ref, m->Kp, n_it, n_rt, U, maxseg};
+        int64_t kld = (int64_t)m->Kp * m->terms;
+        CMT_TRY(make_map(&ta, m->opA, m->n_img, kld, TC_BM));
+        CMT_TRY(make_map(&tb, m->opB, m->n_ref, kld, TC_BN));
+        TcWork wk{(int)m->n_img, (int)m->n_ref, (int)kld, n_it, n_rt, U, maxseg};
         CMT_TRY_CUDA(cudaFuncSetAttribute(k_dist_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
         CMT_TRY_CUDA(cudaMemsetAsync(m->err, 0, sizeof(int), st));
         k_dist_tc<<<(unsigned)G, TC_THREADS, TC_SMEM, st>>>(ta, tb, wk, m->ca, m->cb, m->pscore, m->pidx, m->err);
@@ -888,9 +961,9 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
                                                        (const float *)m->data, m->w, m->sref, m->n_pix, best_idx,
                                                        best_d, second_d, near_tie);
     CMT_LAUNCH_CHECK();
-    if (m->mode == 0 || n_near_host) {
+    if (m->mode == 0 || m->mode == 3 || n_near_host) {
         int herr = 0;
-        if (m->mode == 0) CMT_TRY_CUDA(cudaMemcpyAsync(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (m->mode == 0 || m->mode == 3) CMT_TRY_CUDA(cudaMemcpyAsync(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CMT_TRY_CUDA(cudaStreamSynchronize(st));
         if (herr) {
             set_error("tensor-core distance kernel: a bounded pipeline wait timed out");
@@ -920,7 +993,7 @@ extern "C" int cmt_match_stats(cmt_match *m, double *host_out)
 extern "C" int cmt_match_destroy(cmt_match *m)
 {
     if (!m) return CMT_OK;
-    void *bufs[] = {m->w, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
+    void *bufs[] = {m->w, m->cen, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
                     m->ca, m->cb, m->stats, m->pscore, m->pidx, m->err, m->near, m->scratch_d};
     for (void *b : bufs) cudaFree(b);
     delete m;

@@ -53,6 +53,7 @@ struct Cg {
     bool have_big = false, have_small = false;
     cmt_plan *pair_plan = nullptr;
     cudaGraphExec_t graph = nullptr;
+    cudaStream_t cap_stream = nullptr;  // private stream the iteration is captured on
     bool ready = false;
 };
 
@@ -396,6 +397,62 @@ static void cg_destroy(Cg *c)
         cufftDestroy(c->c2r_small);
     }
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+}
+
+// Route every launch of the solver (its kernels, its cuFFT plans, the pair plan) to s.
+static int route_to(Cg &c, cudaStream_t s)
+{
+    c.stream = s;
+    if (c.have_big) {
+        CMT_TRY_CUFFT(cufftSetStream(c.r2c_big, s));
+        CMT_TRY_CUFFT(cufftSetStream(c.c2r_big, s));
+    }
+    if (c.have_small) {
+        CMT_TRY_CUFFT(cufftSetStream(c.r2c_small, s));
+        CMT_TRY_CUFFT(cufftSetStream(c.c2r_small, s));
+    }
+    if (c.pair_plan) CMT_TRY(cmt_plan_set_stream(c.pair_plan, s));
+    return CMT_OK;
+}
+
+// Capture one iteration on the private stream (legacy-default-stream callers cannot be
+// captured) and instantiate it; the graph is then launched on the caller's stream.
+template <typename T> static int iteration(Cg &c);
+
+template <typename T>
+static int capture_iteration(Cg &c)
+{
+    if (c.graph) {
+        cudaGraphExecDestroy(c.graph);
+        c.graph = nullptr;
+    }
+    if (!c.cap_stream) CMT_TRY_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
+    cudaStream_t user = c.stream;
+    CMT_TRY(route_to(c, c.cap_stream));
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c.cap_stream, cudaStreamCaptureModeThreadLocal);
+    int rc = e == cudaSuccess ? iteration<T>(c) : CMT_ERR_CUDA;
+    cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(c.cap_stream, &graph) : e;
+    int rc2 = route_to(c, user);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        set_error("CG graph capture: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+        if (graph) cudaGraphDestroy(graph);
+        return CMT_ERR_CUDA;
+    }
+    if (rc != CMT_OK) {
+        cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (rc2 != CMT_OK) {
+        cudaGraphDestroy(graph);
+        return rc2;
+    }
+    e = cudaGraphInstantiate(&c.graph, graph, 0);
+    cudaGraphDestroy(graph);
+    CMT_TRY_CUDA(e);
+    c.ready = true;
+    return CMT_OK;
 }
 
 }  // namespace cmt
@@ -526,6 +583,7 @@ extern "C" int cmt_cg_set_pair_plan(cmt_cg *c, cmt_plan *plan)
 {
     CMT_CHECK_ARG(c && plan, "null argument");
     CMT_CHECK_ARG(c->op == 1, "pair plan applies to the explicit-pair operator");
+    CMT_TRY(cmt_plan_prepare_pair(plan));
     c->pair_plan = plan;
     c->ready = false;
     return CMT_OK;
@@ -591,21 +649,7 @@ static int solve_impl(Cg &c, const T *d, T *x, int maxiter, double rtol, double 
                                                  &sc->rho);
     CMT_LAUNCH_CHECK();
     if (use_graph) {
-        if (!c.ready) {
-            if (c.graph) {
-                cudaGraphExecDestroy(c.graph);
-                c.graph = nullptr;
-            }
-            cudaGraph_t graph;
-            CMT_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            int rc = iteration<T>(c);
-            cudaError_t e = cudaStreamEndCapture(st, &graph);
-            if (rc != CMT_OK) return rc;
-            CMT_TRY_CUDA(e);
-            CMT_TRY_CUDA(cudaGraphInstantiate(&c.graph, graph, 0));
-            cudaGraphDestroy(graph);
-            c.ready = true;
-        }
+        if (!c.ready) CMT_TRY(capture_iteration<T>(c));
         for (int it = 0; it < maxiter; ++it) CMT_TRY_CUDA(cudaGraphLaunch(c.graph, st));
     } else {
         for (int it = 0; it < maxiter; ++it) CMT_TRY(iteration<T>(c));

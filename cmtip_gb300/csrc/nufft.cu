@@ -1180,6 +1180,27 @@ extern "C" int cmt_execute_pair(cmt_plan *p, const void *fin, void *fout, const 
     return exec_pair<float>(*p, (const float *)fin, (float *)fout, support, scale);
 }
 
+extern "C" int cmt_plan_set_stream(cmt_plan *p, void *stream)
+{
+    CMT_CHECK_ARG(p, "null plan");
+    p->stream = (cudaStream_t)stream;
+    if (p->has_c2c) CMT_TRY_CUFFT(cufftSetStream(p->fft_c2c, p->stream));
+    if (p->has_r2c) CMT_TRY_CUFFT(cufftSetStream(p->fft_r2c, p->stream));
+    if (p->has_c2r) CMT_TRY_CUFFT(cufftSetStream(p->fft_c2r, p->stream));
+    return CMT_OK;
+}
+
+extern "C" int cmt_plan_prepare_pair(cmt_plan *p)
+{
+    CMT_CHECK_ARG(p, "null plan");
+    CMT_TRY(ensure_fft(*p, 0));
+    if (!p->fine2) CMT_TRY_CUDA(cudaMalloc(&p->fine2, 2 * elem(*p) * (size_t)p->n * p->n * p->n));
+    int sm = smem_bytes(*p, 2, true);
+    if (p->prec == 64) CMT_TRY(prep_smem(k_pair<double>, sm));
+    else CMT_TRY(prep_smem(k_pair<float>, sm));
+    return CMT_OK;
+}
+
 extern "C" int cmt_plan_destroy(cmt_plan *p)
 {
     if (!p) return CMT_OK;

@@ -99,6 +99,13 @@ int cmt_execute_pair(cmt_plan *plan, const void *f_in, void *f_out, const float 
 
 int cmt_plan_destroy(cmt_plan *plan);
 
+/* Move the plan (its kernels and its cuFFT plans) to another stream. */
+int cmt_plan_set_stream(cmt_plan *plan, void *stream);
+
+/* Allocate the pair operator's workspace (second fine grid, C2C transform) now, so that a
+ * later cmt_execute_pair allocates nothing (e.g. inside CUDA graph capture). */
+int cmt_plan_prepare_pair(cmt_plan *plan);
+
 /* ---------------------------------------------------------------- CG solve
  * Solver of W x = d, W = alambda * S.conv(T, S x) + rlambda * x + flambda * S.Re(IFFT(FFT(S x).A))
  * (cmtip/autocorrelation/autocorrelation.py:113-173 setup_linops, :150-155 W_matvec) with
@@ -141,7 +148,9 @@ int cmt_support_from_estimate(float *est, int M, float *support, float *scratch,
  * Weighted euclidean distances between images and model slices with a fused running
  * top-k epilogue, then exact re-scoring of the candidates (cmtip/alignment/align.py:68-132:
  * std scaling :122-124, generate_weights :11-24, calc_eudist :27-36, argmin :131).
- * mode 0: BF16 operands on tcgen05 tensor cores (TMA + TMEM); 1: plain FP32; 2: plain FP64. */
+ * mode 0: BF16 operands on tcgen05 tensor cores (TMA + TMEM); 1: plain FP32; 2: plain FP64;
+ * 3: BF16x3 (each operand split into two bf16 terms, hi.hi + hi.lo + lo.hi in one GEMM).
+ * Both operands are centred on the mean weighted image (distances are shift invariant). */
 typedef struct cmt_match cmt_match;
 
 int cmt_match_create(int64_t n_pix, int mode, void *stream, cmt_match **match);

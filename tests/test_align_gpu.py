@@ -15,7 +15,7 @@ from oracle import nufft as on
 from oracle import reference_port as rp
 
 pytestmark = pytest.mark.gpu
-MODES = ["fp64", "fp32", "bf16"]
+MODES = ["fp64", "fp32", "bf16", "bf16x3"]
 
 
 @pytest.fixture(scope="module")
