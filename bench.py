@@ -1,0 +1,502 @@
+#!/usr/bin/env python
+"""Benchmark of the cmtip reconstruction hot path on one GB300 (or N replicas).
+
+Metric (the reference's): seconds per CG iteration of the autocorrelation solve at 5000
+images, M = 81 (plus orientation-matching images/s), mixed precision against this
+project's plain-FP64 GPU form.
+
+Step: one ``solve_ac`` (cmtip/autocorrelation/autocorrelation.py:176-248) on 5000 images x
+4 x 256 x 256 Ewald-sphere pixels (1.31e9 nonuniform points), M = 81, 100 CG iterations
+(the reference's hard-coded maxiter, run to completion: rtol = 0): rotated q-points
+counting-sorted twice (M and 2M fine grids), the Toeplitz kernel (type 1 of ones onto 2M
+modes), the right-hand side (type 1 of the data onto M modes), then 100 graph-replayed CG
+iterations.  value = step time / 100 (setup amortised over the iterations, as a user of
+solve_ac pays it); the pure iteration time, the explicit type-2/type-1 pair operator,
+the NUFFT throughputs, the FP64 form and the alignment rates are reported beside it.
+
+Inputs are synthetic with the reference's shapes: seeded uniform-random quaternions,
+intensities N(0, 1) per point, a 150-Gaussian particle autocorrelation as the estimate.
+--impl reference times the reference's own CPU path for the same step on the host cores
+(bounded sample, scaled; see cpu_reference_step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+CFG = dict(n_img=5000, P=256, M=81, maxiter=100, eps=1e-6, n_atoms=150, radius=12.0, seed=2024)
+ALIGN_CFG = dict(n_img=5000, P=64, M=81, n_ref=20000, noise=0.05, seed=77)
+
+
+# ------------------------------------------------------------------ utilities
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        out.update(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows))
+        return out
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch of a kernel from its committed ncu summary (line
+    'dram_bytes_per_launch: <bytes>'), or None."""
+    path = os.path.join(HERE, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------------ synthetic inputs
+
+def synthetic_geometry(cfg):
+    from cmtip_gb300 import geometry
+    rng = np.random.default_rng(cfg["seed"])
+    ppr, rext = geometry.ewald_detector(cfg["P"])
+    rext = rext / 0.9  # |q|max = 0.9 pi in grid units
+    quats = geometry.random_quaternions(cfg["n_img"], rng).astype(np.float32)
+    rho = geometry.gaussian_particle(cfg["M"], cfg["n_atoms"], cfg["radius"], rng)
+    ac = geometry.autocorrelation_of(rho).astype(np.float32)
+    return ppr, rext, quats, ac
+
+
+# ------------------------------------------------------------------ CPU reference leg
+
+def cpu_reference_step(cfg, n_sample_img=8, n_iter_sample=2):
+    """The reference's solve_ac on the host cores for this step, from a bounded sample:
+    positions (gen_nonuniform_positions) and both type-1 spreads on n_sample_img images
+    (finufft stand-in: the oracle's FP64 ES-kernel NUFFT at eps 1e-7, all cores), scaled
+    linearly to all images; the two uniform-grid FFT/deconvolution stages once; and
+    n_iter_sample iterations of the reference's Toeplitz W_matvec + CG update (numpy
+    complex128, autocorrelation.py:32-63, 88-110, 150-155) scaled to maxiter.
+    Returns (seconds per CG iteration with setup amortised, details)."""
+    from oracle import nufft as on
+    from oracle import reference_port as rp
+    ppr, rext, quats, ac = synthetic_geometry(cfg)
+    M, maxiter = cfg["M"], cfg["maxiter"]
+    n_pix = ppr.shape[-1]
+    n_full = cfg["n_img"] * n_pix
+    rng = np.random.default_rng(1)
+    t0 = time.perf_counter()
+    H, K, L = rp.gen_nonuniform_positions(quats[:n_sample_img], ppr)
+    t_pos = time.perf_counter() - t0
+    xs = [a.astype(np.float32).ravel() / rext * np.pi for a in (H, K, L)]
+    data = rng.standard_normal(xs[0].size)
+    eps = 1e-7
+    w, beta = on.es_params(eps)
+    spread_t, fixed_t = 0.0, 0.0
+    for m_modes, strengths in ((2 * M, np.ones_like(data)), (M, data)):
+        n = on.fine_size(m_modes, w)
+        t0 = time.perf_counter()
+        g = on.spread(*xs, strengths.astype(np.complex128), n, w, beta)
+        spread_t += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        G = np.fft.ifftn(g) * float(n) ** 3
+        idx = on.modes(m_modes) % n
+        p = on._deconv(m_modes, n, w, beta)
+        f = G[np.ix_(idx, idx, idx)] * (p[:, None, None] * p[None, :, None] * p[None, None, :])
+        if m_modes == 2 * M:
+            np.fft.fftn(np.fft.ifftshift(f.real / m_modes ** 3))
+        fixed_t += time.perf_counter() - t0
+        del g, G
+    scale = n_full / data.size
+    # CG iterations with the reference's operator
+    s = rp.solve_ac_inputs(ppr, np.zeros((n_sample_img, 1, n_pix), np.float32), M, quats[:n_sample_img], ac.copy())
+    Fk = np.fft.fftn(np.fft.ifftshift(rng.standard_normal((2 * M,) * 3)))
+    anti = rp.gen_F_antisupport(M)
+    x = s["x0"].astype(np.complex128)
+    r = rng.standard_normal(M ** 3).astype(np.complex128)
+    pvec = r.copy()
+    t0 = time.perf_counter()
+    for _ in range(n_iter_sample):
+        q = (rp.core_problem_convolution(pvec, M, Fk, 2 * M, s["ac_support"]) + 1e-3 * pvec
+             + 1e3 * rp.fourier_reg(pvec, s["ac_support"], anti, M, True))
+        rho = np.vdot(r, r)
+        alpha = rho / np.vdot(pvec, q)
+        x += alpha * pvec
+        r -= alpha * q
+        beta_ = np.vdot(r, r) / rho
+        pvec = r + beta_ * pvec
+    t_iter = (time.perf_counter() - t0) / n_iter_sample
+    total = t_pos * scale + spread_t * scale + fixed_t + maxiter * t_iter
+    details = dict(sample_images=n_sample_img, sample_points=int(data.size), scale=scale,
+                   spread_s_sample=spread_t, fft_deconv_s=fixed_t, positions_s_sample=t_pos,
+                   cg_iteration_s=t_iter, solve_s_estimate=total, eps=eps, width=w)
+    return total / maxiter, details
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def gpu_arm(args):
+    import torch
+    import cmtip_gb300.nufft as nf
+    import cmtip_gb300.autocorrelation as acm
+    import cmtip_gb300.alignment as alm
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    cfg = dict(CFG)
+    if args.small:
+        cfg.update(n_img=200, P=128)
+    M, maxiter = cfg["M"], cfg["maxiter"]
+    ppr, rext, quats, ac = synthetic_geometry(cfg)
+    n_pix = ppr.shape[-1]
+    n_img = cfg["n_img"]
+    N = n_img * n_pix
+    g = torch.Generator(device=dev).manual_seed(cfg["seed"] + rank)
+    slices = torch.randn((n_img, 1, n_pix), generator=g, device=dev, dtype=torch.float32)
+    ppr_d = torch.from_numpy(ppr).to(dev)
+    quats_d = torch.from_numpy(quats).to(dev)
+    est = torch.from_numpy(ac).to(dev)
+
+    nf.PROFILE_KERNELS = True
+
+    def step():
+        return acm.solve_ac(0, ppr_d, rext, slices, M, orientations=quats_d, ac_estimate=est.clone(),
+                            maxiter=maxiter, rtol=0.0, eps=cfg["eps"], verbose=False)
+
+    def barrier():
+        if dist is not None:
+            dist.all_reduce(torch.zeros(1, device=dev))
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    ws = acm._workspace(M, 32, acm.TOEPLITZ, cfg["eps"], dev)
+    for p in ws.plans():
+        p.profile_read()
+    clocks = Clocks(local)
+    barrier()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        step()
+    ev1.record()
+    barrier()
+    clk = clocks.stop()
+    t_step = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    if dist is not None:
+        tt = torch.tensor([t_step], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt)
+    prof = {"2M": ws.plan_2M.profile_read(), "M": ws.plan_M.profile_read()}
+    info2, infoM = ws.plan_2M.info(), ws.plan_M.info()
+
+    out = {}
+    if rank == 0:
+        # dominant kernel: the type-1 spread (two launches per step: ones onto the 2M grid,
+        # data onto the M grid).  Algorithmic bytes per launch: per point 12 B bin-relative
+        # coordinates + 4 B permutation (+ 4 B strength for the data), plus one write of
+        # the real fine grid.
+        spread = {}
+        for key, info, strength_b in (("2M", info2, 0), ("M", infoM, 4)):
+            ms = [t for t, k in prof[key] if k == 1]
+            nfine = info["n_fine"]
+            alg = N * (12 + 4 + strength_b) + nfine * nfine * (nfine + 2) * 4
+            spread[key] = dict(ms=float(np.mean(ms)) if ms else None, launches=len(ms), bytes=alg, n_fine=nfine,
+                               width=info["width"])
+        dom = max(spread.values(), key=lambda s: s["ms"] or 0)
+        peaks = measured_peaks()
+        achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
+        traffic = profile_traffic("k_spread_type1_5000img_M81.md")
+        out["roofline"] = {"bound": "hbm", "kernel": "k_spread<float,false> (type-1 spread, real strengths)",
+                           "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                           "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+                           "peak_source": peaks["source"],
+                           "launch_ms": round(dom["ms"], 3), "algorithmic_bytes": dom["bytes"],
+                           "note": "shared-memory-atomic bound (w^3 adds per point), not HBM bound"}
+        out["spread_kernels"] = spread
+        out["clocks"] = clk
+
+        # ---------------- pure CG iteration (graph replay) and the explicit pair
+        d = torch.randn(M ** 3, device=dev, dtype=torch.float64)
+        x0 = torch.zeros(M ** 3, device=dev, dtype=torch.float64)
+        ws.solver.solve(d, x0, maxiter=3, rtol=0.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ws.solver.solve(d, x0, maxiter=maxiter, rtol=0.0)
+        e1.record()
+        torch.cuda.synchronize()
+        t_cg = e0.elapsed_time(e1) / 1e3 / maxiter
+        extras = {"cg_iteration_s": t_cg, "setup_s": t_step - maxiter * t_cg}
+        if not args.no_extras:
+            extras.update(pair_and_nufft(torch, nf, acm, ws, cfg, dev, N, args))
+            extras.update(fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_step))
+            extras["align"] = align_bench(torch, nf, alm, args)
+        out["extras"] = extras
+
+        # ---------------- end to end through the public API with host buffers
+        slices_h = slices.cpu().pin_memory()
+        quats_h = torch.from_numpy(quats).pin_memory()
+        ppr_h = torch.from_numpy(ppr).pin_memory()
+        est_h = est.cpu().pin_memory()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n_e2e = max(1, min(args.steps, 2))
+        for _ in range(n_e2e):
+            res = acm.solve_ac(0, ppr_h, rext, slices_h, M, orientations=quats_h, ac_estimate=est_h.clone(),
+                               maxiter=maxiter, rtol=0.0, eps=cfg["eps"], verbose=False).cpu()
+        t_e2e = (time.perf_counter() - t0) / n_e2e
+        h2d = slices_h.numel() * 4 + quats_h.numel() * 4 + ppr_h.numel() * 8 + est_h.numel() * 4
+        out["e2e"] = {"value": t_e2e / maxiter, "unit": "s/CG-iteration", "h2d_bytes_per_step": int(h2d),
+                      "d2h_bytes_per_step": int(res.numel() * 8)}
+        # my kernel launches per step: 2 plans x (4 sort + spread + crop), rotations, support (4),
+        # Toeplitz kernel scale + mask, CG start (<= 8), 100 x 5 graph kernels
+        out["gpu_launches"] = args.steps * (2 * 6 + 1 + 4 + 2 + 8 + 5 * maxiter)
+    if dist is not None:
+        dist.destroy_process_group()
+    return t_step, cfg, out, N
+
+
+def pair_and_nufft(torch, nf, acm, ws, cfg, dev, N, args):
+    """Explicit-pair CG iteration and plain type-2 / type-1 throughput on the step's points."""
+    M = cfg["M"]
+    res = {}
+    solver = acm.CGSolver(M, prec=32, op=acm.PAIR)
+    sup = torch.ones(M ** 3, device=dev)
+    solver.set_operator(sup, 1.0, 1e-3, 1e3)
+    solver.set_pair_plan(ws.plan_M)
+    d = torch.randn(M ** 3, device=dev, dtype=torch.float64)
+    x0 = torch.zeros_like(d)
+    solver.solve(d, x0, maxiter=1, rtol=0.0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    solver.solve(d, x0, maxiter=2, rtol=0.0)
+    e1.record()
+    torch.cuda.synchronize()
+    res["cg_pair_iteration_s"] = e0.elapsed_time(e1) / 1e3 / 2
+    solver.close()
+    # type 1 / type 2 on the same 1.31e9 points, complex N(0,1) strengths / modes (eps 1e-6)
+    g = torch.Generator(device=dev).manual_seed(5)
+    c = torch.randn(N, device=dev, dtype=torch.complex64, generator=g)
+    f = ws.plan_M.execute(c)
+    torch.cuda.synchronize()
+    e0.record()
+    f = ws.plan_M.execute(c)
+    e1.record()
+    torch.cuda.synchronize()
+    res["type1_pts_per_s"] = N / (e0.elapsed_time(e1) / 1e3)
+    del c
+    p2 = nf.Plan(2, M, eps=cfg["eps"], isign=-1)
+    ppr_np, rext, quats_np, _ = synthetic_geometry(cfg)
+    p2.set_pts_quat(nf.inverse_rotations(torch.from_numpy(quats_np).to(dev)), torch.from_numpy(ppr_np).to(dev), rext)
+    fm = torch.randn((M,) * 3, device=dev, dtype=torch.complex64, generator=g)
+    out = p2.execute(fm)
+    torch.cuda.synchronize()
+    e0.record()
+    out = p2.execute(fm, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    res["type2_pts_per_s"] = N / (e0.elapsed_time(e1) / 1e3)
+    res["interp_kernel_ms"] = [round(t, 3) for t, k in p2.profile_read() if k == 2]
+    del out
+    p2.close()
+    torch.cuda.empty_cache()
+    return res
+
+
+def fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_mixed):
+    M, maxiter = cfg["M"], cfg["maxiter"]
+    kw = dict(orientations=quats_d, maxiter=maxiter, rtol=0.0, eps=cfg["eps"], verbose=False)
+    ref = acm.solve_ac(0, ppr_d, rext, slices, M, ac_estimate=est.clone(), prec=32, **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ac64 = acm.solve_ac(0, ppr_d, rext, slices, M, ac_estimate=est.clone(), prec=64, **kw)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    err = float(torch.linalg.norm(ref - ac64) / torch.linalg.norm(ac64))
+    acm.clear_workspaces()
+    torch.cuda.empty_cache()
+    return {"fp64_form_s_per_iteration": t64 / maxiter, "speedup_vs_fp64_form": t64 / t_mixed,
+            "ac_rel_l2_mixed_vs_fp64": err}
+
+
+def align_bench(torch, nf, alm, args):
+    """5000 images x 4 x 64^2 pixels (5% multiplicative noise) against 20000 references."""
+    from cmtip_gb300 import geometry
+    cfg = dict(ALIGN_CFG)
+    if args.small:
+        cfg.update(n_img=512, n_ref=4000)
+    rng = np.random.default_rng(cfg["seed"])
+    ppr, rext = geometry.ewald_detector(cfg["P"])
+    rext /= 0.9
+    rho = geometry.gaussian_particle(cfg["M"], CFG["n_atoms"], CFG["radius"], rng)
+    ac = geometry.autocorrelation_of(rho).astype(np.float32)
+    quats = geometry.random_quaternions(cfg["n_img"], rng).astype(np.float32)
+    img = alm.compute_slices(torch.from_numpy(quats), ppr, rext, torch.from_numpy(ac).cuda(), prec=64)
+    n_pix = ppr.shape[-1]
+    img = img.reshape(cfg["n_img"], n_pix)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    img = (img * (1.0 + cfg["noise"] * torch.randn(img.shape, device="cuda", dtype=torch.float64, generator=g)))
+    img = img.float().reshape(cfg["n_img"], 1, n_pix)
+    refs = geometry.uniform_quaternions(cfg["n_ref"])
+    acd = torch.from_numpy(ac).cuda()
+    res = {"n_img": cfg["n_img"], "n_ref": cfg["n_ref"], "n_pix": n_pix}
+    idx = {}
+    for mode in ("bf16", "bf16x3", "fp32", "fp64"):
+        kw = dict(ref_orientations=refs, mode=mode, return_info=True)
+        alm.match_orientations(0, ppr, rext, img, acd, cfg["n_ref"], **kw)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        q, info = alm.match_orientations(0, ppr, rext, img, acd, cfg["n_ref"], **kw)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        idx[mode] = info
+        res[mode] = {"img_per_s": cfg["n_img"] / t, "s": t, "near_ties": info["near_ties"]}
+    a = idx["fp64"]
+    for mode in ("bf16", "bf16x3", "fp32"):
+        b = idx[mode]
+        diff = a["index"] != b["index"]
+        tie = (a["second"] - a["best"]) <= a["best"] * 2.0 ** -23
+        res[mode]["argmin_disagree_vs_fp64"] = int(diff.sum())
+        res[mode]["disagree_outside_fp32_ties"] = int((diff & ~tie).sum())
+    res["speedup_bf16_vs_fp64_form"] = res["fp64"]["s"] / res["bf16"]["s"]
+    return res
+
+
+# ------------------------------------------------------------------ main
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="reduced sizes (smoke runs)")
+    ap.add_argument("--no-extras", action="store_true", help="skip pair/NUFFT/FP64/alignment extras")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    rank, world, _ = rank_info()
+    metric = "CG-iter s & align img/s, 5k imgs M=81: mixed-prec vs FP64 GPU at ≤1e-5 err"
+    cfg = dict(CFG)
+    if args.small:
+        cfg.update(n_img=200, P=128)
+    workload = (f"solve_ac: {cfg['n_img']} images x 4x{cfg['P']}x{cfg['P']} Ewald pixels "
+                f"({cfg['n_img'] * 4 * cfg['P'] ** 2:.3g} points), M={cfg['M']}, {cfg['maxiter']} CG iterations")
+    config = {"workload": workload, "n_images": cfg["n_img"], "pixels_per_image": 4 * cfg["P"] ** 2, "M": cfg["M"],
+              "cg_iterations": cfg["maxiter"], "nufft_eps": cfg["eps"], "operator": "toeplitz",
+              "parallelism": f"replicas{args.gpus}" if args.gpus > 1 else "single-gpu",
+              "l2": "inputs larger than L2 (5.2 GB intensities, 21 GB sorted points per plan)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        v, det = cpu_reference_step(cfg)
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": "s/CG-iteration", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * cfg["maxiter"] * 1e3,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": v, "unit": "s/CG-iteration", "cores": cores(), "kind": "port",
+                                 "sample": f"{det['sample_images']} of {cfg['n_img']} images' spreads scaled x"
+                                           f"{det['scale']:.0f}; 2 CG iterations scaled to {cfg['maxiter']}",
+                                 "details": det},
+                "e2e": {"value": v, "unit": "s/CG-iteration", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    t_step, cfg_used, out, N = gpu_arm(args)
+    if rank != 0:
+        return
+    line = {"metric": metric, "value": t_step / cfg["maxiter"], "unit": "s/CG-iteration", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 dots/norms/alpha/beta)",
+            "data": "synthetic (seeded quaternions, N(0,1) intensities, Gaussian-particle AC estimate)",
+            "config": config}
+    line.update(out)
+    if not args.no_cpu and world == 1:
+        v, det = cpu_reference_step(cfg)
+        line["cpu_baseline"] = {"value": v, "unit": "s/CG-iteration", "cores": cores(), "kind": "port",
+                                "sample": f"{det['sample_images']} of {cfg['n_img']} images' spreads scaled "
+                                          f"x{det['scale']:.0f}; 2 CG iterations scaled to {cfg['maxiter']}",
+                                "details": det}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

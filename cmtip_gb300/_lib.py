@@ -41,6 +41,8 @@ SIGNATURES = {
     "cmt_execute_pair": [_vp, _vp, _vp, _vp, _f64],
     "cmt_plan_destroy": [_vp],
     "cmt_plan_set_stream": [_vp, _vp],
+    "cmt_plan_profile": [_vp, _i32],
+    "cmt_plan_profile_read": [_vp, _vp, _vp, _i32, ctypes.POINTER(_i32)],
     "cmt_plan_prepare_pair": [_vp],
     "cmt_inverse_rotations": [_vp, _i64, _vp, _vp],
     "cmt_cg_create": [_i32, _i32, _i32, _vp, ctypes.POINTER(_vp)],

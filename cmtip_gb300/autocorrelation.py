@@ -181,9 +181,39 @@ def setup_linops(H, K, L, data, ac_support, weights, x0, M, Mtot, N, reciprocal_
     return W, (d.cpu().numpy() if numpy_io else d)
 
 
+class _Workspace:
+    """Plans and solver reused across solve_ac calls with the same (M, prec, operator, eps):
+    the sorted-point buffers, fine grids and cuFFT plans are allocated once."""
+
+    def __init__(self, M, prec, op, eps):
+        self.solver = CGSolver(M, prec=prec, op=op)
+        self.plan_M = Plan(1, M, eps=eps, isign=1, prec=prec)
+        self.plan_2M = Plan(1, 2 * M, eps=eps, isign=1, prec=prec) if op == TOEPLITZ else None
+
+    def plans(self):
+        return [p for p in (self.plan_M, self.plan_2M) if p is not None]
+
+
+_WORKSPACES = {}
+
+
+def _workspace(M, prec, op, eps, dev) -> _Workspace:
+    key = (int(M), int(prec), int(op), float(eps), str(dev), torch.cuda.current_stream().cuda_stream)
+    ws = _WORKSPACES.get(key)
+    if ws is None:
+        if len(_WORKSPACES) >= 4:
+            _WORKSPACES.pop(next(iter(_WORKSPACES)))
+        ws = _WORKSPACES[key] = _Workspace(M, prec, op, eps)
+    return ws
+
+
+def clear_workspaces():
+    _WORKSPACES.clear()
+
+
 def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, M, orientations=None,
              ac_estimate=None, use_gpu=True, use_recip_sym=True, *, maxiter=100, rtol=1e-5, prec=32,
-             operator="toeplitz", eps=DEFAULT_EPS, use_graph=True, return_info=False, rng=None):
+             operator="toeplitz", eps=DEFAULT_EPS, use_graph=True, return_info=False, rng=None, verbose=True):
     """autocorrelation.py:176-248 on the GPU.  Returns the float64 (M, M, M) autocorrelation
     (numpy for numpy inputs, a CUDA tensor for tensor inputs); with ``return_info`` also a
     dict with the iteration count."""
@@ -216,23 +246,21 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
         x0 = est.reshape(-1).to(torch.float64)
     alambda, rlambda, flambda = 1.0, Mtot / N / 1000, 1e3
     op = PAIR if operator == "pair" else TOEPLITZ
-    solver = CGSolver(M, prec=prec, op=op)
+    ws = _workspace(M, prec, op, eps, dev)
+    solver, plan_M, plan_2M = ws.solver, ws.plan_M, ws.plan_2M
     solver.set_operator(sup, alambda, rlambda, flambda)
-    plan_M = Plan(1, M, eps=eps, isign=1, prec=prec)
     plan_M.set_pts_quat(inv_rot, ppr, float(reciprocal_extent))
     if op == TOEPLITZ:
-        plan_2M = Plan(1, 2 * M, eps=eps, isign=1, prec=prec)
         plan_2M.set_pts_quat(inv_rot, ppr, float(reciprocal_extent))
         solver.set_kernel(toeplitz_kernel(plan_2M, M))
-        plan_2M.close()
     else:
         solver.set_pair_plan(plan_M)
-    adb = plan_M.execute(data.to(rt), support=sup, scale=1.0 / float(M) ** 3, real_out=True).reshape(-1)
+    adb = plan_M.execute(data if data.dtype == rt else data.to(rt), support=sup, scale=1.0 / float(M) ** 3,
+                         real_out=True).reshape(-1)
     d = alambda * adb.to(torch.float64) + rlambda * x0
     x, iters = solver.solve(d, x0, maxiter=maxiter, rtol=rtol, use_graph=use_graph)
     ac = x.to(torch.float64).reshape((M,) * 3)
-    solver.close()
-    plan_M.close()
-    print(f"Recovered AC in {iters} iterations.", flush=True)
+    if verbose:
+        print(f"Recovered AC in {iters} iterations.", flush=True)
     out = ac.cpu().numpy() if numpy_io else ac
     return (out, {"iterations": iters}) if return_info else out

@@ -117,7 +117,30 @@ struct Plan {
     void *deconv = nullptr; // |k| -> 1/psi_hat(k h), k = 0 .. M/2 + 1
     cufftHandle fft_c2c = 0, fft_r2c = 0, fft_c2r = 0;
     bool has_c2c = false, has_r2c = false, has_c2r = false;
+
+    // optional per-launch timing of the spread / interp / pair kernels (CUDA events on the
+    // plan's stream, read back after the timed region)
+    static constexpr int PROF_CAP = 256;
+    bool prof = false;
+    cudaEvent_t ev[2 * PROF_CAP] = {};
+    int kind[PROF_CAP] = {};
+    int nev = 0;
 };
+
+enum { PROF_SPREAD = 1, PROF_INTERP = 2, PROF_PAIR = 3 };
+
+static inline void prof_begin(Plan &p)
+{
+    if (p.prof && p.nev < Plan::PROF_CAP) cudaEventRecord(p.ev[2 * p.nev], p.stream);
+}
+
+static inline void prof_end(Plan &p, int kind)
+{
+    if (p.prof && p.nev < Plan::PROF_CAP) {
+        cudaEventRecord(p.ev[2 * p.nev + 1], p.stream);
+        p.kind[p.nev++] = kind;
+    }
+}
 
 }  // namespace cmt
 
@@ -914,10 +937,12 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
         CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * (size_t)n * n * rs, st));
         int sm = smem_bytes(p, 1, false);
         CMT_TRY(prep_smem(k_spread<T, false>, sm));
+        prof_begin(p);
         k_spread<T, false><<<(unsigned)nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
                                                             (T *)p.ux, (T *)p.uy, (T *)p.uz, c, nullptr, n, rs, p.bs,
                                                             p.nb, p.w, p.S, beta, p.maxsub, (T *)p.fine);
         CMT_LAUNCH_CHECK();
+        prof_end(p, PROF_SPREAD);
         if (p.prec == 64)
             CMT_TRY_CUFFT(cufftExecD2Z(p.fft_r2c, (double *)p.fine, (cufftDoubleComplex *)p.fine));
         else
@@ -936,10 +961,12 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
         CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * 2 * (size_t)n * n * n, st));
         int sm = smem_bytes(p, 1, true);
         CMT_TRY(prep_smem(k_spread<T, true>, sm));
+        prof_begin(p);
         k_spread<T, true><<<(unsigned)nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
                                                            (T *)p.ux, (T *)p.uy, (T *)p.uz, c, nullptr, n, n, p.bs,
                                                            p.nb, p.w, p.S, beta, p.maxsub, (T *)p.fine);
         CMT_LAUNCH_CHECK();
+        prof_end(p, PROF_SPREAD);
         int dir = p.isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
         if (p.prec == 64)
             CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
@@ -985,10 +1012,12 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
             CMT_TRY_CUFFT(cufftExecC2R(p.fft_c2r, (cufftComplex *)p.fine, (float *)p.fine));
         int sm = smem_bytes(p, 1, false);
         CMT_TRY(prep_smem(k_interp<T, 2>, sm));
+        prof_begin(p);
         k_interp<T, 2><<<(unsigned)p.nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
                                                           (T *)p.ux, (T *)p.uy, (T *)p.uz, (T *)p.fine, n, n + 2, p.bs,
                                                           p.nb, p.w, p.S, beta, p.maxsub, c);
         CMT_LAUNCH_CHECK();
+        prof_end(p, PROF_INTERP);
     } else {
         CMT_TRY(ensure_fft(p, 0));
         int64_t tot = (int64_t)n * n * n;
@@ -1006,10 +1035,12 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
             CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, dir));
         int sm = smem_bytes(p, 1, true);
         CMT_TRY(prep_smem(k_interp<T, 0>, sm));
+        prof_begin(p);
         k_interp<T, 0><<<(unsigned)p.nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
                                                           (T *)p.ux, (T *)p.uy, (T *)p.uz, (T *)p.fine, n, n, p.bs,
                                                           p.nb, p.w, p.S, beta, p.maxsub, c);
         CMT_LAUNCH_CHECK();
+        prof_end(p, PROF_INTERP);
     }
     return CMT_OK;
 }
@@ -1066,6 +1097,8 @@ static void destroy(Plan *p)
     cudaFree(p->fine);
     cudaFree(p->fine2);
     cudaFree(p->deconv);
+    for (int i = 0; i < 2 * Plan::PROF_CAP; ++i)
+        if (p->ev[i]) cudaEventDestroy(p->ev[i]);
     if (p->has_c2c) cufftDestroy(p->fft_c2c);
     if (p->has_r2c) cufftDestroy(p->fft_r2c);
     if (p->has_c2r) cufftDestroy(p->fft_c2r);
@@ -1178,6 +1211,35 @@ extern "C" int cmt_execute_pair(cmt_plan *p, const void *fin, void *fout, const 
     }
     if (p->prec == 64) return exec_pair<double>(*p, (const double *)fin, (double *)fout, support, scale);
     return exec_pair<float>(*p, (const float *)fin, (float *)fout, support, scale);
+}
+
+// Per-launch timing of the spread / interpolation kernels.  enable != 0 creates the events
+// and starts recording (at most 256 launches until the next read); 0 stops.
+extern "C" int cmt_plan_profile(cmt_plan *p, int enable)
+{
+    CMT_CHECK_ARG(p, "null plan");
+    if (enable && !p->ev[0])
+        for (int i = 0; i < 2 * Plan::PROF_CAP; ++i) CMT_TRY_CUDA(cudaEventCreate(&p->ev[i]));
+    p->prof = enable != 0 && p->ev[0];
+    p->nev = 0;
+    return CMT_OK;
+}
+
+// Read (and clear) the recorded launches: ms[i] duration, kinds[i] 1 spread / 2 interp.
+extern "C" int cmt_plan_profile_read(cmt_plan *p, float *ms, int *kinds, int max, int *count)
+{
+    CMT_CHECK_ARG(p && count, "null argument");
+    int n = std::min(p->nev, max);
+    for (int i = 0; i < n; ++i) {
+        CMT_TRY_CUDA(cudaEventSynchronize(p->ev[2 * i + 1]));
+        float t = 0.f;
+        CMT_TRY_CUDA(cudaEventElapsedTime(&t, p->ev[2 * i], p->ev[2 * i + 1]));
+        if (ms) ms[i] = t;
+        if (kinds) kinds[i] = p->kind[i];
+    }
+    *count = n;
+    p->nev = 0;
+    return CMT_OK;
 }
 
 extern "C" int cmt_plan_set_stream(cmt_plan *p, void *stream)

@@ -25,6 +25,11 @@ from . import _lib
 
 DEFAULT_EPS = 1e-6
 
+# When true, plans created afterwards record per-launch CUDA-event timings of their
+# spread / interpolation kernels (read with Plan.profile_read); benchmarks use this.
+PROFILE_KERNELS = False
+_LIVE_PLANS = None  # weakref.WeakSet of plans created while PROFILE_KERNELS is set
+
 
 def _stream_ptr(stream=None):
     s = stream if stream is not None else torch.cuda.current_stream()
@@ -64,6 +69,25 @@ class Plan:
         self._h = h
         self.N = 0
         self._keep = ()
+        if PROFILE_KERNELS:
+            self.profile(True)
+            global _LIVE_PLANS
+            import weakref
+            if _LIVE_PLANS is None:
+                _LIVE_PLANS = weakref.WeakSet()
+            _LIVE_PLANS.add(self)
+
+    # -- kernel timing
+    def profile(self, enable=True):
+        _lib.call("cmt_plan_profile", self._h, int(bool(enable)))
+
+    def profile_read(self, max_launches=256):
+        """[(ms, kind)] of the spread (kind 1) / interpolation (kind 2) launches since the last read."""
+        ms = (ctypes.c_float * max_launches)()
+        kinds = (ctypes.c_int * max_launches)()
+        n = ctypes.c_int()
+        _lib.call("cmt_plan_profile_read", self._h, ms, kinds, max_launches, ctypes.byref(n))
+        return [(ms[i], kinds[i]) for i in range(n.value)]
 
     # -- info
     def info(self):

@@ -99,6 +99,12 @@ int cmt_execute_pair(cmt_plan *plan, const void *f_in, void *f_out, const float 
 
 int cmt_plan_destroy(cmt_plan *plan);
 
+/* Per-launch CUDA-event timing of the spread / interpolation kernels (enable 0/1), and
+ * read-back of up to max recorded launches (ms, kinds: 1 spread, 2 interp) since the last
+ * read.  Used by benchmarks; recording adds two event records per launch. */
+int cmt_plan_profile(cmt_plan *plan, int enable);
+int cmt_plan_profile_read(cmt_plan *plan, float *ms, int *kinds, int max, int *count);
+
 /* Move the plan (its kernels and its cuFFT plans) to another stream. */
 int cmt_plan_set_stream(cmt_plan *plan, void *stream);
 

@@ -63,7 +63,9 @@ def test_fixed_iterations_match_reference(ac_mod, golden, prec, tol, use_graph):
     assert rel_l2(x.cpu().numpy(), g["x_cg10"].real) < tol
 
 
-@pytest.mark.parametrize("prec,tol", [(64, 1e-5), (32, TOL_AC)])
+# solve_ac stops at ||r|| < 1e-5 ||d|| (scipy's default rtol); stopping one or two iterations
+# apart moves the solution by about that much, so both forms are held to the 1e-4 bar
+@pytest.mark.parametrize("prec,tol", [(64, TOL_AC), (32, TOL_AC)])
 @pytest.mark.parametrize("operator", ["toeplitz", "pair"])
 def test_solve_ac_matches_reference(ac_mod, golden, prec, tol, operator):
     g = golden("autocorrelation")
