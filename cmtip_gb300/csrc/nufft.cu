@@ -393,7 +393,12 @@ __device__ __forceinline__ int kernel_vals(T u, int w, T beta, T *k)
     return l0;
 }
 
-template <typename T> struct Vec2Ops;
+// Bijection of [0, cnt) for cnt <= SCATTER_PRIME: t -> t * P mod cnt (P prime > maxsub).
+constexpr int SCATTER_PRIME = 8191;
+__device__ __forceinline__ int scatter_index(int t, int cnt)
+{
+    return (int)(((long long)t * SCATTER_PRIME) % cnt);
+}
 
 // ------------------------------------------------------------------ spread (type 1)
 
@@ -419,7 +424,10 @@ __global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *s
     const int h = w / 2;
     const T tb = beta;
     for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-        int pos = p0 + t;
+        // Scatter the lane -> point assignment: a bin's list holds runs of neighbouring
+        // pixels (same fine cell, identical windows); handing them to one warp's lanes would
+        // make the 32 shared-memory atomics of an instruction hit the same address.
+        int pos = p0 + scatter_index(t, cnt);
         int j = perm[pos];
         T vr, vi = T(0);
         if (CPLX) {
@@ -587,7 +595,7 @@ __global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub
     int cnt = min(maxsub, bin_count[b] - off);
     int p0 = bin_start[b] + off;
     for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-        int pos = p0 + t;
+        int pos = p0 + scatter_index(t, cnt);  // see k_spread
         T kx[MAXW], ky[MAXW], kz[MAXW];
         int lx = kernel_vals<T>(ux[pos], w, beta, kx) + h;
         int ly = kernel_vals<T>(uy[pos], w, beta, ky) + h;
