@@ -263,4 +263,6 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
     if verbose:
         print(f"Recovered AC in {iters} iterations.", flush=True)
     out = ac.cpu().numpy() if numpy_io else ac
-    return (out, {"iterations": iters}) if return_info else out
+    if return_info:
+        return out, {"iterations": iters, "d": d, "x0": x0, "solver": solver}
+    return out
