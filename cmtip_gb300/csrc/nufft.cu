@@ -98,6 +98,7 @@ struct Plan {
     int type = 1, prec = 32, M = 0, isign = 1;
     double eps = 1e-6, sigma = 2.0;
     int n = 0, w = 0, bs = 8, nb = 0, S = 0;  // fine size, width, bin size, bins/dim, subgrid size
+    int P = 0, ew = 8;                         // subgrid row pitch, z lanes of the warp layout
     double beta = 0.0;
     int maxsub = 2048;
     cudaStream_t stream = nullptr;
@@ -393,261 +394,7 @@ __device__ __forceinline__ int kernel_vals(T u, int w, T beta, T *k)
     return l0;
 }
 
-// Bijection of [0, cnt) for cnt <= SCATTER_PRIME: t -> t * P mod cnt (P prime > maxsub).
-constexpr int SCATTER_PRIME = 8191;
-__device__ __forceinline__ int scatter_index(int t, int cnt)
-{
-    return (int)(((long long)t * SCATTER_PRIME) % cnt);
-}
-
-// ------------------------------------------------------------------ spread (type 1)
-
-// One CTA per subproblem.  CPLX: complex strengths (interleaved), else real.
-// Fine grid: complex n^3 (CPLX) or real with row stride rs (in-place R2C layout).
-template <typename T, bool CPLX>
-__global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *sub_off, const int *bin_count,
-                                                const int *bin_start, const int *perm, const T *ux, const T *uy,
-                                                const T *uz, const T *c, const T *weight, int n, int rs, int bs,
-                                                int nb, int w, int S, T beta, int maxsub, T *fine)
-{
-    extern __shared__ unsigned char smem_raw[];
-    T *sg = reinterpret_cast<T *>(smem_raw);
-    const int nc = CPLX ? 2 : 1;
-    const int cells = S * S * S;
-    for (int i = threadIdx.x; i < cells * nc; i += blockDim.x) sg[i] = T(0);
-    __syncthreads();
-
-    int b = sub_bin[blockIdx.x];
-    int off = sub_off[blockIdx.x];
-    int cnt = min(maxsub, bin_count[b] - off);
-    int p0 = bin_start[b] + off;
-    const int h = w / 2;
-    const T tb = beta;
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-        // Scatter the lane -> point assignment: a bin's list holds runs of neighbouring
-        // pixels (same fine cell, identical windows); handing them to one warp's lanes would
-        // make the 32 shared-memory atomics of an instruction hit the same address.
-        int pos = p0 + scatter_index(t, cnt);
-        int j = perm[pos];
-        T vr, vi = T(0);
-        if (CPLX) {
-            vr = c[2 * (int64_t)j];
-            vi = c[2 * (int64_t)j + 1];
-        } else {
-            vr = c ? c[j] : T(1);
-        }
-        if (weight) {
-            T wj = weight[j];
-            vr *= wj;
-            vi *= wj;
-        }
-        T kx[MAXW], ky[MAXW], kz[MAXW];
-        int lx = kernel_vals<T>(ux[pos], w, tb, kx) + h;
-        int ly = kernel_vals<T>(uy[pos], w, tb, ky) + h;
-        int lz = kernel_vals<T>(uz[pos], w, tb, kz) + h;
-        for (int a = 0; a < w; ++a) {
-            for (int bb = 0; bb < w; ++bb) {
-                T kab = kx[a] * ky[bb];
-                int row = ((lx + a) * S + (ly + bb)) * S + lz;
-                T ar = kab * vr, ai = kab * vi;
-#pragma unroll
-                for (int e = 0; e < MAXW; ++e) {
-                    if (e < w) {
-                        if (CPLX) {
-                            atomicAdd(&sg[2 * (row + e)], ar * kz[e]);
-                            atomicAdd(&sg[2 * (row + e) + 1], ai * kz[e]);
-                        } else {
-                            atomicAdd(&sg[row + e], ar * kz[e]);
-                        }
-                    }
-                }
-            }
-        }
-    }
-    __syncthreads();
-    // flush: bin origin minus halo, periodic wrap
-    int bx = b / (nb * nb), by = (b / nb) % nb, bz = b % nb;
-    int ox = bx * bs - h, oy = by * bs - h, oz = bz * bs - h;
-    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
-        int a = i / (S * S), r = i - a * S * S, bb = r / S, e = r - bb * S;
-        int gx = ox + a, gy = oy + bb, gz = oz + e;
-        gx += gx < 0 ? n : (gx >= n ? -n : 0);
-        gy += gy < 0 ? n : (gy >= n ? -n : 0);
-        gz += gz < 0 ? n : (gz >= n ? -n : 0);
-        if (CPLX) {
-            T vr = sg[2 * i], vi = sg[2 * i + 1];
-            if (vr != T(0) || vi != T(0)) {
-                int64_t g = ((int64_t)gx * n + gy) * n + gz;
-                atomicAdd(&fine[2 * g], vr);
-                atomicAdd(&fine[2 * g + 1], vi);
-            }
-        } else {
-            T v = sg[i];
-            if (v != T(0)) atomicAdd(&fine[((int64_t)gx * n + gy) * rs + gz], v);
-        }
-    }
-}
-
-// ------------------------------------------------------------------ interp (type 2)
-
-// OUT: 0 complex values, 1 real part of complex grid, 2 real grid (values real)
-template <typename T, int OUT>
-__global__ void __launch_bounds__(256) k_interp(const int *sub_bin, const int *sub_off, const int *bin_count,
-                                                const int *bin_start, const int *perm, const T *ux, const T *uy,
-                                                const T *uz, const T *fine, int n, int rs, int bs, int nb, int w,
-                                                int S, T beta, int maxsub, T *out)
-{
-    extern __shared__ unsigned char smem_raw[];
-    T *sg = reinterpret_cast<T *>(smem_raw);
-    const bool cgrid = OUT != 2;
-    const int cells = S * S * S;
-    int b = sub_bin[blockIdx.x];
-    int bx = b / (nb * nb), by = (b / nb) % nb, bz = b % nb;
-    const int h = w / 2;
-    int ox = bx * bs - h, oy = by * bs - h, oz = bz * bs - h;
-    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
-        int a = i / (S * S), r = i - a * S * S, bb = r / S, e = r - bb * S;
-        int gx = ox + a, gy = oy + bb, gz = oz + e;
-        gx += gx < 0 ? n : (gx >= n ? -n : 0);
-        gy += gy < 0 ? n : (gy >= n ? -n : 0);
-        gz += gz < 0 ? n : (gz >= n ? -n : 0);
-        if (cgrid) {
-            int64_t g = ((int64_t)gx * n + gy) * n + gz;
-            sg[2 * i] = fine[2 * g];
-            sg[2 * i + 1] = fine[2 * g + 1];
-        } else {
-            sg[i] = fine[((int64_t)gx * n + gy) * rs + gz];
-        }
-    }
-    __syncthreads();
-    int off = sub_off[blockIdx.x];
-    int cnt = min(maxsub, bin_count[b] - off);
-    int p0 = bin_start[b] + off;
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-        int pos = p0 + t;
-        T kx[MAXW], ky[MAXW], kz[MAXW];
-        int lx = kernel_vals<T>(ux[pos], w, beta, kx) + h;
-        int ly = kernel_vals<T>(uy[pos], w, beta, ky) + h;
-        int lz = kernel_vals<T>(uz[pos], w, beta, kz) + h;
-        T sr = T(0), si = T(0);
-        for (int a = 0; a < w; ++a) {
-            T ar = T(0), ai = T(0);
-            for (int bb = 0; bb < w; ++bb) {
-                int row = ((lx + a) * S + (ly + bb)) * S + lz;
-                T rr = T(0), ri = T(0);
-#pragma unroll
-                for (int e = 0; e < MAXW; ++e) {
-                    if (e < w) {
-                        if (cgrid) {
-                            rr += kz[e] * sg[2 * (row + e)];
-                            if (OUT == 0) ri += kz[e] * sg[2 * (row + e) + 1];
-                        } else {
-                            rr += kz[e] * sg[row + e];
-                        }
-                    }
-                }
-                ar += ky[bb] * rr;
-                ai += ky[bb] * ri;
-            }
-            sr += kx[a] * ar;
-            si += kx[a] * ai;
-        }
-        int j = perm[pos];
-        if (OUT == 0) {
-            out[2 * (int64_t)j] = sr;
-            out[2 * (int64_t)j + 1] = si;
-        } else {
-            out[j] = sr;
-        }
-    }
-}
-
-// ------------------------------------------------------------------ fused pair
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub_off, const int *bin_count,
-                                              const int *bin_start, const T *ux, const T *uy, const T *uz,
-                                              const T *g1, int n, int bs, int nb, int w, int S, T beta, int maxsub,
-                                              T *g2)
-{
-    extern __shared__ unsigned char smem_raw[];
-    const int cells = S * S * S;
-    T *sa = reinterpret_cast<T *>(smem_raw);
-    T *sb = sa + 2 * cells;
-    int b = sub_bin[blockIdx.x];
-    int bx = b / (nb * nb), by = (b / nb) % nb, bz = b % nb;
-    const int h = w / 2;
-    int ox = bx * bs - h, oy = by * bs - h, oz = bz * bs - h;
-    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
-        int a = i / (S * S), r = i - a * S * S, bb = r / S, e = r - bb * S;
-        int gx = ox + a, gy = oy + bb, gz = oz + e;
-        gx += gx < 0 ? n : (gx >= n ? -n : 0);
-        gy += gy < 0 ? n : (gy >= n ? -n : 0);
-        gz += gz < 0 ? n : (gz >= n ? -n : 0);
-        int64_t g = ((int64_t)gx * n + gy) * n + gz;
-        sa[2 * i] = g1[2 * g];
-        sa[2 * i + 1] = g1[2 * g + 1];
-        sb[2 * i] = T(0);
-        sb[2 * i + 1] = T(0);
-    }
-    __syncthreads();
-    int off = sub_off[blockIdx.x];
-    int cnt = min(maxsub, bin_count[b] - off);
-    int p0 = bin_start[b] + off;
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-        int pos = p0 + scatter_index(t, cnt);  // see k_spread
-        T kx[MAXW], ky[MAXW], kz[MAXW];
-        int lx = kernel_vals<T>(ux[pos], w, beta, kx) + h;
-        int ly = kernel_vals<T>(uy[pos], w, beta, ky) + h;
-        int lz = kernel_vals<T>(uz[pos], w, beta, kz) + h;
-        T sr = T(0), si = T(0);
-        for (int a = 0; a < w; ++a) {
-            T ar = T(0), ai = T(0);
-            for (int bb = 0; bb < w; ++bb) {
-                int row = ((lx + a) * S + (ly + bb)) * S + lz;
-                T rr = T(0), ri = T(0);
-#pragma unroll
-                for (int e = 0; e < MAXW; ++e) {
-                    if (e < w) {
-                        rr += kz[e] * sa[2 * (row + e)];
-                        ri += kz[e] * sa[2 * (row + e) + 1];
-                    }
-                }
-                ar += ky[bb] * rr;
-                ai += ky[bb] * ri;
-            }
-            sr += kx[a] * ar;
-            si += kx[a] * ai;
-        }
-        for (int a = 0; a < w; ++a) {
-            for (int bb = 0; bb < w; ++bb) {
-                T kab = kx[a] * ky[bb];
-                int row = ((lx + a) * S + (ly + bb)) * S + lz;
-                T vr = kab * sr, vi = kab * si;
-#pragma unroll
-                for (int e = 0; e < MAXW; ++e) {
-                    if (e < w) {
-                        atomicAdd(&sb[2 * (row + e)], vr * kz[e]);
-                        atomicAdd(&sb[2 * (row + e) + 1], vi * kz[e]);
-                    }
-                }
-            }
-        }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
-        T vr = sb[2 * i], vi = sb[2 * i + 1];
-        if (vr == T(0) && vi == T(0)) continue;
-        int a = i / (S * S), r = i - a * S * S, bb = r / S, e = r - bb * S;
-        int gx = ox + a, gy = oy + bb, gz = oz + e;
-        gx += gx < 0 ? n : (gx >= n ? -n : 0);
-        gy += gy < 0 ? n : (gy >= n ? -n : 0);
-        gz += gz < 0 ? n : (gz >= n ? -n : 0);
-        int64_t g = ((int64_t)gx * n + gy) * n + gz;
-        atomicAdd(&g2[2 * g], vr);
-        atomicAdd(&g2[2 * g + 1], vi);
-    }
-}
+#include "spread_interp.cuh"
 
 // ------------------------------------------------------------------ deconvolution stages
 
@@ -776,6 +523,16 @@ __global__ void k_crop_deconv(const T *spec, const float *support, const T *deco
 
 static size_t elem(const Plan &p) { return p.prec == 64 ? sizeof(double) : sizeof(float); }
 
+// smallest pitch >= S whose residue mod 32 spreads the 32/EW row offsets over distinct banks
+static int padded_pitch(int S, int ew)
+{
+    for (int P = S;; ++P) {
+        int r = P % 32;
+        if (ew == 8 && (r == 8 || r == 24)) return P;
+        if (ew == 16 && r == 16) return P;
+    }
+}
+
 static int choose_params(Plan &p)
 {
     double eps = p.eps;
@@ -792,13 +549,31 @@ static int choose_params(Plan &p)
     p.sigma = sigma;
     p.beta = 0.97 * kPi * w * (1.0 - 0.5 / sigma);
     p.n = next_nice(std::max((int)ceil(sigma * p.M), 2 * w));
-    // bin size: subgrid (bs + w)^3 complex fits two CTAs per SM for the pair kernel
-    size_t e2 = 2 * elem(p);
-    int bs = 16;
-    while (bs > 4 && (size_t)(bs + w) * (bs + w) * (bs + w) * e2 * 2 > 100 * 1024) bs /= 2;
-    p.bs = std::min(bs, p.n);
+    // Warp layout: z offsets over EW lanes (8 for w <= 8, else 16); subgrid rows padded to a
+    // pitch P with P mod 32 = 8/24 (EW 8) or 16 (EW 16) for conflict-free shared access.
+    // Bin size: the largest whose pair-kernel footprint (two complex subgrids) allows two
+    // CTAs per SM; without room for the padding the rows stay unpadded.
+    p.ew = w <= 8 ? 8 : 16;
+    const size_t budget = 100 * 1024;
+    p.bs = 0;
+    for (int pad = 1; pad >= 0 && p.bs == 0; --pad) {
+        for (int bs = 16; bs >= 2 && p.bs == 0; bs /= 2) {
+            int bsc = std::min(bs, p.n);
+            int S = bsc + w;
+            int P = pad ? padded_pitch(S, p.ew) : S;
+            if ((size_t)S * S * P * 4 * elem(p) <= budget) {
+                p.bs = bsc;
+                p.S = S;
+                p.P = P;
+            }
+        }
+    }
+    if (p.bs == 0) {  // very wide kernels: smallest bins, unpadded rows
+        p.bs = 2;
+        p.S = 2 + w;
+        p.P = p.S;
+    }
     p.nb = (p.n + p.bs - 1) / p.bs;
-    p.S = p.bs + w;
     return CMT_OK;
 }
 
@@ -917,15 +692,77 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     return CMT_OK;
 }
 
-static int smem_bytes(const Plan &p, int grids, bool cplx)
-{
-    return p.S * p.S * p.S * (cplx ? 2 : 1) * (int)elem(p) * grids;
-}
+static SubgridGeom geom(const Plan &p, int rs) { return SubgridGeom{p.n, rs, p.bs, p.nb, p.w, p.S, p.P, p.maxsub}; }
+
+// bytes of one channel of one padded subgrid copy
+static size_t sub_bytes(const Plan &p) { return (size_t)p.S * p.S * p.P * elem(p); }
+
+constexpr size_t SMEM_BUDGET = 100 * 1024;  // two CTAs per SM
 
 template <typename K>
 static int prep_smem(K kernel, int bytes)
 {
     if (bytes > 48 * 1024) CMT_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return CMT_OK;
+}
+
+// Spread launcher: real strengths use per-warp private subgrid copies (4 warps) when they
+// fit, complex strengths one shared copy with atomics (8 warps).
+template <typename T, bool CPLX>
+static int launch_spread(Plan &p, const T *c, int rs)
+{
+    size_t one = sub_bytes(p) * (CPLX ? 2 : 1);
+    bool priv = !CPLX && one * 4 <= SMEM_BUDGET;
+    int threads = priv ? 128 : 256;
+    int sm = (int)(priv ? 4 * one : one);
+    SubgridGeom g = geom(p, rs);
+    T beta = (T)p.beta;
+    void (*k)(const int *, const int *, const int *, const int *, const int *, const T *, const T *, const T *,
+              const T *, SubgridGeom, T, T *);
+    if (p.ew == 8) k = priv ? k_spread<T, CPLX, 8, true> : k_spread<T, CPLX, 8, false>;
+    else k = priv ? k_spread<T, CPLX, 16, true> : k_spread<T, CPLX, 16, false>;
+    CMT_TRY(prep_smem(k, sm));
+    prof_begin(p);
+    k<<<(unsigned)p.nsub, threads, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
+                                                    (const T *)p.ux, (const T *)p.uy, (const T *)p.uz, c, g, beta,
+                                                    (T *)p.fine);
+    CMT_LAUNCH_CHECK();
+    prof_end(p, PROF_SPREAD);
+    return CMT_OK;
+}
+
+template <typename T, int OUT>
+static int launch_interp(Plan &p, int rs, T *out)
+{
+    int sm = (int)(sub_bytes(p) * (OUT == 0 ? 2 : 1));
+    SubgridGeom g = geom(p, rs);
+    void (*k)(const int *, const int *, const int *, const int *, const int *, const T *, const T *, const T *,
+              const T *, SubgridGeom, T, T *);
+    k = p.ew == 8 ? k_interp<T, OUT, 8> : k_interp<T, OUT, 16>;
+    CMT_TRY(prep_smem(k, sm));
+    prof_begin(p);
+    k<<<(unsigned)p.nsub, 256, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
+                                                (const T *)p.ux, (const T *)p.uy, (const T *)p.uz, (const T *)p.fine,
+                                                g, (T)p.beta, out);
+    CMT_LAUNCH_CHECK();
+    prof_end(p, PROF_INTERP);
+    return CMT_OK;
+}
+
+template <typename T>
+static int launch_pair(Plan &p, bool prepare_only)
+{
+    int sm = (int)(4 * sub_bytes(p));
+    SubgridGeom g = geom(p, p.n);
+    void (*k)(const int *, const int *, const int *, const int *, const T *, const T *, const T *, const T *,
+              SubgridGeom, T, T *);
+    k = p.ew == 8 ? k_pair<T, 8> : k_pair<T, 16>;
+    CMT_TRY(prep_smem(k, sm));
+    if (prepare_only) return CMT_OK;
+    k<<<(unsigned)p.nsub, 256, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, (const T *)p.ux,
+                                                (const T *)p.uy, (const T *)p.uz, (const T *)p.fine, g, (T)p.beta,
+                                                (T *)p.fine2);
+    CMT_LAUNCH_CHECK();
     return CMT_OK;
 }
 
@@ -943,14 +780,7 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
         CMT_TRY(ensure_fft(p, 1));
         int rs = n + 2;
         CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * (size_t)n * n * rs, st));
-        int sm = smem_bytes(p, 1, false);
-        CMT_TRY(prep_smem(k_spread<T, false>, sm));
-        prof_begin(p);
-        k_spread<T, false><<<(unsigned)nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
-                                                            (T *)p.ux, (T *)p.uy, (T *)p.uz, c, nullptr, n, rs, p.bs,
-                                                            p.nb, p.w, p.S, beta, p.maxsub, (T *)p.fine);
-        CMT_LAUNCH_CHECK();
-        prof_end(p, PROF_SPREAD);
+        CMT_TRY((launch_spread<T, false>(p, c, rs)));
         if (p.prec == 64)
             CMT_TRY_CUFFT(cufftExecD2Z(p.fft_r2c, (double *)p.fine, (cufftDoubleComplex *)p.fine));
         else
@@ -967,14 +797,7 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
     } else {
         CMT_TRY(ensure_fft(p, 0));
         CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * 2 * (size_t)n * n * n, st));
-        int sm = smem_bytes(p, 1, true);
-        CMT_TRY(prep_smem(k_spread<T, true>, sm));
-        prof_begin(p);
-        k_spread<T, true><<<(unsigned)nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
-                                                           (T *)p.ux, (T *)p.uy, (T *)p.uz, c, nullptr, n, n, p.bs,
-                                                           p.nb, p.w, p.S, beta, p.maxsub, (T *)p.fine);
-        CMT_LAUNCH_CHECK();
-        prof_end(p, PROF_SPREAD);
+        CMT_TRY((launch_spread<T, true>(p, c, n)));
         int dir = p.isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
         if (p.prec == 64)
             CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
@@ -1018,14 +841,7 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
             CMT_TRY_CUFFT(cufftExecZ2D(p.fft_c2r, (cufftDoubleComplex *)p.fine, (double *)p.fine));
         else
             CMT_TRY_CUFFT(cufftExecC2R(p.fft_c2r, (cufftComplex *)p.fine, (float *)p.fine));
-        int sm = smem_bytes(p, 1, false);
-        CMT_TRY(prep_smem(k_interp<T, 2>, sm));
-        prof_begin(p);
-        k_interp<T, 2><<<(unsigned)p.nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
-                                                          (T *)p.ux, (T *)p.uy, (T *)p.uz, (T *)p.fine, n, n + 2, p.bs,
-                                                          p.nb, p.w, p.S, beta, p.maxsub, c);
-        CMT_LAUNCH_CHECK();
-        prof_end(p, PROF_INTERP);
+        CMT_TRY((launch_interp<T, 2>(p, n + 2, c)));
     } else {
         CMT_TRY(ensure_fft(p, 0));
         int64_t tot = (int64_t)n * n * n;
@@ -1041,14 +857,7 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
             CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
         else
             CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, dir));
-        int sm = smem_bytes(p, 1, true);
-        CMT_TRY(prep_smem(k_interp<T, 0>, sm));
-        prof_begin(p);
-        k_interp<T, 0><<<(unsigned)p.nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
-                                                          (T *)p.ux, (T *)p.uy, (T *)p.uz, (T *)p.fine, n, n, p.bs,
-                                                          p.nb, p.w, p.S, beta, p.maxsub, c);
-        CMT_LAUNCH_CHECK();
-        prof_end(p, PROF_INTERP);
+        CMT_TRY((launch_interp<T, 0>(p, n, c)));
     }
     return CMT_OK;
 }
@@ -1071,12 +880,7 @@ static int exec_pair(Plan &p, const T *fin, T *fout, const float *support, doubl
     else
         CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, CUFFT_FORWARD));
     CMT_TRY_CUDA(cudaMemsetAsync(p.fine2, 0, 2 * elem(p) * (size_t)n * n * n, st));
-    int sm = smem_bytes(p, 2, true);
-    CMT_TRY(prep_smem(k_pair<T>, sm));
-    k_pair<T><<<(unsigned)p.nsub, 256, sm, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, (T *)p.ux,
-                                                 (T *)p.uy, (T *)p.uz, (T *)p.fine, n, p.bs, p.nb, p.w, p.S,
-                                                 (T)p.beta, p.maxsub, (T *)p.fine2);
-    CMT_LAUNCH_CHECK();
+    CMT_TRY(launch_pair<T>(p, false));
     // A^H: isign +1 (cmtip's adjoint, adjoint.py:33)
     if (p.prec == 64)
         CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine2, (cufftDoubleComplex *)p.fine2, CUFFT_INVERSE));
@@ -1265,9 +1069,8 @@ extern "C" int cmt_plan_prepare_pair(cmt_plan *p)
     CMT_CHECK_ARG(p, "null plan");
     CMT_TRY(ensure_fft(*p, 0));
     if (!p->fine2) CMT_TRY_CUDA(cudaMalloc(&p->fine2, 2 * elem(*p) * (size_t)p->n * p->n * p->n));
-    int sm = smem_bytes(*p, 2, true);
-    if (p->prec == 64) CMT_TRY(prep_smem(k_pair<double>, sm));
-    else CMT_TRY(prep_smem(k_pair<float>, sm));
+    if (p->prec == 64) CMT_TRY(launch_pair<double>(*p, true));
+    else CMT_TRY(launch_pair<float>(*p, true));
     return CMT_OK;
 }
 
