@@ -18,11 +18,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "cmt_common.cuh"
+#include "nufft_plan.cuh"
 
 namespace cmt {
 
@@ -94,58 +96,8 @@ static int next_nice(int n)
 
 // ------------------------------------------------------------------ plan
 
-struct Plan {
-    int type = 1, prec = 32, M = 0, isign = 1;
-    double eps = 1e-6, sigma = 2.0;
-    int n = 0, w = 0, bs = 8, nb = 0, S = 0;  // fine size, width, bin size, bins/dim, subgrid size
-    int P = 0, ew = 8;                         // subgrid row pitch, z lanes of the warp layout
-    double beta = 0.0;
-    int maxsub = 2048;
-    cudaStream_t stream = nullptr;
-
-    int64_t N = 0;
-    int64_t nsub = 0;
-    int *bin_count = nullptr, *bin_start = nullptr, *bin_fill = nullptr;
-    int *sub_bin = nullptr, *sub_off = nullptr;
-    int *perm = nullptr;
-    void *ux = nullptr, *uy = nullptr, *uz = nullptr;  // bin-relative sorted coordinates
-    int64_t cap_pts = 0, cap_sub = 0;
-    int *dflag = nullptr;      // device: range error flag, totals
-    long long *dtot = nullptr; // device: [total subproblems]
-
-    void *fine = nullptr;   // 2 n^3 elements of prec (complex n^3 or padded real)
-    void *fine2 = nullptr;  // second grid for the pair operator
-    void *deconv = nullptr; // |k| -> 1/psi_hat(k h), k = 0 .. M/2 + 1
-    cufftHandle fft_c2c = 0, fft_r2c = 0, fft_c2r = 0;
-    bool has_c2c = false, has_r2c = false, has_c2r = false;
-
-    // optional per-launch timing of the spread / interp / pair kernels (CUDA events on the
-    // plan's stream, read back after the timed region)
-    static constexpr int PROF_CAP = 256;
-    bool prof = false;
-    cudaEvent_t ev[2 * PROF_CAP] = {};
-    int kind[PROF_CAP] = {};
-    int nev = 0;
-};
-
-enum { PROF_SPREAD = 1, PROF_INTERP = 2, PROF_PAIR = 3 };
-
-static inline void prof_begin(Plan &p)
-{
-    if (p.prof && p.nev < Plan::PROF_CAP) cudaEventRecord(p.ev[2 * p.nev], p.stream);
-}
-
-static inline void prof_end(Plan &p, int kind)
-{
-    if (p.prof && p.nev < Plan::PROF_CAP) {
-        cudaEventRecord(p.ev[2 * p.nev + 1], p.stream);
-        p.kind[p.nev++] = kind;
-    }
-}
-
 }  // namespace cmt
 
-struct cmt_plan : cmt::Plan {};
 
 namespace cmt {
 
@@ -394,8 +346,6 @@ __device__ __forceinline__ int kernel_vals(T u, int w, T beta, T *k)
     return l0;
 }
 
-#include "spread_interp.cuh"
-
 // ------------------------------------------------------------------ deconvolution stages
 
 __device__ __forceinline__ int freq_of(int i, int n) { return i <= n / 2 ? i : i - n; }
@@ -521,7 +471,6 @@ __global__ void k_crop_deconv(const T *spec, const float *support, const T *deco
 
 // ------------------------------------------------------------------ host side
 
-static size_t elem(const Plan &p) { return p.prec == 64 ? sizeof(double) : sizeof(float); }
 
 // smallest pitch >= S whose residue mod 32 spreads the 32/EW row offsets over distinct banks
 static int padded_pitch(int S, int ew)
@@ -692,87 +641,12 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     return CMT_OK;
 }
 
-static SubgridGeom geom(const Plan &p, int rs) { return SubgridGeom{p.n, rs, p.bs, p.nb, p.w, p.S, p.P, p.maxsub}; }
-
-// bytes of one channel of one padded subgrid copy
-static size_t sub_bytes(const Plan &p) { return (size_t)p.S * p.S * p.P * elem(p); }
-
-constexpr size_t SMEM_BUDGET = 100 * 1024;  // two CTAs per SM
-
-template <typename K>
-static int prep_smem(K kernel, int bytes)
-{
-    if (bytes > 48 * 1024) CMT_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    return CMT_OK;
-}
-
-// Spread launcher: real strengths use per-warp private subgrid copies (4 warps) when they
-// fit, complex strengths one shared copy with atomics (8 warps).
-template <typename T, bool CPLX>
-static int launch_spread(Plan &p, const T *c, int rs)
-{
-    size_t one = sub_bytes(p) * (CPLX ? 2 : 1);
-    bool priv = !CPLX && one * 4 <= SMEM_BUDGET;
-    int threads = priv ? 128 : 256;
-    int sm = (int)(priv ? 4 * one : one);
-    SubgridGeom g = geom(p, rs);
-    T beta = (T)p.beta;
-    void (*k)(const int *, const int *, const int *, const int *, const int *, const T *, const T *, const T *,
-              const T *, SubgridGeom, T, T *);
-    if (p.ew == 8) k = priv ? k_spread<T, CPLX, 8, true> : k_spread<T, CPLX, 8, false>;
-    else k = priv ? k_spread<T, CPLX, 16, true> : k_spread<T, CPLX, 16, false>;
-    CMT_TRY(prep_smem(k, sm));
-    prof_begin(p);
-    k<<<(unsigned)p.nsub, threads, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
-                                                    (const T *)p.ux, (const T *)p.uy, (const T *)p.uz, c, g, beta,
-                                                    (T *)p.fine);
-    CMT_LAUNCH_CHECK();
-    prof_end(p, PROF_SPREAD);
-    return CMT_OK;
-}
-
-template <typename T, int OUT>
-static int launch_interp(Plan &p, int rs, T *out)
-{
-    int sm = (int)(sub_bytes(p) * (OUT == 0 ? 2 : 1));
-    SubgridGeom g = geom(p, rs);
-    void (*k)(const int *, const int *, const int *, const int *, const int *, const T *, const T *, const T *,
-              const T *, SubgridGeom, T, T *);
-    k = p.ew == 8 ? k_interp<T, OUT, 8> : k_interp<T, OUT, 16>;
-    CMT_TRY(prep_smem(k, sm));
-    prof_begin(p);
-    k<<<(unsigned)p.nsub, 256, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
-                                                (const T *)p.ux, (const T *)p.uy, (const T *)p.uz, (const T *)p.fine,
-                                                g, (T)p.beta, out);
-    CMT_LAUNCH_CHECK();
-    prof_end(p, PROF_INTERP);
-    return CMT_OK;
-}
-
-template <typename T>
-static int launch_pair(Plan &p, bool prepare_only)
-{
-    int sm = (int)(4 * sub_bytes(p));
-    SubgridGeom g = geom(p, p.n);
-    void (*k)(const int *, const int *, const int *, const int *, const T *, const T *, const T *, const T *,
-              SubgridGeom, T, T *);
-    k = p.ew == 8 ? k_pair<T, 8> : k_pair<T, 16>;
-    CMT_TRY(prep_smem(k, sm));
-    if (prepare_only) return CMT_OK;
-    k<<<(unsigned)p.nsub, 256, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, (const T *)p.ux,
-                                                (const T *)p.uy, (const T *)p.uz, (const T *)p.fine, g, (T)p.beta,
-                                                (T *)p.fine2);
-    CMT_LAUNCH_CHECK();
-    return CMT_OK;
-}
-
 template <typename T>
 static int exec_type1(Plan &p, const T *c, T *f, const float *support, double scale, int flags)
 {
     bool real_in = flags & CMT_REAL_IN, real_out = flags & CMT_REAL_OUT, fftord = flags & CMT_MODEORD_FFT;
     cudaStream_t st = p.stream;
     int n = p.n;
-    int64_t nsub = p.nsub;
     T beta = (T)p.beta;
     int M = p.M;
     int64_t mt = (int64_t)M * M * M;
@@ -780,7 +654,7 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
         CMT_TRY(ensure_fft(p, 1));
         int rs = n + 2;
         CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * (size_t)n * n * rs, st));
-        CMT_TRY((launch_spread<T, false>(p, c, rs)));
+        CMT_TRY(launch_spread(p, c, false, rs));
         if (p.prec == 64)
             CMT_TRY_CUFFT(cufftExecD2Z(p.fft_r2c, (double *)p.fine, (cufftDoubleComplex *)p.fine));
         else
@@ -797,7 +671,7 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
     } else {
         CMT_TRY(ensure_fft(p, 0));
         CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * 2 * (size_t)n * n * n, st));
-        CMT_TRY((launch_spread<T, true>(p, c, n)));
+        CMT_TRY(launch_spread(p, c, true, n));
         int dir = p.isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
         if (p.prec == 64)
             CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
@@ -841,7 +715,7 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
             CMT_TRY_CUFFT(cufftExecZ2D(p.fft_c2r, (cufftDoubleComplex *)p.fine, (double *)p.fine));
         else
             CMT_TRY_CUFFT(cufftExecC2R(p.fft_c2r, (cufftComplex *)p.fine, (float *)p.fine));
-        CMT_TRY((launch_interp<T, 2>(p, n + 2, c)));
+        CMT_TRY(launch_interp(p, 2, n + 2, c));
     } else {
         CMT_TRY(ensure_fft(p, 0));
         int64_t tot = (int64_t)n * n * n;
@@ -857,7 +731,7 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
             CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
         else
             CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, dir));
-        CMT_TRY((launch_interp<T, 0>(p, n, c)));
+        CMT_TRY(launch_interp(p, 0, n, c));
     }
     return CMT_OK;
 }
@@ -880,7 +754,7 @@ static int exec_pair(Plan &p, const T *fin, T *fout, const float *support, doubl
     else
         CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, CUFFT_FORWARD));
     CMT_TRY_CUDA(cudaMemsetAsync(p.fine2, 0, 2 * elem(p) * (size_t)n * n * n, st));
-    CMT_TRY(launch_pair<T>(p, false));
+    CMT_TRY(launch_pair(p, false));
     // A^H: isign +1 (cmtip's adjoint, adjoint.py:33)
     if (p.prec == 64)
         CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine2, (cufftDoubleComplex *)p.fine2, CUFFT_INVERSE));
@@ -948,6 +822,9 @@ extern "C" int cmt_plan_create(int type, int M, int prec, double eps, int isign,
     p->sigma = upsampfac > 1.0 ? upsampfac : 2.0;
     p->stream = (cudaStream_t)stream;
     choose_params(*p);
+    // layout override for tuning: CMT_SPREAD_PRIV=1 spreads real strengths into per-warp
+    // private subgrids instead of one subgrid with shared atomics
+    if (const char *env = getenv("CMT_SPREAD_PRIV")) p->spread_priv = atoi(env) != 0;
     int rc = CMT_OK;
     size_t bytes = 2 * elem(*p) * (size_t)p->n * p->n * p->n;
     cudaError_t e = cudaMalloc(&p->fine, bytes);
@@ -1069,8 +946,7 @@ extern "C" int cmt_plan_prepare_pair(cmt_plan *p)
     CMT_CHECK_ARG(p, "null plan");
     CMT_TRY(ensure_fft(*p, 0));
     if (!p->fine2) CMT_TRY_CUDA(cudaMalloc(&p->fine2, 2 * elem(*p) * (size_t)p->n * p->n * p->n));
-    if (p->prec == 64) CMT_TRY(launch_pair<double>(*p, true));
-    else CMT_TRY(launch_pair<float>(*p, true));
+    CMT_TRY(launch_pair(*p, true));
     return CMT_OK;
 }
 

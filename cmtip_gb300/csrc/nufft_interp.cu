@@ -1,0 +1,90 @@
+// Launchers of the interpolation (type 2) and fused pair kernels.
+#include "cmt_common.cuh"
+#include "nufft_plan.cuh"
+
+namespace cmt {
+
+#include "spread_interp.cuh"
+
+namespace {
+
+template <typename T>
+using InterpFn = void (*)(const int *, const int *, const int *, const int *, const int *, const T *, const T *,
+                          const T *, const T *, SubgridGeom, T, T *);
+template <typename T>
+using PairFn = void (*)(const int *, const int *, const int *, const int *, const T *, const T *, const T *,
+                        const T *, SubgridGeom, T, T *);
+
+template <typename T, int OUT>
+InterpFn<T> pick_interp(int w)
+{
+    switch (w) {
+    case 2: return k_interp<T, OUT, 2>;
+    case 3: return k_interp<T, OUT, 3>;
+    case 4: return k_interp<T, OUT, 4>;
+    case 5: return k_interp<T, OUT, 5>;
+    case 6: return k_interp<T, OUT, 6>;
+    case 7: return k_interp<T, OUT, 7>;
+    case 8: return k_interp<T, OUT, 8>;
+    default: return k_interp<T, OUT, 0>;
+    }
+}
+
+template <typename T>
+PairFn<T> pick_pair(int w)
+{
+    switch (w) {
+    case 2: return k_pair<T, 2>;
+    case 3: return k_pair<T, 3>;
+    case 4: return k_pair<T, 4>;
+    case 5: return k_pair<T, 5>;
+    case 6: return k_pair<T, 6>;
+    case 7: return k_pair<T, 7>;
+    case 8: return k_pair<T, 8>;
+    default: return k_pair<T, 0>;
+    }
+}
+
+template <typename T, int OUT>
+int run_interp(Plan &p, int rs, void *out)
+{
+    InterpFn<T> k = pick_interp<T, OUT>(p.w);
+    int sm = (int)(sub_bytes(p) * (OUT == 0 ? 2 : 1));
+    CMT_TRY(prep_smem(k, sm));
+    prof_begin(p);
+    k<<<(unsigned)p.nsub, 256, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
+                                                (const T *)p.ux, (const T *)p.uy, (const T *)p.uz, (const T *)p.fine,
+                                                geom(p, rs), (T)p.beta, (T *)out);
+    CMT_LAUNCH_CHECK();
+    prof_end(p, PROF_INTERP);
+    return CMT_OK;
+}
+
+template <typename T>
+int run_pair(Plan &p, bool prepare_only)
+{
+    PairFn<T> k = pick_pair<T>(p.w);
+    int sm = (int)(4 * sub_bytes(p));
+    CMT_TRY(prep_smem(k, sm));
+    if (prepare_only) return CMT_OK;
+    k<<<(unsigned)p.nsub, 256, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, (const T *)p.ux,
+                                                (const T *)p.uy, (const T *)p.uz, (const T *)p.fine, geom(p, p.n),
+                                                (T)p.beta, (T *)p.fine2);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+}  // namespace
+
+int launch_interp(Plan &p, int out_mode, int rs, void *out)
+{
+    if (p.prec == 64) return out_mode == 0 ? run_interp<double, 0>(p, rs, out) : run_interp<double, 2>(p, rs, out);
+    return out_mode == 0 ? run_interp<float, 0>(p, rs, out) : run_interp<float, 2>(p, rs, out);
+}
+
+int launch_pair(Plan &p, bool prepare_only)
+{
+    return p.prec == 64 ? run_pair<double>(p, prepare_only) : run_pair<float>(p, prepare_only);
+}
+
+}  // namespace cmt
