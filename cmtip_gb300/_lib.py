@@ -33,6 +33,7 @@ _f64 = ctypes.c_double
 # name -> argtypes (restype int unless listed in _RESTYPE)
 SIGNATURES = {
     "cmt_plan_create": [_i32, _i32, _i32, _f64, _i32, _f64, _vp, ctypes.POINTER(_vp)],
+    "cmt_plan_create_derived": [_vp, _i32, _i32, _i32, ctypes.POINTER(_vp)],
     "cmt_plan_info": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_f64),
                       ctypes.POINTER(_i32), ctypes.POINTER(_i64)],
     "cmt_set_pts": [_vp, _i64, _vp, _vp, _vp],

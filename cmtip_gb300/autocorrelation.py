@@ -168,7 +168,7 @@ def setup_linops(H, K, L, data, ac_support, weights, x0, M, Mtot, N, reciprocal_
     solver.set_operator(sup, alambda, rlambda, flambda)
     plan_M = Plan(1, M, eps=eps, isign=1, prec=prec).set_pts(*xs)
     if op == TOEPLITZ:
-        plan_2M = Plan(1, 2 * M, eps=eps, isign=1, prec=prec).set_pts(*xs)
+        plan_2M = plan_M.derive(1, 2 * M, isign=1)
         solver.set_kernel(toeplitz_kernel(plan_2M, M))
         plan_2M.close()
     else:
@@ -188,7 +188,8 @@ class _Workspace:
     def __init__(self, M, prec, op, eps):
         self.solver = CGSolver(M, prec=prec, op=op)
         self.plan_M = Plan(1, M, eps=eps, isign=1, prec=prec)
-        self.plan_2M = Plan(1, 2 * M, eps=eps, isign=1, prec=prec) if op == TOEPLITZ else None
+        # the 2M-mode plan borrows plan_M's sorted points (fine grid exactly twice as fine)
+        self.plan_2M = self.plan_M.derive(1, 2 * M, isign=1) if op == TOEPLITZ else None
 
     def plans(self):
         return [p for p in (self.plan_M, self.plan_2M) if p is not None]
@@ -251,7 +252,6 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
     solver.set_operator(sup, alambda, rlambda, flambda)
     plan_M.set_pts_quat(inv_rot, ppr, float(reciprocal_extent))
     if op == TOEPLITZ:
-        plan_2M.set_pts_quat(inv_rot, ppr, float(reciprocal_extent))
         solver.set_kernel(toeplitz_kernel(plan_2M, M))
     else:
         solver.set_pair_plan(plan_M)

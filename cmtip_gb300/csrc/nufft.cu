@@ -128,7 +128,60 @@ struct QuatSrc {
     const double *ppr;
     int64_t n_pix;
     double rext;
+    const float2 *rot_df;  // FP32 plans: inv_rot and ppr split into double-float pairs
+    const float2 *ppr_df;
+    float2 scale_df;       // pi / rext as a double-float pair
 };
+
+__global__ void k_split_df(const double *in, int64_t n, float2 *out)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = in[i];
+    float h = __double2float_rn(v);
+    out[i] = make_float2(h, __double2float_rn(v - (double)h));
+}
+
+// ---- double-float arithmetic (Dekker 1971, Knuth TAOCP vol. 2): a value carried as an
+// unevaluated float sum hi + lo with ~48 significant bits, for the float64 coordinate
+// chain of the reference at FP32 throughput (GB300's FP64 rate is a small fraction).
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_from(double v)
+{
+    float h = __double2float_rn(v);
+    return DF{h, __double2float_rn(v - (double)h)};
+}
+
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b)
+{
+    float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ DF df_add(DF a, DF b)
+{
+    float s = __fadd_rn(a.hi, b.hi);
+    float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    return df_fast_two_sum(s, e);
+}
+
+__device__ __forceinline__ DF df_mul(DF a, DF b)
+{
+    float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return df_fast_two_sum(p, e);
+}
+
+// float32 of a double-float (hi is already the nearest float of hi + lo unless lo sits on
+// half an ulp, which __fadd_rn resolves)
+__device__ __forceinline__ float df_to_float(DF a) { return __fadd_rn(a.hi, a.lo); }
 
 template <typename T>
 __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, const T *y, const T *z,
@@ -138,6 +191,25 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
         px = x[j];
         py = y[j];
         pz = z[j];
+    } else if (sizeof(T) == 4) {
+        // the chain below in double-float: H = inv(R) . p, float32(H), * (pi / extent), with
+        // the rotations and q-vectors pre-split into (hi, lo) float pairs
+        int64_t img = j / q.n_pix, pix = j - img * q.n_pix;
+        const float2 *R = q.rot_df + 9 * img;
+        float2 a0 = q.ppr_df[pix], a1 = q.ppr_df[q.n_pix + pix], a2 = q.ppr_df[2 * q.n_pix + pix];
+        DF p0{a0.x, a0.y}, p1{a1.x, a1.y}, p2{a2.x, a2.y};
+        DF s{q.scale_df.x, q.scale_df.y};
+        float o[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            float2 r0 = R[3 * r], r1 = R[3 * r + 1], r2 = R[3 * r + 2];
+            DF h = df_add(df_add(df_mul(DF{r0.x, r0.y}, p0), df_mul(DF{r1.x, r1.y}, p1)), df_mul(DF{r2.x, r2.y}, p2));
+            DF hf{df_to_float(h), 0.0f};
+            o[r] = df_to_float(df_mul(hf, s));
+        }
+        px = (T)o[0];
+        py = (T)o[1];
+        pz = (T)o[2];
     } else {
         // float32(inv(R) . p) / reciprocal_extent * pi, as in align.py:52-57 and
         // autocorrelation.py:27,210 + setup_linops :133-135 (products not fused).
@@ -472,6 +544,9 @@ __global__ void k_crop_deconv(const T *spec, const float *support, const T *deco
 // ------------------------------------------------------------------ host side
 
 
+static void unborrow(Plan &p);
+static void sync_borrowed(Plan &p);
+
 // smallest pitch >= S whose residue mod 32 spreads the 32/EW row offsets over distinct banks
 static int padded_pitch(int S, int ew)
 {
@@ -570,6 +645,7 @@ static int grid_for(int64_t N)
 template <typename T>
 static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q)
 {
+    unborrow(p);
     p.N = 0;
     CMT_CHECK_ARG(N > 0 && N <= 0x7fffffffLL, "number of points %lld outside [1, 2^31-1]", (long long)N);
     int nbins = p.nb * p.nb * p.nb;
@@ -766,9 +842,42 @@ static int exec_pair(Plan &p, const T *fin, T *fout, const float *support, doubl
     return CMT_OK;
 }
 
+// a derived plan follows its source's current points (the source may have been given new
+// points since the derivation)
+static void sync_borrowed(Plan &p)
+{
+    const Plan *s = p.points_of;
+    if (!s) return;
+    p.N = s->N;
+    p.nsub = s->nsub;
+    p.bin_count = s->bin_count;
+    p.bin_start = s->bin_start;
+    p.sub_bin = s->sub_bin;
+    p.sub_off = s->sub_off;
+    p.perm = s->perm;
+    p.ux = s->ux;
+    p.uy = s->uy;
+    p.uz = s->uz;
+}
+
+// a plan that borrowed another plan's points drops the borrowed pointers (not its own)
+static void unborrow(Plan &p)
+{
+    if (!p.points_of) return;
+    p.bin_count = p.bin_fill = p.bin_start = p.sub_bin = p.sub_off = p.perm = nullptr;
+    p.ux = p.uy = p.uz = nullptr;
+    p.dflag = nullptr;
+    p.dtot = nullptr;
+    p.cap_pts = p.cap_sub = 0;
+    p.N = p.nsub = 0;
+    p.points_of = nullptr;
+    p.cscale = 1.0;
+}
+
 static void destroy(Plan *p)
 {
     if (!p) return;
+    unborrow(*p);
     cudaFree(p->bin_count);
     cudaFree(p->bin_fill);
     cudaFree(p->bin_start);
@@ -842,6 +951,67 @@ extern "C" int cmt_plan_create(int type, int M, int prec, double eps, int isign,
     return CMT_OK;
 }
 
+// A plan on the points of src with a fine grid exactly twice as fine: bins twice as large
+// (in fine cells) cover the same regions, so src's bin order, permutation and subproblem
+// list apply unchanged and the stored coordinates are scaled by 2 on the fly.  Used for
+// the Toeplitz kernel of the autocorrelation solve (2M modes on the points that the M-mode
+// plan already sorted).  src must keep its points and outlive this plan (or until this
+// plan gets points of its own through set_pts).
+extern "C" int cmt_plan_create_derived(const cmt_plan *src, int type, int M, int isign, cmt_plan **out)
+{
+    CMT_CHECK_ARG(src && out, "null argument");
+    *out = nullptr;
+    CMT_CHECK_ARG(type == 1 || type == 2, "type must be 1 or 2");
+    CMT_CHECK_ARG(isign == 1 || isign == -1, "isign must be +1 or -1");
+    CMT_CHECK_ARG(M >= 1 && 2 * src->n >= 2 * src->w && 2 * src->n > M, "M too large for a grid of %d", 2 * src->n);
+    cmt_plan *p = new (std::nothrow) cmt_plan();
+    if (!p) return CMT_ERR_OOM;
+    p->type = type;
+    p->M = M;
+    p->prec = src->prec;
+    p->eps = src->eps;
+    p->isign = isign;
+    p->stream = src->stream;
+    p->n = 2 * src->n;
+    p->sigma = (double)p->n / M;
+    p->w = src->w;
+    p->beta = src->beta;
+    p->ew = src->ew;
+    p->bs = 2 * src->bs;
+    p->nb = src->nb;
+    p->S = p->bs + p->w;
+    p->P = padded_pitch(p->S, p->ew);
+    p->maxsub = src->maxsub;
+    p->spread_priv = 0;
+    p->points_of = src;
+    p->cscale = 2.0 * src->cscale;
+    p->N = src->N;
+    p->nsub = src->nsub;
+    p->bin_count = src->bin_count;
+    p->bin_start = src->bin_start;
+    p->sub_bin = src->sub_bin;
+    p->sub_off = src->sub_off;
+    p->perm = src->perm;
+    p->ux = src->ux;
+    p->uy = src->uy;
+    p->uz = src->uz;
+    int rc = CMT_OK;
+    size_t bytes = 2 * elem(*p) * (size_t)p->n * p->n * p->n;
+    cudaError_t e = cudaMalloc(&p->fine, bytes);
+    if (e != cudaSuccess) {
+        set_error("fine grid allocation (%zu bytes): %s", bytes, cudaGetErrorString(e));
+        rc = CMT_ERR_OOM;
+    }
+    if (rc == CMT_OK) rc = p->prec == 64 ? upload_deconv<double>(*p) : upload_deconv<float>(*p);
+    if (rc != CMT_OK) {
+        destroy(p);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return CMT_OK;
+}
+
 extern "C" int cmt_plan_info(const cmt_plan *p, int *n_fine, int *width, double *beta, int *bin_size,
                              int64_t *n_sub)
 {
@@ -857,7 +1027,7 @@ extern "C" int cmt_plan_info(const cmt_plan *p, int *n_fine, int *width, double 
 extern "C" int cmt_set_pts(cmt_plan *p, int64_t N, const void *x, const void *y, const void *z)
 {
     CMT_CHECK_ARG(p && x && y && z, "null argument");
-    QuatSrc q{nullptr, nullptr, 1, 1.0};
+    QuatSrc q{nullptr, nullptr, 1, 1.0, nullptr, nullptr, make_float2(0.f, 0.f)};
     if (p->prec == 64) return set_pts_impl<double>(*p, 0, N, (const double *)x, (const double *)y, (const double *)z, q);
     return set_pts_impl<float>(*p, 0, N, (const float *)x, (const float *)y, (const float *)z, q);
 }
@@ -868,10 +1038,23 @@ extern "C" int cmt_set_pts_quat(cmt_plan *p, int64_t n_img, const double *inv_ro
     CMT_CHECK_ARG(p && inv_rot && ppr, "null argument");
     CMT_CHECK_ARG(n_img > 0 && n_pix > 0, "empty image set");
     CMT_CHECK_ARG(rext > 0, "reciprocal_extent must be positive");
-    QuatSrc q{inv_rot, ppr, n_pix, rext};
+    QuatSrc q{inv_rot, ppr, n_pix, rext, nullptr, nullptr, make_float2(0.f, 0.f)};
     int64_t N = n_img * n_pix;
     if (p->prec == 64) return set_pts_impl<double>(*p, 1, N, nullptr, nullptr, nullptr, q);
-    return set_pts_impl<float>(*p, 1, N, nullptr, nullptr, nullptr, q);
+    // FP32 plans evaluate the float64 coordinate chain in double-float arithmetic
+    float2 *split = nullptr;
+    int64_t ns = 9 * n_img + 3 * n_pix;
+    CMT_TRY_CUDA(cudaMallocAsync(&split, sizeof(float2) * ns, p->stream));
+    k_split_df<<<ceil_div(9 * n_img, 256), 256, 0, p->stream>>>(inv_rot, 9 * n_img, split);
+    k_split_df<<<ceil_div(3 * n_pix, 256), 256, 0, p->stream>>>(ppr, 3 * n_pix, split + 9 * n_img);
+    double s = kPi / rext;
+    float sh = (float)s;
+    q.rot_df = split;
+    q.ppr_df = split + 9 * n_img;
+    q.scale_df = make_float2(sh, (float)(s - (double)sh));
+    int rc = set_pts_impl<float>(*p, 1, N, nullptr, nullptr, nullptr, q);
+    cudaFreeAsync(split, p->stream);
+    return rc;
 }
 
 extern "C" int cmt_execute(cmt_plan *p, void *c, void *f, const float *support, double scale, int flags)
@@ -879,6 +1062,7 @@ extern "C" int cmt_execute(cmt_plan *p, void *c, void *f, const float *support, 
     // type 1 with real strengths accepts c == NULL: every strength is 1 (the Toeplitz
     // kernel's adjoint of ones, autocorrelation.py:141-147)
     CMT_CHECK_ARG(p && f && (c || (p->type == 1 && (flags & CMT_REAL_IN))), "null argument");
+    sync_borrowed(*p);
     if (p->N <= 0) {
         set_error("execute before set_pts");
         return CMT_ERR_STATE;
@@ -894,6 +1078,7 @@ extern "C" int cmt_execute(cmt_plan *p, void *c, void *f, const float *support, 
 extern "C" int cmt_execute_pair(cmt_plan *p, const void *fin, void *fout, const float *support, double scale)
 {
     CMT_CHECK_ARG(p && fin && fout, "null argument");
+    sync_borrowed(*p);
     if (p->N <= 0) {
         set_error("execute before set_pts");
         return CMT_ERR_STATE;

@@ -12,6 +12,8 @@ struct Plan {
     int n = 0, w = 0, bs = 8, nb = 0, S = 0;  // fine size, width, bin size, bins/dim, subgrid size
     int P = 0, ew = 8;                         // subgrid row pitch, z lanes of the warp layout
     int spread_priv = 0;                       // real spreading into per-warp private subgrids
+    double cscale = 1.0;                       // coordinate scale of borrowed points
+    const Plan *points_of = nullptr;           // set: the point arrays belong to this plan
     double beta = 0.0;
     int maxsub = 2048;
     cudaStream_t stream = nullptr;
@@ -60,11 +62,15 @@ static inline void prof_end(Plan &p, int kind)
 // Geometry handed to the spreading / interpolation kernels.
 struct SubgridGeom {
     int n, rs, bs, nb, w, S, P, maxsub;
+    float cscale;  // bin-relative coordinates are stored / cscale (derived plans share points)
 };
 
 inline size_t elem(const Plan &p) { return p.prec == 64 ? sizeof(double) : sizeof(float); }
 
-inline SubgridGeom geom(const Plan &p, int rs) { return SubgridGeom{p.n, rs, p.bs, p.nb, p.w, p.S, p.P, p.maxsub}; }
+inline SubgridGeom geom(const Plan &p, int rs)
+{
+    return SubgridGeom{p.n, rs, p.bs, p.nb, p.w, p.S, p.P, p.maxsub, (float)p.cscale};
+}
 
 // bytes of one channel of one padded subgrid copy
 inline size_t sub_bytes(const Plan &p) { return (size_t)p.S * p.S * p.P * elem(p); }

@@ -103,7 +103,8 @@ __global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *s
         const int tl = base + lane;
         const bool valid = tl < t1;
         const int pos = p0 + (valid ? tl : t0);
-        const T mx = ux[pos], my = uy[pos], mz = uz[pos];
+        const T cs = (T)gm.cscale;
+        const T mx = ux[pos] * cs, my = uy[pos] * cs, mz = uz[pos] * cs;
         T mr = T(1), mi = T(0);
         if (c && valid) {
             const int64_t j = perm[pos];
@@ -267,7 +268,8 @@ __global__ void __launch_bounds__(256) k_interp(const int *sub_bin, const int *s
         const int tl = base + lane;
         const bool valid = tl < t1;
         const int pos = p0 + (valid ? tl : t0);
-        const T mx = ux[pos], my = uy[pos], mz = uz[pos];
+        const T cs = (T)gm.cscale;
+        const T mx = ux[pos] * cs, my = uy[pos] * cs, mz = uz[pos] * cs;
         T rr = T(0), ri = T(0);  // lane q keeps point q's result
         const int nq = min(32, t1 - base);
         for (int q = 0; q < nq; ++q) {
@@ -333,7 +335,8 @@ __global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub
     for (int base = t0; base < t1; base += 32) {
         const int tl = base + lane;
         const int pos = p0 + (tl < t1 ? tl : t0);
-        const T mx = ux[pos], my = uy[pos], mz = uz[pos];
+        const T cs = (T)gm.cscale;
+        const T mx = ux[pos] * cs, my = uy[pos] * cs, mz = uz[pos] * cs;
         const int nq = min(32, t1 - base);
         for (int q = 0; q < nq; ++q) {
             const T px = __shfl_sync(0xffffffffu, mx, q);

@@ -67,6 +67,7 @@ class Plan:
             _lib.call("cmt_plan_create", self.type, self.M, self.prec, float(eps), self.isign,
                       float(upsampfac), _stream_ptr(self.stream), ctypes.byref(h))
         self._h = h
+        self._src = None
         self.N = 0
         self._keep = ()
         if PROFILE_KERNELS:
@@ -76,6 +77,30 @@ class Plan:
             if _LIVE_PLANS is None:
                 _LIVE_PLANS = weakref.WeakSet()
             _LIVE_PLANS.add(self)
+
+    @property
+    def N(self):
+        return self._src.N if getattr(self, "_src", None) is not None else self._n
+
+    @N.setter
+    def N(self, value):
+        self._n = value
+
+    def derive(self, nufft_type: int, M: int, isign: int | None = None) -> "Plan":
+        """A plan on this plan's points with a fine grid twice as fine (no second sort):
+        used for the Toeplitz kernel on 2M modes.  Keeps this plan alive."""
+        d = Plan.__new__(Plan)
+        d.type, d.M, d.prec = int(nufft_type), int(M), self.prec
+        d.isign = int(isign if isign is not None else (1 if d.type == 1 else -1))
+        d.device, d.stream = self.device, self.stream
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.call("cmt_plan_create_derived", self._h, d.type, d.M, d.isign, ctypes.byref(h))
+        d._h, d._src, d._n, d._keep = h, self, 0, ()
+        if PROFILE_KERNELS:
+            d.profile(True)
+            _LIVE_PLANS.add(d)
+        return d
 
     # -- kernel timing
     def profile(self, enable=True):

@@ -69,6 +69,13 @@ typedef struct cmt_plan cmt_plan;
 int cmt_plan_create(int type, int M, int prec, double eps, int isign, double upsampfac,
                     void *stream, cmt_plan **plan);
 
+/* A plan (type, M modes, isign) on the points of src whose fine grid is exactly twice as
+ * fine as src's: src's bin order and permutation apply unchanged, so no second sort and no
+ * second copy of the points.  It follows src's current points at every execute; src must
+ * outlive it.  The autocorrelation solve uses it for the Toeplitz kernel on 2M modes
+ * (cmtip/autocorrelation/autocorrelation.py:141-147) over the points of the M-mode plan. */
+int cmt_plan_create_derived(const cmt_plan *src, int type, int M, int isign, cmt_plan **plan);
+
 /* Query the chosen fine-grid size, kernel width, ES shape parameter and bin size. */
 int cmt_plan_info(const cmt_plan *plan, int *n_fine, int *width, double *beta, int *bin_size,
                   int64_t *n_subproblems);

@@ -156,6 +156,28 @@ def test_quaternion_points_match_reference_chain(nf):
 
 
 @pytest.mark.parametrize("prec", [32, 64])
+def test_derived_plan_on_twice_finer_grid(nf, prec):
+    # the 2M-mode plan borrowing an M-mode plan's sorted points equals an independent plan
+    rng = np.random.default_rng(21)
+    M, N = 17, 20000
+    x, y, z = _pts(rng, N)
+    c = rng.standard_normal(N)
+    eps, tol = (1e-6, TOL32) if prec == 32 else (1e-12, TOL64)
+    src = nf.Plan(1, M, eps=eps, isign=1, prec=prec).set_pts(*(torch.from_numpy(a) for a in (x, y, z)))
+    d = src.derive(1, 2 * M, isign=1)
+    assert d.info()["n_fine"] == 2 * src.info()["n_fine"]
+    ref = on.type1(x, y, z, c, 2 * M, eps=1e-13, isign=1)
+    got = d.execute(torch.from_numpy(c), real_out=True, fft_order=True, scale=0.5)
+    assert rel_l2(got.cpu().numpy(), 0.5 * np.fft.ifftshift(ref.real)) < tol
+    assert rel_l2(d.execute(None, real_out=True).cpu().numpy(),
+                  on.type1(x, y, z, np.ones(N), 2 * M, eps=1e-13).real) < tol
+    # new points on the source are followed by the derived plan
+    x2 = x[::-1].copy()
+    src.set_pts(*(torch.from_numpy(a) for a in (x2, y, z)))
+    assert rel_l2(d.execute(torch.from_numpy(c)).cpu().numpy(), on.type1(x2, y, z, c, 2 * M, eps=1e-13)) < tol
+
+
+@pytest.mark.parametrize("prec", [32, 64])
 def test_pair_is_normal_operator(nf, prec):
     rng = np.random.default_rng(11)
     M, N = 15, 30000
