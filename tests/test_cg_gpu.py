@@ -70,7 +70,9 @@ def test_fixed_iterations_match_reference(ac_mod, golden, prec, tol, use_graph):
 def test_solve_ac_matches_reference(ac_mod, golden, prec, tol, operator):
     g = golden("autocorrelation")
     M = int(g["M"])
-    eps = 1e-6 if prec == 32 else 1e-12
+    # the explicit pair re-applies the NUFFT error every iteration (the Toeplitz kernel
+    # carries it once), so over ~90 iterations its FP32 form needs the FP32-limit kernel
+    eps = (1e-7 if operator == "pair" else 1e-6) if prec == 32 else 1e-12
     est = g["estimate"].copy()
     ac, info = ac_mod.solve_ac(1, g["ppr"], g["rext"], g["slices"], M, orientations=g["quats"], ac_estimate=est,
                                prec=prec, operator=operator, eps=eps, return_info=True)
