@@ -54,6 +54,7 @@ SIGNATURES = {
     "cmt_cg_solve": [_vp, _vp, _vp, _i32, _f64, _f64, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_f64)],
     "cmt_cg_destroy": [_vp],
     "cmt_support_from_estimate": [_vp, _i32, _vp, _vp, _i32, _vp],
+    "cmt_support_from_estimate_noalloc": [_vp, _i32, _vp, _i32, _vp],
     "cmt_match_create": [_i64, _i32, _vp, ctypes.POINTER(_vp)],
     "cmt_match_set_data": [_vp, _i64, _vp, _vp],
     "cmt_match_set_refs": [_vp, _i64, _vp, _i32],

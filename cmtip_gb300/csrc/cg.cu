@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -713,6 +714,73 @@ extern "C" int cmt_support_from_estimate(float *est, int M, float *support, floa
     k_gauss_axis<<<gb, 256, 0, st>>>(est, a, M, 0, w[0], w[1], w[2]);
     k_gauss_axis<<<gb, 256, 0, st>>>(a, b, M, 1, w[0], w[1], w[2]);
     k_gauss_axis<<<gb, 256, 0, st>>>(b, a, M, 2, w[0], w[1], w[2]);
+    k_threshold<<<gb, 256, 0, st>>>(a, support, est_inplace ? est : nullptr, m3, 1e-12);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+// ---------------------------------------------------------------- allocation-free variant
+//
+// Same computation as cmt_support_from_estimate, for callers that cannot allocate device
+// memory: a host program driving this library from inside CUDA graph capture (a plain
+// cudaMalloc is not capturable), or one that hands the GPU's memory to its own pool and
+// forbids any other allocator from taking or returning blocks.  The two M^3 float grids
+// of scratch live in a file-scope device array, so every GPU that loads the library holds
+// CMT_NOALLOC_MAX_M^3 * 2 floats (16 MiB) until the process exits.
+static __device__ __align__(256) float g_support_scratch[2 * CMT_NOALLOC_MAX_M * CMT_NOALLOC_MAX_M *
+                                                         CMT_NOALLOC_MAX_M];
+
+namespace {
+std::mutex g_scratch_mu;
+constexpr int kMaxDevices = 128;
+float *g_scratch_ptr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of the scratch array on the current device.  Host code only sees a
+// host-side stand-in under the array's name, so the address is looked up once per
+// device (with that device current) and cached.
+static int scratch_address(float **out)
+{
+    int dev = 0;
+    CMT_TRY_CUDA(cudaGetDevice(&dev));
+    CMT_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        float *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_support_scratch);
+        if (e != cudaSuccess) {
+            set_error("cudaGetSymbolAddress of the support scratch: %s", cudaGetErrorString(e));
+            return CMT_ERR_CUDA;
+        }
+        g_scratch_ptr[dev] = ptr;
+    }
+    *out = g_scratch_ptr[dev];
+    return CMT_OK;
+}
+
+extern "C" int cmt_support_from_estimate_noalloc(float *est, int M, float *support, int est_inplace, void *stream)
+{
+    CMT_CHECK_ARG(est && support, "null argument");
+    CMT_CHECK_ARG(M > 0 && M <= CMT_NOALLOC_MAX_M,
+                  "M = %d outside [1, %d]: the allocation-free support filter has a fixed scratch for grids of at "
+                  "most %d^3 voxels (use cmt_support_from_estimate with caller scratch)",
+                  M, CMT_NOALLOC_MAX_M, CMT_NOALLOC_MAX_M);
+    float *scratch = nullptr;
+    CMT_TRY(scratch_address(&scratch));
+    cudaStream_t st = (cudaStream_t)stream;
+    int64_t m3 = (int64_t)M * M * M;
+    double phi[5], tot = 0.0;
+    for (int k = -2; k <= 2; ++k) {
+        phi[k + 2] = exp(-0.5 / (0.5 * 0.5) * k * k);
+        tot += phi[k + 2];
+    }
+    // every pass writes all M^3 entries of its scratch grid before the next one reads it,
+    // so nothing left from an earlier call is read and no clearing is needed
+    float *a = scratch, *b = scratch + m3;
+    unsigned gb = (unsigned)ceil_div(m3, 256);
+    k_gauss_axis<<<gb, 256, 0, st>>>(est, a, M, 0, phi[2] / tot, phi[3] / tot, phi[4] / tot);
+    k_gauss_axis<<<gb, 256, 0, st>>>(a, b, M, 1, phi[2] / tot, phi[3] / tot, phi[4] / tot);
+    k_gauss_axis<<<gb, 256, 0, st>>>(b, a, M, 2, phi[2] / tot, phi[3] / tot, phi[4] / tot);
     k_threshold<<<gb, 256, 0, st>>>(a, support, est_inplace ? est : nullptr, m3, 1e-12);
     CMT_LAUNCH_CHECK();
     return CMT_OK;

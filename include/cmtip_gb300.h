@@ -157,6 +157,20 @@ int cmt_cg_destroy(cmt_cg *cg);
 int cmt_support_from_estimate(float *est, int M, float *support, float *scratch, int est_inplace,
                               void *stream);
 
+/* Largest grid edge accepted by cmt_support_from_estimate_noalloc. */
+#define CMT_NOALLOC_MAX_M 128
+
+/* cmt_support_from_estimate without the scratch argument and without any allocation, for
+ * callers that cannot allocate device memory: code running inside CUDA graph capture, or
+ * an application whose own pool owns the GPU's memory.  No counterpart in the reference
+ * (cmtip computes the support on the host with scipy).  The scratch is a fixed
+ * 2 * 128^3-float (16 MiB) device array that every GPU loading the library keeps until the
+ * process exits; M > CMT_NOALLOC_MAX_M returns CMT_ERR_ARG.  The first call on a device
+ * looks the array's device address up: make it before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU (other streams, other host threads) race:
+ * order them on one stream. */
+int cmt_support_from_estimate_noalloc(float *est, int M, float *support, int est_inplace, void *stream);
+
 /* ---------------------------------------------------------------- orientation matching
  * Weighted euclidean distances between images and model slices with a fused running
  * top-k epilogue, then exact re-scoring of the candidates (cmtip/alignment/align.py:68-132:
