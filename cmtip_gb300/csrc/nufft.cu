@@ -254,16 +254,43 @@ __device__ __forceinline__ unsigned lanemask_lt()
     return m;
 }
 
-// Pass 1: per-bin counts (warp-aggregated atomics), range check.
+// Sort key of a point: its bin, then (within the bin) the origin of its kernel window on
+// this grid, then the origin's offset on a grid twice as fine (0/1 per dimension).  Points
+// sharing a key share their whole w^3 window on this grid and on a derived plan's twice
+// finer grid, so the kernels can keep a window in registers across runs of such points.
+// Keys per bin: kb = (bs+1)^3 * 8 when fine sorting, else 1.
+template <typename T>
+__device__ __forceinline__ int64_t point_key(int b, T rx, T ry, T rz, int w, int bs, int fine_sort)
+{
+    if (!fine_sort) return b;
+    const T hw = T(0.5) * T(w);
+    const int h = w / 2, O = bs + 1;
+    int lx = (int)ceil(rx - hw), ly = (int)ceil(ry - hw), lz = (int)ceil(rz - hw);
+    int ox = min(max(lx + h, 0), bs), oy = min(max(ly + h, 0), bs), oz = min(max(lz + h, 0), bs);
+    const int base = (w - 2 - (w & 1)) / 2;
+    int dx = (int)ceil(T(2) * rx - hw) - 2 * lx - base;
+    int dy = (int)ceil(T(2) * ry - hw) - 2 * ly - base;
+    int dz = (int)ceil(T(2) * rz - hw) - 2 * lz - base;
+    dx = min(max(dx, 0), 1);
+    dy = min(max(dy, 0), 1);
+    dz = min(max(dz, 0), 1);
+    return ((((int64_t)b * O + ox) * O + oy) * O + oz) * 8 + dx * 4 + dy * 2 + dz;
+}
+
+struct SortGeom {
+    int n, bs, nb, w, fine_sort;
+};
+
+// Pass 1: per-key counts (warp-aggregated atomics), range check.
 template <typename T>
 __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q, T s_hi, T s_lo,
-                            int n, int bs, int nb, int *count, int *flag)
+                            SortGeom sg, int *count, int *flag)
 {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t base = (int64_t)blockIdx.x * blockDim.x;
     for (; base < N; base += stride) {
         int64_t j = base + threadIdx.x;
-        int b = -1;
+        long long key = -1;
         if (j < N) {
             T px, py, pz, rx, ry, rz;
             bool bad;
@@ -271,52 +298,140 @@ __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T
             if (bad) {
                 atomicOr(flag, 1);
             } else {
-                b = bin_of<T>(px, py, pz, s_hi, s_lo, n, bs, nb, rx, ry, rz);
+                int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.bs, sg.nb, rx, ry, rz);
+                key = point_key<T>(b, rx, ry, rz, sg.w, sg.bs, sg.fine_sort);
             }
         }
-        unsigned peers = __match_any_sync(0xffffffffu, b);
+        unsigned peers = __match_any_sync(0xffffffffu, key);
         int leader = __ffs(peers) - 1;
-        if (b >= 0 && (int)(threadIdx.x & 31) == leader) atomicAdd(&count[b], __popc(peers));
+        if (key >= 0 && (int)(threadIdx.x & 31) == leader) atomicAdd(&count[key], __popc(peers));
     }
 }
 
-// Pass 2: scatter permutation and bin-relative coordinates into bin order.
+// Pass 2: scatter permutation and bin-relative coordinates into key order.  next[key]
+// starts at the key's first position; start[key + 1] bounds it.
 template <typename T>
 __global__ void k_bin_scatter(int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q, T s_hi,
-                              T s_lo, int n, int bs, int nb, const int *start, const int *count, int *fill,
-                              int *perm, T *ux, T *uy, T *uz, int *flag)
+                              T s_lo, SortGeom sg, const int *start, int *next, int *perm, T *ux, T *uy, T *uz,
+                              int *flag)
 {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t base = (int64_t)blockIdx.x * blockDim.x;
     for (; base < N; base += stride) {
         int64_t j = base + threadIdx.x;
-        int b = -1;
+        long long key = -1;
         T rx = 0, ry = 0, rz = 0;
         if (j < N) {
             T px, py, pz;
             bool bad;
             point_coords<T>(mode, j, x, y, z, q, px, py, pz, bad);
-            if (!bad) b = bin_of<T>(px, py, pz, s_hi, s_lo, n, bs, nb, rx, ry, rz);
+            if (!bad) {
+                int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.bs, sg.nb, rx, ry, rz);
+                key = point_key<T>(b, rx, ry, rz, sg.w, sg.bs, sg.fine_sort);
+            }
         }
-        unsigned peers = __match_any_sync(0xffffffffu, b);
+        unsigned peers = __match_any_sync(0xffffffffu, key);
         int lane = threadIdx.x & 31;
         int leader = __ffs(peers) - 1;
         int off = 0;
-        if (b >= 0 && lane == leader) off = atomicAdd(&fill[b], __popc(peers));
+        if (key >= 0 && lane == leader) off = atomicAdd(&next[key], __popc(peers));
         off = __shfl_sync(peers, off, leader);
-        if (b >= 0) {
-            int rank = off + __popc(peers & lanemask_lt());
-            if (rank >= count[b]) {  // pass 1 and 2 disagree: never write out of the bin
+        if (key >= 0) {
+            int pos = off + __popc(peers & lanemask_lt());
+            if (pos >= start[key + 1]) {  // pass 1 and 2 disagree: never write out of the key's range
                 atomicOr(flag, 2);
                 continue;
             }
-            int pos = start[b] + rank;
             perm[pos] = (int)j;
             ux[pos] = rx;
             uy[pos] = ry;
             uz[pos] = rz;
         }
     }
+}
+
+// ---- exclusive scan of n ints (n < 2^31 total), three kernels: tile scan, scan of the
+// tile sums (one CTA), tile offsets
+constexpr int SCAN_THREADS = 256, SCAN_PER = 8, SCAN_TILE = SCAN_THREADS * SCAN_PER;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int &total)
+{
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int s = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        sh[lane] = s;
+    }
+    __syncthreads();
+    int prefix = (wid > 0 ? sh[wid - 1] : 0) + x - v;
+    total = sh[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return prefix;
+}
+
+__global__ void k_scan_tiles(const int *in, int *out, int64_t n, int *tile_sums)
+{
+    __shared__ int sh[32];
+    int64_t t0 = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_PER;
+    int v[SCAN_PER];
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_PER; ++i) {
+        v[i] = t0 + i < n ? in[t0 + i] : 0;
+        s += v[i];
+    }
+    int total;
+    int run = block_exclusive_scan(s, sh, total);
+#pragma unroll
+    for (int i = 0; i < SCAN_PER; ++i) {
+        if (t0 + i < n) out[t0 + i] = run;
+        run += v[i];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_single(int *a, int n)
+{
+    __shared__ int sh[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int v = i < n ? a[i] : 0;
+        int total;
+        int pre = block_exclusive_scan(v, sh, total);
+        if (i < n) a[i] = carry + pre;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+}
+
+__global__ void k_add_tile_offsets(int *out, int64_t n, const int *tile_off)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += tile_off[i / SCAN_TILE];
+}
+
+// bins from the key scan: bin b's points are [start[b*kb], start[(b+1)*kb])
+__global__ void k_bins_from_keys(int nbins, int64_t kb, const int *key_start, int *bin_count, int *bin_start)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbins) return;
+    int s = key_start[(int64_t)b * kb], e = key_start[(int64_t)(b + 1) * kb];
+    bin_start[b] = s;
+    bin_count[b] = e - s;
 }
 
 // Exclusive scan of bin counts and of per-bin subproblem counts (one CTA).
@@ -649,12 +764,30 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     p.N = 0;
     CMT_CHECK_ARG(N > 0 && N <= 0x7fffffffLL, "number of points %lld outside [1, 2^31-1]", (long long)N);
     int nbins = p.nb * p.nb * p.nb;
+    // keys: bins, refined by window origin when the key space stays moderate (< 2^30)
+    const int64_t O = p.bs + 1;
+    int64_t kb = O * O * O * 8;
+    int fine_sort = (int64_t)nbins * kb < (1LL << 30) ? 1 : 0;
+    if (!fine_sort) kb = 1;
+    const int64_t nkeys = (int64_t)nbins * kb;
+    const int64_t ntiles = (nkeys + 1 + SCAN_TILE - 1) / SCAN_TILE;
     if (!p.bin_count) {
         CMT_TRY_CUDA(cudaMalloc(&p.bin_count, sizeof(int) * nbins));
         CMT_TRY_CUDA(cudaMalloc(&p.bin_fill, sizeof(int) * nbins));
         CMT_TRY_CUDA(cudaMalloc(&p.bin_start, sizeof(int) * nbins));
         CMT_TRY_CUDA(cudaMalloc(&p.dflag, sizeof(int) * 4));
         CMT_TRY_CUDA(cudaMalloc(&p.dtot, sizeof(long long) * 2));
+    }
+    if (nkeys + 1 > p.cap_keys) {
+        cudaFree(p.key_start);
+        cudaFree(p.key_next);
+        cudaFree(p.tile_sums);
+        p.key_start = p.key_next = p.tile_sums = nullptr;
+        p.cap_keys = 0;
+        CMT_TRY_CUDA(cudaMalloc(&p.key_start, sizeof(int) * (nkeys + 1)));
+        CMT_TRY_CUDA(cudaMalloc(&p.key_next, sizeof(int) * (nkeys + 1)));
+        CMT_TRY_CUDA(cudaMalloc(&p.tile_sums, sizeof(int) * ntiles));
+        p.cap_keys = nkeys + 1;
     }
     if (N > p.cap_pts) {
         cudaFree(p.perm);
@@ -671,15 +804,22 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
         p.cap_pts = N;
     }
     cudaStream_t st = p.stream;
-    CMT_TRY_CUDA(cudaMemsetAsync(p.bin_count, 0, sizeof(int) * nbins, st));
-    CMT_TRY_CUDA(cudaMemsetAsync(p.bin_fill, 0, sizeof(int) * nbins, st));
+    CMT_TRY_CUDA(cudaMemsetAsync(p.key_next, 0, sizeof(int) * (nkeys + 1), st));
     CMT_TRY_CUDA(cudaMemsetAsync(p.dflag, 0, sizeof(int) * 4, st));
     double s = p.n / (2.0 * kPi);
     T s_hi = (T)s, s_lo = (T)(s - (double)s_hi);
+    SortGeom sgeo{p.n, p.bs, p.nb, p.w, fine_sort};
     int g = grid_for(N);
-    k_bin_count<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, p.n, p.bs, p.nb, p.bin_count, p.dflag);
+    // pass 1: counts per key (into key_next), then key_start = exclusive scan (with the total
+    // at key_start[nkeys])
+    k_bin_count<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, sgeo, p.key_next, p.dflag);
     CMT_LAUNCH_CHECK();
-    int *sub_start = p.bin_fill;  // reuse as scratch for the subproblem scan
+    k_scan_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, st>>>(p.key_next, p.key_start, nkeys + 1, p.tile_sums);
+    k_scan_single<<<1, 1024, 0, st>>>(p.tile_sums, (int)ntiles);
+    k_add_tile_offsets<<<(unsigned)ceil_div(nkeys + 1, 256), 256, 0, st>>>(p.key_start, nkeys + 1, p.tile_sums);
+    k_bins_from_keys<<<ceil_div(nbins, 256), 256, 0, st>>>(nbins, kb, p.key_start, p.bin_count, p.bin_start);
+    CMT_LAUNCH_CHECK();
+    int *sub_start = p.bin_fill;  // scratch for the subproblem scan
     k_scan_bins<<<1, 1024, 0, st>>>(nbins, p.bin_count, p.bin_start, sub_start, p.maxsub, p.dtot);
     CMT_LAUNCH_CHECK();
     long long tot[2];
@@ -703,9 +843,10 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     }
     k_sub_list<<<ceil_div(nbins, 256), 256, 0, st>>>(nbins, p.bin_count, sub_start, p.maxsub, p.sub_bin, p.sub_off);
     CMT_LAUNCH_CHECK();
-    CMT_TRY_CUDA(cudaMemsetAsync(p.bin_fill, 0, sizeof(int) * nbins, st));
-    k_bin_scatter<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, p.n, p.bs, p.nb, p.bin_start, p.bin_count,
-                                        p.bin_fill, p.perm, (T *)p.ux, (T *)p.uy, (T *)p.uz, p.dflag);
+    // pass 2: scatter, key_next starting at each key's first position
+    CMT_TRY_CUDA(cudaMemcpyAsync(p.key_next, p.key_start, sizeof(int) * (nkeys + 1), cudaMemcpyDeviceToDevice, st));
+    k_bin_scatter<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, sgeo, p.key_start, p.key_next, p.perm,
+                                        (T *)p.ux, (T *)p.uy, (T *)p.uz, p.dflag);
     CMT_LAUNCH_CHECK();
     CMT_TRY_CUDA(cudaMemcpyAsync(&flag, p.dflag, sizeof flag, cudaMemcpyDeviceToHost, st));
     CMT_TRY_CUDA(cudaStreamSynchronize(st));
@@ -880,6 +1021,9 @@ static void destroy(Plan *p)
     unborrow(*p);
     cudaFree(p->bin_count);
     cudaFree(p->bin_fill);
+    cudaFree(p->key_start);
+    cudaFree(p->key_next);
+    cudaFree(p->tile_sums);
     cudaFree(p->bin_start);
     cudaFree(p->sub_bin);
     cudaFree(p->sub_off);

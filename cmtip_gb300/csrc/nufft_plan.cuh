@@ -22,6 +22,8 @@ struct Plan {
     int64_t nsub = 0;
     int *bin_count = nullptr, *bin_start = nullptr, *bin_fill = nullptr;
     int *sub_bin = nullptr, *sub_off = nullptr;
+    int *key_start = nullptr, *key_next = nullptr, *tile_sums = nullptr;  // point-sort keys
+    int64_t cap_keys = 0;
     int *perm = nullptr;
     void *ux = nullptr, *uy = nullptr, *uz = nullptr;  // bin-relative sorted coordinates
     int64_t cap_pts = 0, cap_sub = 0;

@@ -2,27 +2,32 @@
 // nufft_interp.cu).
 //
 // One CTA per subproblem (a bin of the fine grid, or a <= maxsub slice of a dense bin).
-// Each warp walks a contiguous run of the subproblem's points, 32 at a time: the lanes load
-// 32 points' coordinates (and strengths) with coalesced loads, then the warp treats the
-// points one after another, broadcasting each with a shuffle.  The w^3 window of a point is
-// split over the lanes: lane = (bl, e), e = lane % EW the z offset, bl = lane / EW the first
-// y offset, the lane visiting y offsets b = bl + r * (32 / EW) for r < ROUNDS and every x
-// offset a < w.  Shared subgrid rows have a pitch P with P mod 32 in {8, 24} (EW = 8) or 16
-// (EW = 16), so the 32 addresses of a shared-memory instruction sit in 32 distinct banks.
-// Complex grids are planar (re | im).  The 3w kernel values of a point are evaluated once,
-// one per lane, and gathered with shuffles.  W > 0 fixes the kernel width at compile time
-// (all loops unrolled, constant divisions); W = 0 reads it at run time (w <= 16).
+// Points are sorted by bin, then by the origin of their kernel window (see point_key in
+// nufft.cu), so consecutive points of a subproblem mostly share the whole w^3 window.  Each
+// warp walks a contiguous run of the subproblem's points, 32 at a time: the lanes load 32
+// points' coordinates (and strengths) with coalesced loads, then the warp treats the points
+// one after another, broadcasting each with a shuffle.  The window is split over the lanes:
+// lane = (bl, e), e = lane % EW the z offset, bl = lane / EW the first y offset, the lane
+// covering y offsets b = bl + r * (32 / EW) for r < ROUNDS and every x offset a < w.  Shared
+// subgrid rows have a pitch P with P mod 32 in {8, 24} (EW = 8) or 16 (EW = 16), so the 32
+// addresses of a shared-memory instruction fall in 32 distinct banks.  Complex grids are
+// planar (re | im).  The 3w kernel values of a point are evaluated once, one per lane, and
+// gathered with shuffles.
 //
-// Spreading accumulates into one shared copy with shared atomics, or (real strengths,
-// SPREAD_PRIV) into per-warp private copies with plain read-modify-write; the flush adds
-// the subgrid to the fine grid once per subproblem (global atomics only there, where
-// neighbouring bins' halos overlap).
+// W > 0 fixes the kernel width at compile time; the lane's ROUNDS x W window cells then
+// live in registers across a run of points with the same window origin: spreading
+// accumulates into them and touches shared memory (shared atomics) only when the origin
+// changes; interpolation loads them once per run.  W = 0 reads the width at run time
+// (w <= 16) and works on shared memory point by point.  The flush adds a subproblem's
+// subgrid to the fine grid once (global atomics only there, where neighbouring bins'
+// halos overlap).
 
 template <int W>
 struct WarpLayout {
     static constexpr int EW = (W > 0 && W <= 8) ? 8 : 16;  // z lanes
     static constexpr int BR = 32 / EW;                      // y offsets per round
     static constexpr int KMAX = W > 0 ? W : MAXW;           // unroll bound of the x loop
+    static constexpr int RMAX = W > 0 ? (W + BR - 1) / BR : 8;
 };
 
 // value q (< 3w) of the point's kernel values, held in lane q % 32 of v0 (q < 32) or v1
@@ -35,15 +40,21 @@ __device__ __forceinline__ T getk(T v0, T v1, int q, bool two)
     return q < 32 ? a : b;
 }
 
-// Window starts (relative to the bin origin) and this lane's share of the 3w kernel values.
-template <typename T, int W>
-__device__ __forceinline__ void point_window(T px, T py, T pz, int w, T beta, int lane, int &lx, int &ly, int &lz,
-                                             T &v0, T &v1)
+// Window origin (relative to the bin origin) of a point, and this lane's share of its 3w
+// kernel values.
+template <typename T>
+__device__ __forceinline__ void point_origin(T px, T py, T pz, int w, int &lx, int &ly, int &lz)
 {
     const T hw = T(0.5) * T(w);
     lx = (int)ceil(px - hw);
     ly = (int)ceil(py - hw);
     lz = (int)ceil(pz - hw);
+}
+
+template <typename T>
+__device__ __forceinline__ void point_values(T px, T py, T pz, int lx, int ly, int lz, int w, T beta, int lane,
+                                             T &v0, T &v1)
+{
     const T inv = T(2) / T(w);
     auto val = [&](int q) -> T {
         if (q >= 3 * w) return T(0);
@@ -67,10 +78,13 @@ __device__ __forceinline__ void warp_run(int cnt, int warp, int nwarps, int &t0,
     t1 = min(cnt, t0 + chunk);
 }
 
+// origins are bin-relative, in [-w/2, bs] with bs <= 32: pack them into one int
+__device__ __forceinline__ int origin_key(int lx, int ly, int lz) { return ((lx + 16) * 64 + (ly + 16)) * 64 + lz + 16; }
+
 // ------------------------------------------------------------------ spread (type 1)
 
 // CPLX: complex strengths (interleaved in c), else real (c == nullptr: all ones).
-// PRIV: per-warp private subgrid copies (no atomics), else one copy with shared atomics.
+// PRIV: per-warp private subgrid copies (plain adds), else one copy with shared atomics.
 // Fine grid: complex n^3 interleaved (CPLX) or real with row stride rs (in-place R2C layout).
 template <typename T, bool CPLX, int W, bool PRIV>
 __global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *sub_off, const int *bin_count,
@@ -97,13 +111,47 @@ __global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *s
     const int e = lane % L::EW, bl = lane / L::EW;
     const bool ez = e < w;
     T *mine = sg + (PRIV ? warp * nch * copy : 0);
+    auto add = [&](int idx, T v) {
+        if (PRIV) mine[idx] += v;
+        else atomicAdd(&mine[idx], v);
+    };
+
+    // register window of the current run (W > 0)
+    T acc[L::RMAX][L::KMAX], aci[L::RMAX][L::KMAX];
+    int cur_key = -1, cur_base = 0;
+    auto flush = [&]() {
+        if (W == 0 || cur_key < 0) return;
+#pragma unroll
+        for (int r = 0; r < L::RMAX; ++r) {
+            const int bb = bl + r * L::BR;
+            const bool ok = ez && bb < w;
+#pragma unroll
+            for (int a = 0; a < L::KMAX; ++a) {
+                if (ok) {
+                    const int idx = cur_base + bb * P + a * plane;
+                    add(idx, acc[r][a]);
+                    if (CPLX) add(copy + idx, aci[r][a]);
+                }
+                acc[r][a] = T(0);
+                aci[r][a] = T(0);
+            }
+        }
+    };
+#pragma unroll
+    for (int r = 0; r < L::RMAX; ++r)
+#pragma unroll
+        for (int a = 0; a < L::KMAX; ++a) {
+            acc[r][a] = T(0);
+            aci[r][a] = T(0);
+        }
+
     int t0, t1;
     warp_run(cnt, warp, nwarps, t0, t1);
+    const T cs = (T)gm.cscale;
     for (int base = t0; base < t1; base += 32) {
         const int tl = base + lane;
         const bool valid = tl < t1;
         const int pos = p0 + (valid ? tl : t0);
-        const T cs = (T)gm.cscale;
         const T mx = ux[pos] * cs, my = uy[pos] * cs, mz = uz[pos] * cs;
         T mr = T(1), mi = T(0);
         if (c && valid) {
@@ -123,38 +171,51 @@ __global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *s
             const T vr = __shfl_sync(0xffffffffu, mr, q);
             const T vi = CPLX ? __shfl_sync(0xffffffffu, mi, q) : T(0);
             int lx, ly, lz;
+            point_origin(px, py, pz, w, lx, ly, lz);
             T v0, v1;
-            point_window<T, W>(px, py, pz, w, beta, lane, lx, ly, lz, v0, v1);
+            point_values(px, py, pz, lx, ly, lz, w, beta, lane, v0, v1);
             T kx[L::KMAX];
 #pragma unroll
             for (int a = 0; a < L::KMAX; ++a) kx[a] = (W > 0 || a < w) ? getk(v0, v1, a, two) : T(0);
             const T kz = getk(v0, v1, 2 * w + (ez ? e : 0), two);
             const int base_idx = ((lx + h) * S + (ly + h)) * P + lz + h + e;
+            if (W > 0) {
+                const int key = origin_key(lx, ly, lz);  // warp-uniform
+                if (key != cur_key) {
+                    flush();
+                    cur_key = key;
+                    cur_base = base_idx;
+                }
+            }
 #pragma unroll
-            for (int r = 0; r < (W > 0 ? (W + L::BR - 1) / L::BR : 8); ++r) {
+            for (int r = 0; r < L::RMAX; ++r) {
                 if (W == 0 && r >= rounds) break;
                 const int bb = bl + r * L::BR;
                 const T ky = getk(v0, v1, w + (bb < w ? bb : 0), two);
-                if (!ez || bb >= w) continue;
                 const T kyz = ky * kz;
                 const T wr = kyz * vr, wi = kyz * vi;
-                int idx = base_idx + bb * P;
+                if (W > 0) {
 #pragma unroll
-                for (int a = 0; a < L::KMAX; ++a) {
-                    if (W > 0 || a < w) {
-                        if (PRIV) {
-                            mine[idx] += kx[a] * wr;
-                            if (CPLX) mine[copy + idx] += kx[a] * wi;
-                        } else {
-                            atomicAdd(&mine[idx], kx[a] * wr);
-                            if (CPLX) atomicAdd(&mine[copy + idx], kx[a] * wi);
-                        }
+                    for (int a = 0; a < L::KMAX; ++a) {
+                        acc[r][a] += kx[a] * wr;
+                        if (CPLX) aci[r][a] += kx[a] * wi;
                     }
-                    idx += plane;
+                } else {
+                    if (!ez || bb >= w) continue;
+                    int idx = base_idx + bb * P;
+#pragma unroll
+                    for (int a = 0; a < L::KMAX; ++a) {
+                        if (a < w) {
+                            add(idx, kx[a] * wr);
+                            if (CPLX) add(copy + idx, kx[a] * wi);
+                        }
+                        idx += plane;
+                    }
                 }
             }
         }
     }
+    flush();
     __syncthreads();
     const int bx = b / (gm.nb * gm.nb), by = (b / gm.nb) % gm.nb, bz = b % gm.nb;
     const int ox = bx * gm.bs - h, oy = by * gm.bs - h, oz = bz * gm.bs - h;
@@ -203,26 +264,45 @@ __device__ __forceinline__ void load_subgrid(const T *fine, const SubgridGeom &g
     }
 }
 
-// this lane's partial of the interpolated value at a point
+// Register window of the lane (W > 0): grid values of its cells for the current origin.
 template <typename T, bool CPLX, int W>
-__device__ __forceinline__ void interp_partial(const T *sg, int copy, int S, int P, int plane, int w, int h, int rounds,
-                                               bool two, int lx, int ly, int lz, T v0, T v1, int e, int bl, T &sr,
-                                               T &si, T (&kx)[WarpLayout<W>::KMAX], T &kz)
+struct Window {
+    using L = WarpLayout<W>;
+    T re[L::RMAX][L::KMAX], im[L::RMAX][L::KMAX];
+
+    __device__ __forceinline__ void load(const T *sg, int copy, int plane, int P, int base_idx, int bl, bool ez,
+                                         int w)
+    {
+#pragma unroll
+        for (int r = 0; r < L::RMAX; ++r) {
+            const int bb = bl + r * L::BR;
+            const bool ok = ez && bb < w;
+#pragma unroll
+            for (int a = 0; a < L::KMAX; ++a) {
+                const int idx = base_idx + bb * P + a * plane;
+                re[r][a] = ok ? sg[idx] : T(0);
+                if (CPLX) im[r][a] = ok ? sg[copy + idx] : T(0);
+            }
+        }
+    }
+};
+
+// this lane's partial of the interpolated value at a point (shared-memory path, W = 0 or
+// any W): sum over its cells of kx ky kz G
+template <typename T, bool CPLX, int W>
+__device__ __forceinline__ void interp_partial_smem(const T *sg, int copy, int P, int plane, int w, int rounds,
+                                                    bool two, int base_idx, T v0, T v1, int e, int bl,
+                                                    const T (&kx)[WarpLayout<W>::KMAX], T kz, T &sr, T &si)
 {
     using L = WarpLayout<W>;
-    const bool ez = e < w;
-#pragma unroll
-    for (int a = 0; a < L::KMAX; ++a) kx[a] = (W > 0 || a < w) ? getk(v0, v1, a, two) : T(0);
-    kz = getk(v0, v1, 2 * w + (ez ? e : 0), two);
-    const int base_idx = ((lx + h) * S + (ly + h)) * P + lz + h + e;
     sr = T(0);
     si = T(0);
 #pragma unroll
-    for (int r = 0; r < (W > 0 ? (W + L::BR - 1) / L::BR : 8); ++r) {
+    for (int r = 0; r < L::RMAX; ++r) {
         if (W == 0 && r >= rounds) break;
         const int bb = bl + r * L::BR;
         const T ky = getk(v0, v1, w + (bb < w ? bb : 0), two);
-        if (!ez || bb >= w) continue;
+        if (e >= w || bb >= w) continue;
         int idx = base_idx + bb * P;
         T ar = T(0), ai = T(0);
 #pragma unroll
@@ -232,6 +312,31 @@ __device__ __forceinline__ void interp_partial(const T *sg, int copy, int S, int
                 if (CPLX) ai += kx[a] * sg[copy + idx];
             }
             idx += plane;
+        }
+        sr += ky * ar;
+        si += ky * ai;
+    }
+    sr *= kz;
+    si *= kz;
+}
+
+// the same from the register window
+template <typename T, bool CPLX, int W>
+__device__ __forceinline__ void interp_partial_regs(const Window<T, CPLX, W> &win, int w, bool two, T v0, T v1,
+                                                    int bl, const T (&kx)[WarpLayout<W>::KMAX], T kz, T &sr, T &si)
+{
+    using L = WarpLayout<W>;
+    sr = T(0);
+    si = T(0);
+#pragma unroll
+    for (int r = 0; r < L::RMAX; ++r) {
+        const int bb = bl + r * L::BR;
+        const T ky = getk(v0, v1, w + (bb < w ? bb : 0), two);
+        T ar = T(0), ai = T(0);
+#pragma unroll
+        for (int a = 0; a < L::KMAX; ++a) {
+            ar += kx[a] * win.re[r][a];
+            if (CPLX) ai += kx[a] * win.im[r][a];
         }
         sr += ky * ar;
         si += ky * ai;
@@ -262,13 +367,16 @@ __global__ void __launch_bounds__(256) k_interp(const int *sub_bin, const int *s
     const int cnt = min(gm.maxsub, bin_count[b] - off);
     const int p0 = bin_start[b] + off;
     const int e = lane % L::EW, bl = lane / L::EW;
+    const bool ez = e < w;
+    Window<T, CPLX, W> win;
+    int cur_key = -1;
     int t0, t1;
     warp_run(cnt, warp, nwarps, t0, t1);
+    const T cs = (T)gm.cscale;
     for (int base = t0; base < t1; base += 32) {
         const int tl = base + lane;
         const bool valid = tl < t1;
         const int pos = p0 + (valid ? tl : t0);
-        const T cs = (T)gm.cscale;
         const T mx = ux[pos] * cs, my = uy[pos] * cs, mz = uz[pos] * cs;
         T rr = T(0), ri = T(0);  // lane q keeps point q's result
         const int nq = min(32, t1 - base);
@@ -277,11 +385,26 @@ __global__ void __launch_bounds__(256) k_interp(const int *sub_bin, const int *s
             const T py = __shfl_sync(0xffffffffu, my, q);
             const T pz = __shfl_sync(0xffffffffu, mz, q);
             int lx, ly, lz;
-            T v0, v1, kz, sr, si;
+            point_origin(px, py, pz, w, lx, ly, lz);
+            T v0, v1;
+            point_values(px, py, pz, lx, ly, lz, w, beta, lane, v0, v1);
             T kx[L::KMAX];
-            point_window<T, W>(px, py, pz, w, beta, lane, lx, ly, lz, v0, v1);
-            interp_partial<T, CPLX, W>(sg, copy, S, P, plane, w, h, rounds, two, lx, ly, lz, v0, v1, e, bl, sr, si,
-                                       kx, kz);
+#pragma unroll
+            for (int a = 0; a < L::KMAX; ++a) kx[a] = (W > 0 || a < w) ? getk(v0, v1, a, two) : T(0);
+            const T kz = getk(v0, v1, 2 * w + (ez ? e : 0), two);
+            const int base_idx = ((lx + h) * S + (ly + h)) * P + lz + h + e;
+            T sr, si;
+            if (W > 0) {
+                const int key = origin_key(lx, ly, lz);
+                if (key != cur_key) {
+                    win.load(sg, copy, plane, P, base_idx, bl, ez, w);
+                    cur_key = key;
+                }
+                interp_partial_regs<T, CPLX, W>(win, w, two, v0, v1, bl, kx, kz, sr, si);
+            } else {
+                interp_partial_smem<T, CPLX, W>(sg, copy, P, plane, w, rounds, two, base_idx, v0, v1, e, bl, kx, kz,
+                                                sr, si);
+            }
             for (int o = 16; o > 0; o >>= 1) {
                 sr += __shfl_xor_sync(0xffffffffu, sr, o);
                 if (CPLX) si += __shfl_xor_sync(0xffffffffu, si, o);
@@ -330,12 +453,39 @@ __global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub
     const int p0 = bin_start[b] + off;
     const int e = lane % L::EW, bl = lane / L::EW;
     const bool ez = e < w;
+    Window<T, true, W> win, acc;
+    int cur_key = -1, cur_base = 0;
+    auto flush = [&]() {
+        if (W == 0 || cur_key < 0) return;
+#pragma unroll
+        for (int r = 0; r < L::RMAX; ++r) {
+            const int bb = bl + r * L::BR;
+            const bool ok = ez && bb < w;
+#pragma unroll
+            for (int a = 0; a < L::KMAX; ++a) {
+                if (ok) {
+                    const int idx = cur_base + bb * P + a * plane;
+                    atomicAdd(&sb[idx], acc.re[r][a]);
+                    atomicAdd(&sb[copy + idx], acc.im[r][a]);
+                }
+                acc.re[r][a] = T(0);
+                acc.im[r][a] = T(0);
+            }
+        }
+    };
+#pragma unroll
+    for (int r = 0; r < L::RMAX; ++r)
+#pragma unroll
+        for (int a = 0; a < L::KMAX; ++a) {
+            acc.re[r][a] = T(0);
+            acc.im[r][a] = T(0);
+        }
     int t0, t1;
     warp_run(cnt, warp, nwarps, t0, t1);
+    const T cs = (T)gm.cscale;
     for (int base = t0; base < t1; base += 32) {
         const int tl = base + lane;
         const int pos = p0 + (tl < t1 ? tl : t0);
-        const T cs = (T)gm.cscale;
         const T mx = ux[pos] * cs, my = uy[pos] * cs, mz = uz[pos] * cs;
         const int nq = min(32, t1 - base);
         for (int q = 0; q < nq; ++q) {
@@ -343,37 +493,62 @@ __global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub
             const T py = __shfl_sync(0xffffffffu, my, q);
             const T pz = __shfl_sync(0xffffffffu, mz, q);
             int lx, ly, lz;
-            T v0, v1, kz, sr, si;
+            point_origin(px, py, pz, w, lx, ly, lz);
+            T v0, v1;
+            point_values(px, py, pz, lx, ly, lz, w, beta, lane, v0, v1);
             T kx[L::KMAX];
-            point_window<T, W>(px, py, pz, w, beta, lane, lx, ly, lz, v0, v1);
-            interp_partial<T, true, W>(sa, copy, S, P, plane, w, h, rounds, two, lx, ly, lz, v0, v1, e, bl, sr, si,
-                                       kx, kz);
+#pragma unroll
+            for (int a = 0; a < L::KMAX; ++a) kx[a] = (W > 0 || a < w) ? getk(v0, v1, a, two) : T(0);
+            const T kz = getk(v0, v1, 2 * w + (ez ? e : 0), two);
+            const int base_idx = ((lx + h) * S + (ly + h)) * P + lz + h + e;
+            T sr, si;
+            if (W > 0) {
+                const int key = origin_key(lx, ly, lz);
+                if (key != cur_key) {
+                    flush();
+                    win.load(sa, copy, plane, P, base_idx, bl, ez, w);
+                    cur_key = key;
+                    cur_base = base_idx;
+                }
+                interp_partial_regs<T, true, W>(win, w, two, v0, v1, bl, kx, kz, sr, si);
+            } else {
+                interp_partial_smem<T, true, W>(sa, copy, P, plane, w, rounds, two, base_idx, v0, v1, e, bl, kx, kz,
+                                                sr, si);
+            }
             for (int o = 16; o > 0; o >>= 1) {
                 sr += __shfl_xor_sync(0xffffffffu, sr, o);
                 si += __shfl_xor_sync(0xffffffffu, si, o);
             }
             // every lane holds the interpolated value; spread it back with the same weights
-            const int base_idx = ((lx + h) * S + (ly + h)) * P + lz + h + e;
 #pragma unroll
-            for (int r = 0; r < (W > 0 ? (W + L::BR - 1) / L::BR : 8); ++r) {
+            for (int r = 0; r < L::RMAX; ++r) {
                 if (W == 0 && r >= rounds) break;
                 const int bb = bl + r * L::BR;
                 const T ky = getk(v0, v1, w + (bb < w ? bb : 0), two);
-                if (!ez || bb >= w) continue;
                 const T kyz = ky * kz;
                 const T wr = kyz * sr, wi = kyz * si;
-                int idx = base_idx + bb * P;
+                if (W > 0) {
 #pragma unroll
-                for (int a = 0; a < L::KMAX; ++a) {
-                    if (W > 0 || a < w) {
-                        atomicAdd(&sb[idx], kx[a] * wr);
-                        atomicAdd(&sb[copy + idx], kx[a] * wi);
+                    for (int a = 0; a < L::KMAX; ++a) {
+                        acc.re[r][a] += kx[a] * wr;
+                        acc.im[r][a] += kx[a] * wi;
                     }
-                    idx += plane;
+                } else {
+                    if (!ez || bb >= w) continue;
+                    int idx = base_idx + bb * P;
+#pragma unroll
+                    for (int a = 0; a < L::KMAX; ++a) {
+                        if (a < w) {
+                            atomicAdd(&sb[idx], kx[a] * wr);
+                            atomicAdd(&sb[copy + idx], kx[a] * wi);
+                        }
+                        idx += plane;
+                    }
                 }
             }
         }
     }
+    flush();
     __syncthreads();
     const int bx = b / (gm.nb * gm.nb), by = (b / gm.nb) % gm.nb, bz = b % gm.nb;
     const int ox = bx * gm.bs - h, oy = by * gm.bs - h, oz = bz * gm.bs - h;
