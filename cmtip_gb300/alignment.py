@@ -19,7 +19,7 @@ import torch
 
 from . import _lib
 from .geometry import uniform_quaternions
-from .nufft import DEFAULT_EPS, Plan, _ptr, _stream_ptr, inverse_rotations
+from .nufft import DEFAULT_EPS, Plan, _ptr, _stream_ptr, get_plan, inverse_rotations
 
 MODES = {"bf16": 0, "fp32": 1, "fp64": 2, "bf16x3": 3}
 
@@ -109,6 +109,20 @@ class Matcher:
             pass
 
 
+_MATCHERS = {}
+
+
+def _matcher(n_pix, mode) -> "Matcher":
+    """Matchers reused across calls with the same pixel count and form (operand buffers kept)."""
+    key = (int(n_pix), mode, torch.cuda.current_device(), torch.cuda.current_stream().cuda_stream)
+    mt = _MATCHERS.get(key)
+    if mt is None:
+        if len(_MATCHERS) >= 4:
+            _MATCHERS.pop(next(iter(_MATCHERS))).close()
+        mt = _MATCHERS[key] = Matcher(n_pix, mode=mode)
+    return mt
+
+
 def reference_orientations(n_ref_orientations, nbatches=1, true_orientations=None, ref_orientations=None):
     """align.py:96-111: n_ref rounded up to a multiple of nbatches; uniform quaternions as
     float32; true orientations spliced over the tail and the whole set shuffled."""
@@ -134,21 +148,19 @@ def match_orientations(generation, pixel_position_reciprocal, reciprocal_extent,
     prec = 64 if mode == "fp64" else 32
     acd = ac if torch.is_tensor(ac) else torch.from_numpy(np.ascontiguousarray(ac))
     acd = acd.to("cuda", torch.float64 if prec == 64 else torch.float32)
-    plan = Plan(2, acd.shape[0], eps=eps, isign=-1, prec=prec)
+    plan = get_plan(2, acd.shape[0], eps=eps, isign=-1, prec=prec)  # cached: sort buffers reused
     model = compute_slices(refs, pixel_position_reciprocal, reciprocal_extent, acd, eps=eps, prec=prec, plan=plan)
-    plan.close()
     data = slices_ if torch.is_tensor(slices_) else torch.from_numpy(np.ascontiguousarray(slices_))
     data = data.to("cuda").reshape(-1, n_pix)
     weights = generate_weights(pixel_position_reciprocal if not torch.is_tensor(pixel_position_reciprocal)
                                else pixel_position_reciprocal.cpu().numpy(), order=order)
-    mt = Matcher(n_pix, mode=mode)
+    mt = _matcher(n_pix, mode)
     mt.set_data(data, weights)
     mt.set_refs(model.reshape(n_ref, n_pix), nbatches=nbatches)
     idx, d1, d2, tie, n_near = mt.run()
     index = idx.cpu().numpy().astype(np.int64)
     for s in mt.stats()[:-1]:
         print(f"Data/Model std ratio: {s}.", flush=True)
-    mt.close()
     out = refs[index]
     if return_info:
         return out, dict(index=index, best=d1.cpu().numpy(), second=d2.cpu().numpy(),

@@ -15,7 +15,7 @@ struct Plan {
     double cscale = 1.0;                       // coordinate scale of borrowed points
     const Plan *points_of = nullptr;           // set: the point arrays belong to this plan
     double beta = 0.0;
-    int maxsub = 2048;
+    int maxsub = 8192;                         // points per subproblem (CTA)
     cudaStream_t stream = nullptr;
 
     int64_t N = 0;
