@@ -424,6 +424,61 @@ __global__ void k_add_tile_offsets(int *out, int64_t n, const int *tile_off)
     if (i < n) out[i] += tile_off[i / SCAN_TILE];
 }
 
+// Within-subproblem sort by window origin (one CTA per subproblem).  The global passes sort
+// by bin only (few counters, sequential write streams per bin); this pass stages each
+// subproblem's points in shared memory and counting-sorts them by the window origin on this
+// grid and its offset on a twice finer grid (point_key's refinement), so runs of points
+// sharing a window are contiguous for the spreading / interpolation kernels.
+// smem: nsk counters + maxsub * (4 + 3 sizeof(T)) bytes of staging.
+template <typename T>
+__global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin_count, const int *bin_start, int w,
+                          int bs, int maxsub, int nsk, int *perm, T *ux, T *uy, T *uz)
+{
+    extern __shared__ unsigned char smem_raw[];
+    int *cnt_s = reinterpret_cast<int *>(smem_raw);
+    int *sp = cnt_s + nsk;
+    T *sx = reinterpret_cast<T *>(sp + maxsub);
+    T *sy = sx + maxsub, *sz = sy + maxsub;
+    const int b = sub_bin[blockIdx.x];
+    const int off = sub_off[blockIdx.x];
+    const int cnt = min(maxsub, bin_count[b] - off);
+    const int p0 = bin_start[b] + off;
+    for (int i = threadIdx.x; i < nsk; i += blockDim.x) cnt_s[i] = 0;
+    __syncthreads();
+    const int64_t kb = (int64_t)nsk;
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const T x = ux[p0 + i], y = uy[p0 + i], z = uz[p0 + i];
+        sp[i] = perm[p0 + i];
+        sx[i] = x;
+        sy[i] = y;
+        sz[i] = z;
+        atomicAdd(&cnt_s[(int)(point_key<T>(0, x, y, z, w, bs, 1) % kb)], 1);
+    }
+    __syncthreads();
+    // exclusive scan of the nsk counters: per-thread contiguous ranges + block scan
+    __shared__ int sh[32];
+    const int per = (nsk + blockDim.x - 1) / blockDim.x;
+    const int lo = min((int)threadIdx.x * per, nsk), hi = min(lo + per, nsk);
+    int s = 0;
+    for (int i = lo; i < hi; ++i) s += cnt_s[i];
+    int total;
+    int run = block_exclusive_scan(s, sh, total);
+    for (int i = lo; i < hi; ++i) {
+        int c = cnt_s[i];
+        cnt_s[i] = run;
+        run += c;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const T x = sx[i], y = sy[i], z = sz[i];
+        const int pos = p0 + atomicAdd(&cnt_s[(int)(point_key<T>(0, x, y, z, w, bs, 1) % kb)], 1);
+        perm[pos] = sp[i];
+        ux[pos] = x;
+        uy[pos] = y;
+        uz[pos] = z;
+    }
+}
+
 // bins from the key scan: bin b's points are [start[b*kb], start[(b+1)*kb])
 __global__ void k_bins_from_keys(int nbins, int64_t kb, const int *key_start, int *bin_count, int *bin_start)
 {
@@ -765,10 +820,12 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     CMT_CHECK_ARG(N > 0 && N <= 0x7fffffffLL, "number of points %lld outside [1, 2^31-1]", (long long)N);
     int nbins = p.nb * p.nb * p.nb;
     // keys: bins, refined by window origin when the key space stays moderate (< 2^30)
+    // global passes sort by bin; k_subsort then orders each subproblem by window origin
+    const int fine_sort = 0;
+    const int64_t kb = 1;
     const int64_t O = p.bs + 1;
-    int64_t kb = O * O * O * 8;
-    int fine_sort = (int64_t)nbins * kb < (1LL << 30) ? 1 : 0;
-    if (!fine_sort) kb = 1;
+    const int nsk = (int)(O * O * O * 8);
+    const int sub_smem = (int)(nsk * sizeof(int) + (size_t)p.maxsub * (sizeof(int) + 3 * sizeof(T)));
     const int64_t nkeys = (int64_t)nbins * kb;
     const int64_t ntiles = (nkeys + 1 + SCAN_TILE - 1) / SCAN_TILE;
     if (!p.bin_count) {
@@ -848,6 +905,13 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     k_bin_scatter<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, sgeo, p.key_start, p.key_next, p.perm,
                                         (T *)p.ux, (T *)p.uy, (T *)p.uz, p.dflag);
     CMT_LAUNCH_CHECK();
+    if (sub_smem <= 200 * 1024 && p.nsub > 0) {
+        CMT_TRY(prep_smem(k_subsort<T>, sub_smem));
+        k_subsort<T><<<(unsigned)p.nsub, 512, sub_smem, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.w,
+                                                              p.bs, p.maxsub, nsk, p.perm, (T *)p.ux, (T *)p.uy,
+                                                              (T *)p.uz);
+        CMT_LAUNCH_CHECK();
+    }
     CMT_TRY_CUDA(cudaMemcpyAsync(&flag, p.dflag, sizeof flag, cudaMemcpyDeviceToHost, st));
     CMT_TRY_CUDA(cudaStreamSynchronize(st));
     if (flag) {
