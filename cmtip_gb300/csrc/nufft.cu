@@ -258,7 +258,8 @@ __device__ __forceinline__ unsigned lanemask_lt()
 // this grid, then the origin's offset on a grid twice as fine (0/1 per dimension).  Points
 // sharing a key share their whole w^3 window on this grid and on a derived plan's twice
 // finer grid, so the kernels can keep a window in registers across runs of such points.
-// Keys per bin: kb = (bs+1)^3 * 8 when fine sorting, else 1.
+// Keys per bin: kb = 1 (fine_sort 0: bin only), (bs+1)^3 (2: window origin) or
+// (bs+1)^3 * 8 (1: origin and refinement).
 template <typename T>
 __device__ __forceinline__ int64_t point_key(int b, T rx, T ry, T rz, int w, int bs, int fine_sort)
 {
@@ -267,13 +268,17 @@ __device__ __forceinline__ int64_t point_key(int b, T rx, T ry, T rz, int w, int
     const int h = w / 2, O = bs + 1;
     int lx = (int)ceil(rx - hw), ly = (int)ceil(ry - hw), lz = (int)ceil(rz - hw);
     int ox = min(max(lx + h, 0), bs), oy = min(max(ly + h, 0), bs), oz = min(max(lz + h, 0), bs);
+    if (fine_sort == 2) return (((int64_t)b * O + ox) * O + oy) * O + oz;  // origin only
+    // On the twice finer grid the origin is 2l + base + d with d in {0, 1} (even w) or
+    // {0, 1, 2} (odd w); the refinement splits d = 2 off, so within one refined group the fine
+    // origins differ by at most one per dimension.
     const int base = (w - 2 - (w & 1)) / 2;
     int dx = (int)ceil(T(2) * rx - hw) - 2 * lx - base;
     int dy = (int)ceil(T(2) * ry - hw) - 2 * ly - base;
     int dz = (int)ceil(T(2) * rz - hw) - 2 * lz - base;
-    dx = min(max(dx, 0), 1);
-    dy = min(max(dy, 0), 1);
-    dz = min(max(dz, 0), 1);
+    dx = min(max(dx, 0), 2) >> 1;
+    dy = min(max(dy, 0), 2) >> 1;
+    dz = min(max(dz, 0), 2) >> 1;
     return ((((int64_t)b * O + ox) * O + oy) * O + oz) * 8 + dx * 4 + dy * 2 + dz;
 }
 
@@ -425,10 +430,11 @@ __global__ void k_add_tile_offsets(int *out, int64_t n, const int *tile_off)
 }
 
 // Within-subproblem sort by window origin (one CTA per subproblem).  The global passes sort
-// by bin only (few counters, sequential write streams per bin); this pass stages each
-// subproblem's points in shared memory and counting-sorts them by the window origin on this
-// grid and its offset on a twice finer grid (point_key's refinement), so runs of points
-// sharing a window are contiguous for the spreading / interpolation kernels.
+// by bin and (when the key space is small enough) by window origin on this grid; this pass
+// stages each subproblem's points in shared memory and counting-sorts them by the window
+// origin and its offset on a twice finer grid (point_key's refinement), so runs of points
+// sharing a window on this grid or on a derived plan's grid are contiguous for the
+// spreading / interpolation kernels.
 // smem: nsk counters + maxsub * (4 + 3 sizeof(T)) bytes of staging.
 template <typename T>
 __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin_count, const int *bin_start, int w,
@@ -819,11 +825,14 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     p.N = 0;
     CMT_CHECK_ARG(N > 0 && N <= 0x7fffffffLL, "number of points %lld outside [1, 2^31-1]", (long long)N);
     int nbins = p.nb * p.nb * p.nb;
-    // keys: bins, refined by window origin when the key space stays moderate (< 2^30)
-    // global passes sort by bin; k_subsort then orders each subproblem by window origin
-    const int fine_sort = 0;
-    const int64_t kb = 1;
+    // Global passes sort by bin and window origin on this grid ((bs+1)^3 keys per bin, a few
+    // million counters that stay in L2), so a dense bin's subproblems hold contiguous ranges
+    // of origins: every point sharing a window with another of its bin lands next to it.
+    // k_subsort then orders each subproblem by origin and refinement (point_key).  Plans
+    // without sort_origin, and grids with too many keys, sort by bin only.
     const int64_t O = p.bs + 1;
+    const int fine_sort = p.sort_origin && (int64_t)nbins * O * O * O < (1LL << 27) ? 2 : 0;
+    const int64_t kb = fine_sort ? O * O * O : 1;
     const int nsk = (int)(O * O * O * 8);
     const int sub_smem = (int)(nsk * sizeof(int) + (size_t)p.maxsub * (sizeof(int) + 3 * sizeof(T)));
     const int64_t nkeys = (int64_t)nbins * kb;
@@ -1142,6 +1151,13 @@ extern "C" int cmt_plan_create(int type, int M, int prec, double eps, int isign,
     // layout override for tuning: CMT_SPREAD_PRIV=1 spreads real strengths into per-warp
     // private subgrids instead of one subgrid with shared atomics
     if (const char *env = getenv("CMT_SPREAD_PRIV")) p->spread_priv = atoi(env) != 0;
+    // CMT_SPREAD_TAB=0 selects the per-point spreading kernel for every width, for comparison
+    if (const char *env = getenv("CMT_SPREAD_TAB")) p->spread_tab = atoi(env) != 0;
+    // Spreading plans sort each bin by window origin (long runs of shared windows across the
+    // whole bin); interpolation plans sort by bin only, which costs less and loses little.
+    // CMT_SORT_ORIGIN=0/1 overrides, for comparison.
+    p->sort_origin = type == 1;
+    if (const char *env = getenv("CMT_SORT_ORIGIN")) p->sort_origin = atoi(env) != 0;
     int rc = CMT_OK;
     size_t bytes = 2 * elem(*p) * (size_t)p->n * p->n * p->n;
     cudaError_t e = cudaMalloc(&p->fine, bytes);
@@ -1193,6 +1209,12 @@ extern "C" int cmt_plan_create_derived(const cmt_plan *src, int type, int M, int
     p->spread_priv = 0;
     p->points_of = src;
     p->cscale = 2.0 * src->cscale;
+    // real spreading through the extended register window (k_spread_tab); CMT_SPREAD_EXT=0
+    // selects the plain per-origin kernel, for comparison
+    p->spread_ext = p->cscale == 2.0 && p->w + 1 <= 8;
+    if (const char *env = getenv("CMT_SPREAD_EXT")) p->spread_ext = p->spread_ext && atoi(env) != 0;
+    p->spread_tab = src->spread_tab;
+    if (const char *env = getenv("CMT_SPREAD_TAB")) p->spread_tab = atoi(env) != 0;
     p->N = src->N;
     p->nsub = src->nsub;
     p->bin_count = src->bin_count;

@@ -12,6 +12,9 @@ struct Plan {
     int n = 0, w = 0, bs = 8, nb = 0, S = 0;  // fine size, width, bin size, bins/dim, subgrid size
     int P = 0, ew = 8;                         // subgrid row pitch, z lanes of the warp layout
     int spread_priv = 0;                       // real spreading into per-warp private subgrids
+    int spread_ext = 0;                        // derived plan: (w+1)^3 register window per group
+    int spread_tab = 1;                        // widths <= 8: table-driven spreading kernel
+    int sort_origin = 1;                       // global sort by bin and window origin (else bin)
     double cscale = 1.0;                       // coordinate scale of borrowed points
     const Plan *points_of = nullptr;           // set: the point arrays belong to this plan
     double beta = 0.0;

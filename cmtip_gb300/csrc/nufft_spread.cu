@@ -1,4 +1,4 @@
-// Launchers of the spreading kernel (type 1): precision x strengths x layout x kernel width.
+// Launchers of the spreading kernels (type 1): precision x strengths x layout x kernel width.
 #include "cmt_common.cuh"
 #include "nufft_plan.cuh"
 
@@ -8,12 +8,13 @@ namespace cmt {
 
 namespace {
 
-template <typename T, bool CPLX, bool PRIV>
+template <typename T>
 using SpreadFn = void (*)(const int *, const int *, const int *, const int *, const int *, const T *, const T *,
                           const T *, const T *, SubgridGeom, T, T *);
 
+// per-point kernel: any width (W = 0 reads it at run time), optional private subgrids
 template <typename T, bool CPLX, bool PRIV>
-SpreadFn<T, CPLX, PRIV> pick(int w)
+SpreadFn<T> pick(int w)
 {
     switch (w) {
     case 2: return k_spread<T, CPLX, 2, PRIV>;
@@ -27,11 +28,28 @@ SpreadFn<T, CPLX, PRIV> pick(int w)
     }
 }
 
-template <typename T, bool CPLX, bool PRIV>
-int run(Plan &p, const void *c, int rs, int threads, int sm)
+// table-driven kernel: widths 2..8 (2..7 with the extended window)
+template <typename T, bool CPLX, bool EXT>
+SpreadFn<T> pick_tab(int w)
 {
-    SpreadFn<T, CPLX, PRIV> k = pick<T, CPLX, PRIV>(p.w);
-    CMT_TRY(prep_smem(k, sm));
+    switch (w) {
+    case 2: return k_spread_tab<T, CPLX, 2, EXT>;
+    case 3: return k_spread_tab<T, CPLX, 3, EXT>;
+    case 4: return k_spread_tab<T, CPLX, 4, EXT>;
+    case 5: return k_spread_tab<T, CPLX, 5, EXT>;
+    case 6: return k_spread_tab<T, CPLX, 6, EXT>;
+    case 7: return k_spread_tab<T, CPLX, 7, EXT>;
+    case 8: if constexpr (!EXT) return k_spread_tab<T, CPLX, 8, false>;
+    [[fallthrough]];
+    default: return nullptr;
+    }
+}
+
+template <typename T>
+int run(Plan &p, SpreadFn<T> k, const void *c, int rs, int threads, size_t sm)
+{
+    CMT_CHECK_ARG(k, "no spreading kernel for width %d", p.w);
+    CMT_TRY(prep_smem(k, (int)sm));
     prof_begin(p);
     k<<<(unsigned)p.nsub, threads, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,
                                                     (const T *)p.ux, (const T *)p.uy, (const T *)p.uz,
@@ -41,22 +59,30 @@ int run(Plan &p, const void *c, int rs, int threads, int sm)
     return CMT_OK;
 }
 
+template <typename T>
+int dispatch(Plan &p, const void *c, bool cplx, int rs)
+{
+    const size_t one = sub_bytes(p);
+    const bool priv = !cplx && p.spread_priv && one * 4 <= SMEM_BUDGET;
+    if (p.spread_tab && !priv && p.w >= 2 && p.w <= 8) {
+        if (cplx) return run<T>(p, pick_tab<T, true, false>(p.w), c, rs, 256, spread_tab_smem<T, true>(one, 8));
+        const size_t sm = spread_tab_smem<T, false>(one, 8);
+        if (p.spread_ext && p.w <= 7) return run<T>(p, pick_tab<T, false, true>(p.w), c, rs, 256, sm);
+        return run<T>(p, pick_tab<T, false, false>(p.w), c, rs, 256, sm);
+    }
+    if (cplx) return run<T>(p, pick<T, true, false>(p.w), c, rs, 256, 2 * one);
+    if (priv) return run<T>(p, pick<T, false, true>(p.w), c, rs, 128, 4 * one);
+    return run<T>(p, pick<T, false, false>(p.w), c, rs, 256, one);
+}
+
 }  // namespace
 
-// Real strengths accumulate into per-warp private subgrids (4 warps) when the plan asks for
-// it and they fit; otherwise one subgrid with shared atomics (8 warps).
+// Widths 2..8 spread through the per-warp point table (k_spread_tab; on a derived plan's
+// doubled grid with the extended register window); wider kernels, or a plan that asks for
+// per-warp private subgrids, use the per-point kernel (k_spread).
 int launch_spread(Plan &p, const void *c, bool cplx, int rs)
 {
-    size_t one = sub_bytes(p) * (cplx ? 2 : 1);
-    bool priv = !cplx && p.spread_priv && one * 4 <= SMEM_BUDGET;
-    int threads = priv ? 128 : 256;
-    int sm = (int)(priv ? 4 * one : one);
-    if (p.prec == 64) {
-        if (cplx) return run<double, true, false>(p, c, rs, threads, sm);
-        return priv ? run<double, false, true>(p, c, rs, threads, sm) : run<double, false, false>(p, c, rs, threads, sm);
-    }
-    if (cplx) return run<float, true, false>(p, c, rs, threads, sm);
-    return priv ? run<float, false, true>(p, c, rs, threads, sm) : run<float, false, false>(p, c, rs, threads, sm);
+    return p.prec == 64 ? dispatch<double>(p, c, cplx, rs) : dispatch<float>(p, c, cplx, rs);
 }
 
 }  // namespace cmt

@@ -240,6 +240,265 @@ __global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *s
     }
 }
 
+// ------------------------------------------------------------------ table-driven spread
+
+// 8 consecutive values to / from shared memory with 16-byte accesses (p 16-byte aligned).
+template <typename T>
+__device__ __forceinline__ void load8(const T *p, T (&v)[8])
+{
+    if constexpr (sizeof(T) == 4) {
+        const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
+        v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const double2 d = reinterpret_cast<const double2 *>(p)[i];
+            v[2 * i] = d.x, v[2 * i + 1] = d.y;
+        }
+    }
+}
+template <typename T>
+__device__ __forceinline__ void store8(T *p, const T (&v)[8])
+{
+    if constexpr (sizeof(T) == 4) {
+        reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+        reinterpret_cast<float4 *>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) reinterpret_cast<double2 *>(p)[i] = make_double2(v[2 * i], v[2 * i + 1]);
+    }
+}
+
+// Per-warp point table: 32 records of REC values, one per point of the current batch.
+//   [0, 8)   x kernel values by window column a (zero outside the point's columns)
+//   [8, 16)  y kernel values in pairs (row b, row b + 4), b < 4
+//   [16, ..) z kernel values times the strength: 8 reals, or 8 (re, im) pairs
+template <typename T, bool CPLX>
+struct SpreadTable {
+    static constexpr int REC = CPLX ? 32 : 24;
+    static constexpr size_t bytes_per_warp = 32 * REC * sizeof(T);
+};
+
+// Shared-memory bytes of k_spread_tab: the subgrid(s), 16-byte aligned, then one table per warp.
+template <typename T, bool CPLX>
+__host__ __device__ inline size_t spread_tab_smem(size_t subgrid_bytes, int warps)
+{
+    return ((subgrid_bytes * (CPLX ? 2 : 1) + 15) & ~(size_t)15) + warps * SpreadTable<T, CPLX>::bytes_per_warp;
+}
+
+// Table-driven spreading (kernel width W fixed at compile time).  Each warp walks its run
+// of the subproblem's points in batches of 32.  Per batch, lane t prepares point t alone:
+// coordinates, window origin, its 3W kernel values and strength, written as one record of
+// the warp's table.  The warp then treats the 32 points in order; per point a lane reads the
+// record's x values (two 16-byte broadcasts), its (y, y + 4) pair and its z value times the
+// strength, and adds 2 x NX products into its register window: the lane (bl, e) owns
+// window rows bl and bl + 4 at z offset e, all NX columns.  Shared memory is written only
+// when the window origin changes (the register window is added with shared atomics).
+//
+// EXT (a derived plan's twice finer grid, cscale = 2): the register window is the
+// (W+1)^3 extended window of the point's sort group (point_key's coarse origin and
+// refinement); within a group the fine window origin is the group origin G plus d in {0,1}
+// per dimension, and the owner lane writes its values already shifted by d, so runs span
+// whole groups.  NX = W + 1 (EXT) or W columns, NX <= 8.
+template <typename T, bool CPLX, int W, bool EXT>
+__global__ void __launch_bounds__(256) k_spread_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
+                                                    const int *bin_start, const int *perm, const T *ux,
+                                                    const T *uy, const T *uz, const T *c, SubgridGeom gm, T beta,
+                                                    T *fine)
+{
+    constexpr int NX = EXT ? W + 1 : W;
+    static_assert(W >= 2 && NX <= 8, "table spreading needs a window of at most 8 columns");
+    constexpr int EW = 8, BR = 4, RX = (NX + BR - 1) / BR;
+    constexpr int REC = SpreadTable<T, CPLX>::REC;
+    constexpr int nch = CPLX ? 2 : 1;
+    using T2 = typename cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sg = reinterpret_cast<T *>(smem_raw);
+    const int S = gm.S, P = gm.P, h = W / 2;
+    const int plane = S * P, copy = S * plane;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const size_t sgb = ((size_t)nch * copy * sizeof(T) + 15) & ~(size_t)15;
+    T *tab = reinterpret_cast<T *>(smem_raw + sgb) + warp * 32 * REC;
+    for (int i = threadIdx.x; i < nch * copy; i += blockDim.x) sg[i] = T(0);
+    __syncthreads();
+
+    const int b = sub_bin[blockIdx.x];
+    const int off = sub_off[blockIdx.x];
+    const int cnt = min(gm.maxsub, bin_count[b] - off);
+    const int p0 = bin_start[b] + off;
+    const int e = lane % EW, bl = lane / EW;
+    const int base_off = (W - 2 - (W & 1)) / 2;  // fine origin = 2 * coarse origin + base_off + {0,1,2}
+    const T hw = T(0.5) * T(W), inv = T(2) / T(W);
+
+    T acc[RX][NX], aci[RX][NX];
+#pragma unroll
+    for (int r = 0; r < RX; ++r)
+#pragma unroll
+        for (int a = 0; a < NX; ++a) acc[r][a] = aci[r][a] = T(0);
+    int cur_key = -1, X0 = 0, Y0 = 0, Z0 = 0;  // subgrid cell of the register window's corner
+    auto flush = [&]() {
+        if (cur_key < 0) return;
+        const int zz = Z0 + e;
+#pragma unroll
+        for (int r = 0; r < RX; ++r) {
+            const int yy = Y0 + bl + r * BR;
+            const bool row_ok = e < NX && bl + r * BR < NX && (!EXT || (zz >= 0 && zz < S && yy >= 0 && yy < S));
+#pragma unroll
+            for (int a = 0; a < NX; ++a) {
+                const int xx = X0 + a;
+                // extended cells outside the subgrid never receive a contribution
+                if (row_ok && (!EXT || (xx >= 0 && xx < S))) {
+                    const int idx = (xx * S + yy) * P + zz;
+                    if (acc[r][a] != T(0)) atomicAdd(&sg[idx], acc[r][a]);
+                    if (CPLX && aci[r][a] != T(0)) atomicAdd(&sg[copy + idx], aci[r][a]);
+                }
+                acc[r][a] = aci[r][a] = T(0);
+            }
+        }
+    };
+
+    int t0, t1;
+    warp_run(cnt, warp, nwarps, t0, t1);
+    const T cs = (T)gm.cscale;
+    for (int base = t0; base < t1; base += 32) {
+        // ---- lane `lane` prepares point base + lane
+        const int tl = base + lane;
+        const bool valid = tl < t1;
+        const int pos = p0 + (valid ? tl : t0);
+        const T px = ux[pos] * cs, py = uy[pos] * cs, pz = uz[pos] * cs;
+        T vr = T(1), vi = T(0);
+        if (!valid) {
+            vr = T(0);
+        } else if (c) {
+            const int64_t j = perm[pos];
+            if (CPLX) {
+                const T2 cv = reinterpret_cast<const T2 *>(c)[j];
+                vr = cv.x;
+                vi = cv.y;
+            } else {
+                vr = c[j];
+            }
+        }
+        const int lx = (int)ceil(px - hw), ly = (int)ceil(py - hw), lz = (int)ceil(pz - hw);
+        int gx = lx, gy = ly, gz = lz;
+        if (EXT) {
+            const int cx = (int)ceil(px * T(0.5) - hw), cy = (int)ceil(py * T(0.5) - hw),
+                      cz = (int)ceil(pz * T(0.5) - hw);
+            gx = 2 * cx + base_off + 2 * ((lx - 2 * cx - base_off) >> 1);
+            gy = 2 * cy + base_off + 2 * ((ly - 2 * cy - base_off) >> 1);
+            gz = 2 * cz + base_off + 2 * ((lz - 2 * cz - base_off) >> 1);
+        }
+        const int dx = lx - gx, dy = ly - gy, dz = lz - gz;  // 0 or 1 (EXT), else 0
+        const int my_key = origin_key(gx, gy, gz);
+        T kx[W], ky[W], kz[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            const T tx = (T(lx + k) - px) * inv, ty = (T(ly + k) - py) * inv, tz = (T(lz + k) - pz) * inv;
+            kx[k] = es_eval(tx * tx, beta);
+            ky[k] = es_eval(ty * ty, beta);
+            kz[k] = es_eval(tz * tz, beta);
+        }
+        // the values by window column / row / z offset (shifted by d when EXT)
+        auto col = [&](const T(&v)[W], int d, int a) -> T {
+            const T v0 = a < W ? v[a < W ? a : 0] : T(0);
+            if (!EXT) return v0;
+            const T v1 = (a >= 1 && a - 1 < W) ? v[(a >= 1 && a - 1 < W) ? a - 1 : 0] : T(0);
+            return d ? v1 : v0;
+        };
+        __syncwarp();  // the previous batch's records have been read
+        T *rec = tab + lane * REC;
+        {
+            T o[8];
+#pragma unroll
+            for (int a = 0; a < 8; ++a) o[a] = col(kx, dx, a);
+            store8(rec, o);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                o[2 * q] = col(ky, dy, q);
+                o[2 * q + 1] = col(ky, dy, q + 4);
+            }
+            store8(rec + 8, o);
+            if (CPLX) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const T z = col(kz, dz, q);
+                    o[2 * q] = z * vr;
+                    o[2 * q + 1] = z * vi;
+                }
+                store8(rec + 16, o);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const T z = col(kz, dz, q + 4);
+                    o[2 * q] = z * vr;
+                    o[2 * q + 1] = z * vi;
+                }
+                store8(rec + 24, o);
+            } else {
+#pragma unroll
+                for (int a = 0; a < 8; ++a) o[a] = col(kz, dz, a) * vr;
+                store8(rec + 16, o);
+            }
+        }
+        __syncwarp();
+        // ---- the warp adds the batch's points in order
+        const int nq = min(32, t1 - base);
+        for (int q = 0; q < nq; ++q) {
+            const int key = __shfl_sync(0xffffffffu, my_key, q);  // warp-uniform
+            if (key != cur_key) {
+                flush();
+                cur_key = key;
+                X0 = (key >> 12) - 16 + h;
+                Y0 = ((key >> 6) & 63) - 16 + h;
+                Z0 = (key & 63) - 16 + h;
+            }
+            const T *rq = tab + q * REC;
+            T xv[8];
+            load8(rq, xv);
+            const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
+            if (CPLX) {
+                const T2 zv = reinterpret_cast<const T2 *>(rq + 16)[e];
+                const T wr0 = yv.x * zv.x, wi0 = yv.x * zv.y, wr1 = yv.y * zv.x, wi1 = yv.y * zv.y;
+#pragma unroll
+                for (int a = 0; a < NX; ++a) {
+                    acc[0][a] += xv[a] * wr0;
+                    aci[0][a] += xv[a] * wi0;
+                    if (RX > 1) {
+                        acc[RX - 1][a] += xv[a] * wr1;
+                        aci[RX - 1][a] += xv[a] * wi1;
+                    }
+                }
+            } else {
+                const T zv = rq[16 + e];
+                const T w0 = yv.x * zv, w1 = yv.y * zv;
+#pragma unroll
+                for (int a = 0; a < NX; ++a) {
+                    acc[0][a] += xv[a] * w0;
+                    if (RX > 1) acc[RX - 1][a] += xv[a] * w1;
+                }
+            }
+        }
+    }
+    flush();
+    __syncthreads();
+    const int bx = b / (gm.nb * gm.nb), by = (b / gm.nb) % gm.nb, bz = b % gm.nb;
+    const int ox = bx * gm.bs - h, oy = by * gm.bs - h, oz = bz * gm.bs - h;
+    const int n = gm.n;
+    for (int i = threadIdx.x; i < S * S * S; i += blockDim.x) {
+        const int a = i / (S * S), rem = i - a * S * S, bb = rem / S, ee = rem - bb * S;
+        const int li = (a * S + bb) * P + ee;
+        const T sr = sg[li], si = CPLX ? sg[copy + li] : T(0);
+        if (sr == T(0) && si == T(0)) continue;
+        const int gxx = wrapi(ox + a, n), gyy = wrapi(oy + bb, n), gzz = wrapi(oz + ee, n);
+        if (CPLX) {
+            const int64_t g = ((int64_t)gxx * n + gyy) * n + gzz;
+            atomicAdd(&fine[2 * g], sr);
+            atomicAdd(&fine[2 * g + 1], si);
+        } else {
+            atomicAdd(&fine[((int64_t)gxx * n + gyy) * gm.rs + gzz], sr);
+        }
+    }
+}
+
 // ------------------------------------------------------------------ interp (type 2)
 
 // Loads the subproblem's subgrid (padded rows; planar complex) from the fine grid.

@@ -177,6 +177,43 @@ def test_derived_plan_on_twice_finer_grid(nf, prec):
     assert rel_l2(d.execute(torch.from_numpy(c)).cpu().numpy(), on.type1(x2, y, z, c, 2 * M, eps=1e-13)) < tol
 
 
+@pytest.mark.parametrize("prec,eps", [(32, 1e-3), (32, 1e-4), (32, 1e-5), (32, 1e-6), (64, 1e-6), (64, 1e-5)])
+def test_derived_extended_window_matches_plain(nf, prec, eps, monkeypatch):
+    # widths 4..7: real spreading on the derived grid through the (w+1)^3 register window
+    # equals the per-origin kernel and the oracle
+    rng = np.random.default_rng(22)
+    M, N = 19, 30000
+    x, y, z = _pts(rng, N)
+    c = rng.standard_normal(N)
+    src = nf.Plan(1, M, eps=eps, isign=1, prec=prec).set_pts(*(torch.from_numpy(a) for a in (x, y, z)))
+    ext = src.derive(1, 2 * M, isign=1)
+    monkeypatch.setenv("CMT_SPREAD_EXT", "0")
+    plain = src.derive(1, 2 * M, isign=1)
+    a = ext.execute(torch.from_numpy(c), real_out=True).cpu().numpy()
+    b = plain.execute(torch.from_numpy(c), real_out=True).cpu().numpy()
+    assert rel_l2(a, b) < (1e-6 if prec == 32 else 1e-13)
+    ref = on.type1(x, y, z, c, 2 * M, eps=1e-13, isign=1).real
+    assert rel_l2(a, ref) < 20 * eps
+
+
+@pytest.mark.parametrize("prec,eps", [(32, 1e-2), (32, 1e-4), (32, 1e-6), (64, 1e-7), (64, 1e-5)])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_table_spread_matches_per_point_kernel(nf, prec, eps, cplx, monkeypatch):
+    # widths 3..8: the table-driven spreading kernel equals the per-point kernel and the oracle
+    rng = np.random.default_rng(23)
+    M, N = 24, 40000
+    x, y, z = _pts(rng, N)
+    c = rng.standard_normal(N) + (1j * rng.standard_normal(N) if cplx else 0)
+    pts = [torch.from_numpy(a) for a in (x, y, z)]
+    tab = nf.Plan(1, M, eps=eps, isign=1, prec=prec).set_pts(*pts)
+    monkeypatch.setenv("CMT_SPREAD_TAB", "0")
+    ref_plan = nf.Plan(1, M, eps=eps, isign=1, prec=prec).set_pts(*pts)
+    a = tab.execute(torch.from_numpy(c)).cpu().numpy()
+    b = ref_plan.execute(torch.from_numpy(c)).cpu().numpy()
+    assert rel_l2(a, b) < (1e-6 if prec == 32 else 1e-13)
+    assert rel_l2(a, on.type1(x, y, z, c, M, eps=1e-13, isign=1)) < max(20 * eps, 1e-5)
+
+
 @pytest.mark.parametrize("prec", [32, 64])
 def test_pair_is_normal_operator(nf, prec):
     rng = np.random.default_rng(11)
