@@ -108,14 +108,14 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
 
 
-def profile_traffic(name):
-    """DRAM bytes per launch of a kernel from its committed ncu summary (line
-    'dram_bytes_per_launch: <bytes>'), or None."""
+def profile_traffic(name, key="dram_bytes_per_launch"):
+    """DRAM bytes per launch of a kernel from its committed ncu summary (a line
+    '<key>: <bytes>'), or None."""
     path = os.path.join(HERE, "profiles", name)
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.strip().startswith("dram_bytes_per_launch:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -278,26 +278,32 @@ def gpu_arm(args):
     out = {}
     if rank == 0:
         # dominant kernel: the type-1 spread (two launches per step: ones onto the 2M grid,
-        # data onto the M grid).  Algorithmic bytes per launch: per point 12 B bin-relative
-        # coordinates + 4 B permutation (+ 4 B strength for the data), plus one write of
-        # the real fine grid.
+        # data onto the M grid), both k_spread_tab.  Algorithmic bytes per launch: per point
+        # 12 B bin-relative coordinates (+ 4 B permutation and 4 B strength when spreading
+        # data; the Toeplitz kernel spreads ones and reads neither), plus one write of the
+        # real fine grid n^2 (n + 2) * 4 B.
         spread = {}
-        for key, info, strength_b in (("2M", info2, 0), ("M", infoM, 4)):
+        for key, info, per_pt in (("2M", info2, 12), ("M", infoM, 20)):
             ms = [t for t, k in prof[key] if k == 1]
             nfine = info["n_fine"]
-            alg = N * (12 + 4 + strength_b) + nfine * nfine * (nfine + 2) * 4
+            alg = N * per_pt + nfine * nfine * (nfine + 2) * 4
             spread[key] = dict(ms=float(np.mean(ms)) if ms else None, launches=len(ms), bytes=alg, n_fine=nfine,
-                               width=info["width"])
-        dom = max(spread.values(), key=lambda s: s["ms"] or 0)
+                               width=info["width"], bytes_per_point=per_pt)
+        dom_key = max(spread, key=lambda k: spread[k]["ms"] or 0)
+        dom = spread[dom_key]
         peaks = measured_peaks()
         achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
-        traffic = profile_traffic("k_spread_type1_5000img_M81.md")
-        out["roofline"] = {"bound": "hbm", "kernel": "k_spread<float,false> (type-1 spread, real strengths)",
+        traffic = profile_traffic("k_spread_tab_5000img_M81.md", f"dram_bytes_per_launch_{dom_key}")
+        label = {"2M": "k_spread_tab<float, real, w=7, extended window>: ones onto the 2M-mode Toeplitz grid "
+                       f"(n = {info2['n_fine']})",
+                 "M": f"k_spread_tab<float, real, w=7>: data onto the M-mode grid (n = {infoM['n_fine']})"}[dom_key]
+        out["roofline"] = {"bound": "hbm", "kernel": label,
                            "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
                            "peak_source": peaks["source"],
                            "launch_ms": round(dom["ms"], 3), "algorithmic_bytes": dom["bytes"],
-                           "note": "shared-memory-atomic bound (w^3 adds per point), not HBM bound"}
+                           "note": "instruction-issue bound (w^3 = 343 window updates per point spread over "
+                                   "32 lanes, plus each point's table set-up), not HBM bound"}
         out["spread_kernels"] = spread
         out["clocks"] = clk
 
@@ -456,17 +462,30 @@ def align_bench(torch, nf, alm, args):
 
 # ------------------------------------------------------------------ small kernel cases (profiling)
 
-def kernel_cases():
-    """One small launch of each hot kernel, sized for an ncu capture (a few hundred MB on the
-    device, inputs larger than L2): 200 images x 4 x 128^2 pixels (1.3e7 points) at M = 81 for
-    the spread (type 1, real strengths, M and 2M grids), interpolation (type 2, real part)
-    and pair kernels; 1024 images x 16384 pixels against 4096 references for the tensor-core
-    distance kernel."""
+def kernel_cases(size="small"):
+    """One launch of each hot kernel, for ncu captures.
+
+    small:  200 images x 4 x 128^2 pixels (1.3e7 points) at M = 81 -- spread (type 1, real
+            strengths, M grid and derived 2M grid), pair, interpolation (type 2, real part);
+            1024 images x 16384 pixels against 4096 references for the tensor-core distance
+            kernel.  A few hundred MB on the device.
+    medium: 500 images x 4 x 256^2 pixels (1.3e8 points) with the q-range contracted so that
+            they fill a tenth of the volume at the full workload's point density (the same
+            points per bin and the same runs of shared windows), about 3 GB on the device.
+    full:   the full workload's 5000 images x 4 x 256^2 pixels (1.31e9 points; about 30 GB),
+            spreads and interpolation only -- for one-pass metrics, never a full capture.
+    """
     import torch
     import cmtip_gb300.nufft as nf
     import cmtip_gb300.alignment as alm
-    cfg = dict(CFG, n_img=200, P=128)
+    if size == "small":
+        cfg, qs = dict(CFG, n_img=200, P=128), 1.0
+    elif size == "medium":
+        cfg, qs = dict(CFG, n_img=500), 0.1 ** (1.0 / 3.0)
+    else:
+        cfg, qs = dict(CFG), 1.0
     ppr, rext, quats, ac = synthetic_geometry(cfg)
+    rext = rext / qs
     dev = torch.device("cuda", 0)
     inv = nf.inverse_rotations(torch.from_numpy(quats).to(dev))
     pprd = torch.from_numpy(ppr).to(dev)
@@ -478,21 +497,25 @@ def kernel_cases():
     p1.execute(data, real_out=True)
     p2m = p1.derive(1, 2 * M)  # the Toeplitz-kernel plan of the solve: borrows p1's points
     p2m.execute(None, real_out=True)
-    p1.execute_pair(torch.from_numpy(ac).to(dev))
+    acd = torch.from_numpy(ac).to(dev)
+    if size != "full":
+        p1.execute_pair(acd)
     p2m.close()
     p1.close()
+    del data
     p2 = nf.Plan(2, M, eps=cfg["eps"], isign=-1).set_pts_quat(inv, pprd, rext)
-    p2.execute(torch.from_numpy(ac).to(dev), real_out=True)
+    p2.execute(acd, real_out=True)
     p2.close()
-    n_img, n_ref, n_pix = 1024, 4096, 16384
-    x = torch.randn(n_img, n_pix, device=dev, generator=g).abs()
-    m = torch.randn(n_ref, n_pix, device=dev, generator=g).abs()
-    mt = alm.Matcher(n_pix, mode="bf16")
-    mt.set_data(x, np.full(n_pix, 1.0 / n_pix))
-    mt.set_refs(m)
-    mt.run()
+    if size != "full":
+        n_img, n_ref, n_pix = 1024, 4096, 16384
+        x = torch.randn(n_img, n_pix, device=dev, generator=g).abs()
+        m = torch.randn(n_ref, n_pix, device=dev, generator=g).abs()
+        mt = alm.Matcher(n_pix, mode="bf16")
+        mt.set_data(x, np.full(n_pix, 1.0 / n_pix))
+        mt.set_refs(m)
+        mt.run()
     torch.cuda.synchronize()
-    print("kernel cases done", flush=True)
+    print(f"kernel cases ({size}, {N} points) done", flush=True)
 
 
 # ------------------------------------------------------------------ main
@@ -506,10 +529,11 @@ def main():
     ap.add_argument("--small", action="store_true", help="reduced sizes (smoke runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip pair/NUFFT/FP64/alignment extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--kernels", action="store_true", help="run one small case of each hot kernel and exit")
+    ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full"],
+                    help="run one case of each hot kernel (for ncu captures) and exit")
     args = ap.parse_args()
     if args.kernels:
-        kernel_cases()
+        kernel_cases(args.kernels)
         return
     rank, world, _ = rank_info()
     metric = "CG-iter s & align img/s, 5k imgs M=81: mixed-prec vs FP64 GPU at ≤1e-5 err"

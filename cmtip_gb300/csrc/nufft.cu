@@ -258,8 +258,8 @@ __device__ __forceinline__ unsigned lanemask_lt()
 // this grid, then the origin's offset on a grid twice as fine (0/1 per dimension).  Points
 // sharing a key share their whole w^3 window on this grid and on a derived plan's twice
 // finer grid, so the kernels can keep a window in registers across runs of such points.
-// Keys per bin: kb = 1 (fine_sort 0: bin only), (bs+1)^3 (2: window origin) or
-// (bs+1)^3 * 8 (1: origin and refinement).
+// Keys per bin: kb = 1 (fine_sort 0: bin only), (bs+1)^(fine_sort - 1) (2..4: x / x, y /
+// x, y, z window origin) or (bs+1)^3 * 8 (1: origin and refinement).
 template <typename T>
 __device__ __forceinline__ int64_t point_key(int b, T rx, T ry, T rz, int w, int bs, int fine_sort)
 {
@@ -268,7 +268,9 @@ __device__ __forceinline__ int64_t point_key(int b, T rx, T ry, T rz, int w, int
     const int h = w / 2, O = bs + 1;
     int lx = (int)ceil(rx - hw), ly = (int)ceil(ry - hw), lz = (int)ceil(rz - hw);
     int ox = min(max(lx + h, 0), bs), oy = min(max(ly + h, 0), bs), oz = min(max(lz + h, 0), bs);
-    if (fine_sort == 2) return (((int64_t)b * O + ox) * O + oy) * O + oz;  // origin only
+    if (fine_sort == 2) return ((int64_t)b * O + ox);                            // origin x
+    if (fine_sort == 3) return ((int64_t)b * O + ox) * O + oy;                   // origin x, y
+    if (fine_sort == 4) return (((int64_t)b * O + ox) * O + oy) * O + oz;        // origin
     // On the twice finer grid the origin is 2l + base + d with d in {0, 1} (even w) or
     // {0, 1, 2} (odd w); the refinement splits d = 2 off, so within one refined group the fine
     // origins differ by at most one per dimension.
@@ -825,14 +827,19 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     p.N = 0;
     CMT_CHECK_ARG(N > 0 && N <= 0x7fffffffLL, "number of points %lld outside [1, 2^31-1]", (long long)N);
     int nbins = p.nb * p.nb * p.nb;
-    // Global passes sort by bin and window origin on this grid ((bs+1)^3 keys per bin, a few
-    // million counters that stay in L2), so a dense bin's subproblems hold contiguous ranges
-    // of origins: every point sharing a window with another of its bin lands next to it.
-    // k_subsort then orders each subproblem by origin and refinement (point_key).  Plans
-    // without sort_origin, and grids with too many keys, sort by bin only.
+    // Global passes sort by bin and by the x and y window origin on this grid ((bs+1)^2 keys
+    // per bin), so a dense bin's subproblems hold contiguous ranges of origins and points that
+    // share a window mostly land in one subproblem; k_subsort then orders each subproblem by
+    // origin and refinement (point_key).  Keying z as well lengthens runs a little more but
+    // the scatter's write streams (4 arrays x keys) then overflow L2.  CMT_SORT_KEYS = 1..3
+    // sets the number of origin coordinates keyed, for comparison.  Plans without
+    // sort_origin, and grids with too many keys, sort by bin only.
     const int64_t O = p.bs + 1;
-    const int fine_sort = p.sort_origin && (int64_t)nbins * O * O * O < (1LL << 27) ? 2 : 0;
-    const int64_t kb = fine_sort ? O * O * O : 1;
+    int kd = 2;
+    if (const char *env = getenv("CMT_SORT_KEYS")) kd = std::min(3, std::max(1, atoi(env)));
+    const int64_t kbo = kd == 1 ? O : (kd == 2 ? O * O : O * O * O);
+    const int fine_sort = p.sort_origin && (int64_t)nbins * kbo < (1LL << 27) ? 1 + kd : 0;
+    const int64_t kb = fine_sort ? kbo : 1;
     const int nsk = (int)(O * O * O * 8);
     const int sub_smem = (int)(nsk * sizeof(int) + (size_t)p.maxsub * (sizeof(int) + 3 * sizeof(T)));
     const int64_t nkeys = (int64_t)nbins * kb;
