@@ -529,11 +529,18 @@ def main():
     ap.add_argument("--small", action="store_true", help="reduced sizes (smoke runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip pair/NUFFT/FP64/alignment extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--align", action="store_true", help="run only the orientation-matching leg and exit")
     ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full"],
                     help="run one case of each hot kernel (for ncu captures) and exit")
     args = ap.parse_args()
     if args.kernels:
         kernel_cases(args.kernels)
+        return
+    if args.align:
+        import torch
+        import cmtip_gb300.nufft as nf
+        import cmtip_gb300.alignment as alm
+        print(json.dumps({"align": align_bench(torch, nf, alm, args)}), flush=True)
         return
     rank, world, _ = rank_info()
     metric = "CG-iter s & align img/s, 5k imgs M=81: mixed-prec vs FP64 GPU at ≤1e-5 err"

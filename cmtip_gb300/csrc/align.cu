@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "cmt_common.cuh"
+#include "df.cuh"
 
 namespace cmt {
 
@@ -587,6 +588,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 // ------------------------------------------------------------------ merge + exact re-scoring
 
+__global__ void k_split_weights(const double *w, int64_t n, float2 *out)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DF d = df_from(w[i]);
+    out[i] = make_float2(d.hi, d.lo);
+}
+
 struct SegInfo {
     int mode;       // 0: SIMT layout [ref tile][image]; 1: tcgen05 layout [cta][seg][row]
     int nseg;       // mode 0: reference tiles
@@ -598,8 +607,8 @@ struct SegInfo {
 // One warp per image.  T: type of the raw model / data values (float or double).
 template <typename T>
 __global__ void k_merge_rescore(SegInfo si, const float *pscore, const int *pidx, int n_img, const T *model,
-                                const T *data, const double *w, const double *sref, int64_t n_pix, int *best_idx,
-                                double *best_d, double *second_d, int *near_tie)
+                                const T *data, const double *w, const float2 *wdf, const double *sref,
+                                int64_t n_pix, int *best_idx, double *best_d, double *second_d, int *near_tie)
 {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= n_img) return;
@@ -655,22 +664,53 @@ __global__ void k_merge_rescore(SegInfo si, const float *pscore, const int *pidx
         cand[k] = bi == 0x7fffffff ? -1 : bi;
         if (hi == bi && bi != 0x7fffffff && head < TOPK) ++head;
     }
-    // exact distances of the candidates
+    // exact distances of the candidates, d^2 = sum_p (w_p (s_r m_rp - x_ip))^2: FP64 for
+    // double inputs; for float inputs double-float arithmetic (about 48 significant bits, at
+    // FP32 rate), all eight candidates in one pass over the image
     const T *x = data + (int64_t)i * n_pix;
     double d2[TOPK];
-    for (int k = 0; k < TOPK; ++k) {
-        d2[k] = INFINITY;
-        int r = cand[k];
-        if (r < 0) continue;
-        const T *mr = model + (int64_t)r * n_pix;
-        double sr = sref[r];
-        double acc = 0.0;
-        for (int64_t p = lane; p < n_pix; p += 32) {
-            double dv = w[p] * (sr * (double)mr[p] - (double)x[p]);
-            acc += dv * dv;
+    if constexpr (sizeof(T) == 4) {
+        DF acc[TOPK], sr[TOPK];
+        const float *mr[TOPK];
+#pragma unroll
+        for (int k = 0; k < TOPK; ++k) {
+            const int r = cand[k] < 0 ? 0 : cand[k];
+            acc[k] = DF{0.0f, 0.0f};
+            sr[k] = df_from(sref[r]);
+            mr[k] = reinterpret_cast<const float *>(model) + (int64_t)r * n_pix;
         }
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        d2[k] = acc;
+        for (int64_t p = lane; p < n_pix; p += 32) {
+            const float xp = (float)x[p];
+            const float2 wp = wdf[p];
+            const DF wv{wp.x, wp.y};
+#pragma unroll
+            for (int k = 0; k < TOPK; ++k) {
+                if (cand[k] < 0) continue;  // warp-uniform
+                const DF dv = df_mul(df_add_f(df_mul_f(sr[k], mr[k][p]), -xp), wv);
+                acc[k] = df_add(acc[k], df_mul(dv, dv));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < TOPK; ++k) {
+            double a = df_to_double(acc[k]);
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            d2[k] = cand[k] < 0 ? INFINITY : a;
+        }
+    } else {
+        for (int k = 0; k < TOPK; ++k) {
+            d2[k] = INFINITY;
+            int r = cand[k];
+            if (r < 0) continue;
+            const T *mr = model + (int64_t)r * n_pix;
+            double sr = sref[r];
+            double acc = 0.0;
+            for (int64_t p = lane; p < n_pix; p += 32) {
+                double dv = w[p] * (sr * (double)mr[p] - (double)x[p]);
+                acc += dv * dv;
+            }
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            d2[k] = acc;
+        }
     }
     if (lane == 0) {
         int b1 = -1, b2 = -1;
@@ -705,6 +745,7 @@ struct Match {
     int64_t n_img = 0, n_ref = 0, n_ref_pad = 0;
     const void *data = nullptr, *model = nullptr;  // caller-owned raw values
     double *w = nullptr;                           // owned copy of the weights
+    float2 *wdf = nullptr;                         // the weights as double-float pairs
     void *opA = nullptr, *opB = nullptr;           // weighted operands (mode type)
     int64_t capA = 0, capB = 0;
     double *dsum = nullptr, *dsq = nullptr, *msum = nullptr, *msq = nullptr, *mnorm = nullptr, *sref = nullptr;
@@ -822,6 +863,7 @@ extern "C" int cmt_match_create(int64_t n_pix, int mode, void *stream, cmt_match
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaMalloc(&m->w, sizeof(double) * n_pix) != cudaSuccess || cudaMalloc(&m->cen, sizeof(double) * n_pix) != cudaSuccess ||
+        cudaMalloc(&m->wdf, sizeof(float2) * n_pix) != cudaSuccess ||
         cudaMalloc(&m->err, sizeof(int) * 2) != cudaSuccess ||
         cudaMalloc(&m->stats, sizeof(double) * 1025) != cudaSuccess) {
         set_error("match allocation failed");
@@ -839,6 +881,7 @@ extern "C" int cmt_match_set_data(cmt_match *m, int64_t n_img, const void *data,
     m->n_img = n_img;
     m->data = data;
     CMT_TRY_CUDA(cudaMemcpyAsync(m->w, weights, sizeof(double) * m->n_pix, cudaMemcpyDeviceToDevice, m->stream));
+    k_split_weights<<<(unsigned)ceil_div(m->n_pix, 256), 256, 0, m->stream>>>(m->w, m->n_pix, m->wdf);
     int64_t cap = m->capA;
     CMT_TRY(ensure(&m->opA, cap, (int64_t)op_size(m->mode) * n_img * m->Kp * m->terms));
     m->capA = cap;
@@ -954,11 +997,11 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
     unsigned blocks = (unsigned)((m->n_img * 32 + 255) / 256);
     if (m->mode == 2)
         k_merge_rescore<double><<<blocks, 256, 0, st>>>(si, m->pscore, m->pidx, (int)m->n_img, (const double *)m->model,
-                                                        (const double *)m->data, m->w, m->sref, m->n_pix, best_idx,
+                                                        (const double *)m->data, m->w, m->wdf, m->sref, m->n_pix, best_idx,
                                                         best_d, second_d, near_tie);
     else
         k_merge_rescore<float><<<blocks, 256, 0, st>>>(si, m->pscore, m->pidx, (int)m->n_img, (const float *)m->model,
-                                                       (const float *)m->data, m->w, m->sref, m->n_pix, best_idx,
+                                                       (const float *)m->data, m->w, m->wdf, m->sref, m->n_pix, best_idx,
                                                        best_d, second_d, near_tie);
     CMT_LAUNCH_CHECK();
     if (m->mode == 0 || m->mode == 3 || n_near_host) {
@@ -993,7 +1036,7 @@ extern "C" int cmt_match_stats(cmt_match *m, double *host_out)
 extern "C" int cmt_match_destroy(cmt_match *m)
 {
     if (!m) return CMT_OK;
-    void *bufs[] = {m->w, m->cen, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
+    void *bufs[] = {m->w, m->wdf, m->cen, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
                     m->ca, m->cb, m->stats, m->pscore, m->pidx, m->err, m->near, m->scratch_d};
     for (void *b : bufs) cudaFree(b);
     delete m;

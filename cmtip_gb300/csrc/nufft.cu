@@ -25,6 +25,7 @@
 
 #include "cmt_common.cuh"
 #include "nufft_plan.cuh"
+#include "df.cuh"
 
 namespace cmt {
 
@@ -141,47 +142,6 @@ __global__ void k_split_df(const double *in, int64_t n, float2 *out)
     float h = __double2float_rn(v);
     out[i] = make_float2(h, __double2float_rn(v - (double)h));
 }
-
-// ---- double-float arithmetic (Dekker 1971, Knuth TAOCP vol. 2): a value carried as an
-// unevaluated float sum hi + lo with ~48 significant bits, for the float64 coordinate
-// chain of the reference at FP32 throughput (GB300's FP64 rate is a small fraction).
-struct DF {
-    float hi, lo;
-};
-
-__device__ __forceinline__ DF df_from(double v)
-{
-    float h = __double2float_rn(v);
-    return DF{h, __double2float_rn(v - (double)h)};
-}
-
-__device__ __forceinline__ DF df_fast_two_sum(float a, float b)
-{
-    float s = __fadd_rn(a, b);
-    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-
-__device__ __forceinline__ DF df_add(DF a, DF b)
-{
-    float s = __fadd_rn(a.hi, b.hi);
-    float bb = __fsub_rn(s, a.hi);
-    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
-    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-    return df_fast_two_sum(s, e);
-}
-
-__device__ __forceinline__ DF df_mul(DF a, DF b)
-{
-    float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e = __fmaf_rn(a.hi, b.lo, e);
-    e = __fmaf_rn(a.lo, b.hi, e);
-    return df_fast_two_sum(p, e);
-}
-
-// float32 of a double-float (hi is already the nearest float of hi + lo unless lo sits on
-// half an ulp, which __fadd_rn resolves)
-__device__ __forceinline__ float df_to_float(DF a) { return __fadd_rn(a.hi, a.lo); }
 
 template <typename T>
 __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, const T *y, const T *z,
@@ -1158,8 +1118,10 @@ extern "C" int cmt_plan_create(int type, int M, int prec, double eps, int isign,
     // layout override for tuning: CMT_SPREAD_PRIV=1 spreads real strengths into per-warp
     // private subgrids instead of one subgrid with shared atomics
     if (const char *env = getenv("CMT_SPREAD_PRIV")) p->spread_priv = atoi(env) != 0;
-    // CMT_SPREAD_TAB=0 selects the per-point spreading kernel for every width, for comparison
+    // CMT_SPREAD_TAB=0 / CMT_INTERP_TAB=0 select the per-point spreading / interpolation
+    // kernels for every width, for comparison
     if (const char *env = getenv("CMT_SPREAD_TAB")) p->spread_tab = atoi(env) != 0;
+    if (const char *env = getenv("CMT_INTERP_TAB")) p->interp_tab = atoi(env) != 0;
     // Spreading plans sort each bin by window origin (long runs of shared windows across the
     // whole bin); interpolation plans sort by bin only, which costs less and loses little.
     // CMT_SORT_ORIGIN=0/1 overrides, for comparison.
@@ -1221,7 +1183,9 @@ extern "C" int cmt_plan_create_derived(const cmt_plan *src, int type, int M, int
     p->spread_ext = p->cscale == 2.0 && p->w + 1 <= 8;
     if (const char *env = getenv("CMT_SPREAD_EXT")) p->spread_ext = p->spread_ext && atoi(env) != 0;
     p->spread_tab = src->spread_tab;
+    p->interp_tab = src->interp_tab;
     if (const char *env = getenv("CMT_SPREAD_TAB")) p->spread_tab = atoi(env) != 0;
+    if (const char *env = getenv("CMT_INTERP_TAB")) p->interp_tab = atoi(env) != 0;
     p->N = src->N;
     p->nsub = src->nsub;
     p->bin_count = src->bin_count;

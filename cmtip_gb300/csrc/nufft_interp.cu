@@ -46,10 +46,28 @@ PairFn<T> pick_pair(int w)
 }
 
 template <typename T, int OUT>
+InterpFn<T> pick_interp_tab(int w)
+{
+    switch (w) {
+    case 2: return k_interp_tab<T, OUT, 2>;
+    case 3: return k_interp_tab<T, OUT, 3>;
+    case 4: return k_interp_tab<T, OUT, 4>;
+    case 5: return k_interp_tab<T, OUT, 5>;
+    case 6: return k_interp_tab<T, OUT, 6>;
+    case 7: return k_interp_tab<T, OUT, 7>;
+    case 8: return k_interp_tab<T, OUT, 8>;
+    default: return nullptr;
+    }
+}
+
+// Widths 2..8 interpolate through the per-warp point table (k_interp_tab); wider kernels
+// use the per-point kernel (k_interp).
+template <typename T, int OUT>
 int run_interp(Plan &p, int rs, void *out)
 {
-    InterpFn<T> k = pick_interp<T, OUT>(p.w);
-    int sm = (int)(sub_bytes(p) * (OUT == 0 ? 2 : 1));
+    const bool tab = p.interp_tab && p.w >= 2 && p.w <= 8;
+    InterpFn<T> k = tab ? pick_interp_tab<T, OUT>(p.w) : pick_interp<T, OUT>(p.w);
+    int sm = (int)(tab ? interp_tab_smem<T, OUT == 0>(sub_bytes(p), 8) : sub_bytes(p) * (OUT == 0 ? 2 : 1));
     CMT_TRY(prep_smem(k, sm));
     prof_begin(p);
     k<<<(unsigned)p.nsub, 256, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.perm,

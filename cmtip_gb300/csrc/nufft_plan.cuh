@@ -14,6 +14,7 @@ struct Plan {
     int spread_priv = 0;                       // real spreading into per-warp private subgrids
     int spread_ext = 0;                        // derived plan: (w+1)^3 register window per group
     int spread_tab = 1;                        // widths <= 8: table-driven spreading kernel
+    int interp_tab = 1;                        // widths <= 8: table-driven interpolation kernel
     int sort_origin = 1;                       // global sort by bin and window origin (else bin)
     double cscale = 1.0;                       // coordinate scale of borrowed points
     const Plan *points_of = nullptr;           // set: the point arrays belong to this plan

@@ -269,10 +269,79 @@ __device__ __forceinline__ void store8(T *p, const T (&v)[8])
     }
 }
 
-// Per-warp point table: 32 records of REC values, one per point of the current batch.
-//   [0, 8)   x kernel values by window column a (zero outside the point's columns)
-//   [8, 16)  y kernel values in pairs (row b, row b + 4), b < 4
-//   [16, ..) z kernel values times the strength: 8 reals, or 8 (re, im) pairs
+// Owner-lane set-up of one point for the table-driven kernels: the window origin (with EXT
+// the origin of the point's sort group on a derived plan's twice finer grid: point_key's
+// coarse origin and refinement, the fine origin then being the group origin + d, d in
+// {0,1} per dimension), the 3W kernel values, and the table record rec (16-byte aligned):
+//   [0, 8)   x values by window column a (shifted by d with EXT; zero outside the window)
+//   [8, 16)  y values in pairs (row b, row b + 4), b < 4
+//   [16, ..) z values (ZMODE 0), z values times vr (1), or (z vr, z vi) pairs (2)
+// Returns the origin key (origin_key) of the window.
+template <typename T, int W, bool EXT, int ZMODE>
+__device__ __forceinline__ int tab_prepare(T px, T py, T pz, T beta, T vr, T vi, T *rec)
+{
+    const T hw = T(0.5) * T(W), inv = T(2) / T(W);
+    const int lx = (int)ceil(px - hw), ly = (int)ceil(py - hw), lz = (int)ceil(pz - hw);
+    int gx = lx, gy = ly, gz = lz;
+    if (EXT) {
+        const int base_off = (W - 2 - (W & 1)) / 2;  // fine origin = 2 coarse origin + base_off + {0,1,2}
+        const int cx = (int)ceil(px * T(0.5) - hw), cy = (int)ceil(py * T(0.5) - hw),
+                  cz = (int)ceil(pz * T(0.5) - hw);
+        gx = 2 * cx + base_off + 2 * ((lx - 2 * cx - base_off) >> 1);
+        gy = 2 * cy + base_off + 2 * ((ly - 2 * cy - base_off) >> 1);
+        gz = 2 * cz + base_off + 2 * ((lz - 2 * cz - base_off) >> 1);
+    }
+    const int dx = lx - gx, dy = ly - gy, dz = lz - gz;  // 0 or 1 (EXT), else 0
+    T kx[W], ky[W], kz[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        const T tx = (T(lx + k) - px) * inv, ty = (T(ly + k) - py) * inv, tz = (T(lz + k) - pz) * inv;
+        kx[k] = es_eval(tx * tx, beta);
+        ky[k] = es_eval(ty * ty, beta);
+        kz[k] = es_eval(tz * tz, beta);
+    }
+    // the values by window column / row / z offset (shifted by d when EXT)
+    auto col = [&](const T(&v)[W], int d, int a) -> T {
+        const T v0 = a < W ? v[a < W ? a : 0] : T(0);
+        if (!EXT) return v0;
+        const T v1 = (a >= 1 && a - 1 < W) ? v[(a >= 1 && a - 1 < W) ? a - 1 : 0] : T(0);
+        return d ? v1 : v0;
+    };
+    T o[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) o[a] = col(kx, dx, a);
+    store8(rec, o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        o[2 * q] = col(ky, dy, q);
+        o[2 * q + 1] = col(ky, dy, q + 4);
+    }
+    store8(rec + 8, o);
+    if (ZMODE == 2) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const T z = col(kz, dz, q);
+            o[2 * q] = z * vr;
+            o[2 * q + 1] = z * vi;
+        }
+        store8(rec + 16, o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const T z = col(kz, dz, q + 4);
+            o[2 * q] = z * vr;
+            o[2 * q + 1] = z * vi;
+        }
+        store8(rec + 24, o);
+    } else {
+#pragma unroll
+        for (int a = 0; a < 8; ++a) o[a] = ZMODE == 1 ? col(kz, dz, a) * vr : col(kz, dz, a);
+        store8(rec + 16, o);
+    }
+    return origin_key(gx, gy, gz);
+}
+
+// Per-warp point table of k_spread_tab: 32 records (tab_prepare) of REC values, one per
+// point of the current batch; the z part holds 8 reals or 8 (re, im) pairs.
 template <typename T, bool CPLX>
 struct SpreadTable {
     static constexpr int REC = CPLX ? 32 : 24;
@@ -327,8 +396,6 @@ __global__ void __launch_bounds__(256) k_spread_tab(const int *sub_bin, const in
     const int cnt = min(gm.maxsub, bin_count[b] - off);
     const int p0 = bin_start[b] + off;
     const int e = lane % EW, bl = lane / EW;
-    const int base_off = (W - 2 - (W & 1)) / 2;  // fine origin = 2 * coarse origin + base_off + {0,1,2}
-    const T hw = T(0.5) * T(W), inv = T(2) / T(W);
 
     T acc[RX][NX], aci[RX][NX];
 #pragma unroll
@@ -379,66 +446,8 @@ __global__ void __launch_bounds__(256) k_spread_tab(const int *sub_bin, const in
                 vr = c[j];
             }
         }
-        const int lx = (int)ceil(px - hw), ly = (int)ceil(py - hw), lz = (int)ceil(pz - hw);
-        int gx = lx, gy = ly, gz = lz;
-        if (EXT) {
-            const int cx = (int)ceil(px * T(0.5) - hw), cy = (int)ceil(py * T(0.5) - hw),
-                      cz = (int)ceil(pz * T(0.5) - hw);
-            gx = 2 * cx + base_off + 2 * ((lx - 2 * cx - base_off) >> 1);
-            gy = 2 * cy + base_off + 2 * ((ly - 2 * cy - base_off) >> 1);
-            gz = 2 * cz + base_off + 2 * ((lz - 2 * cz - base_off) >> 1);
-        }
-        const int dx = lx - gx, dy = ly - gy, dz = lz - gz;  // 0 or 1 (EXT), else 0
-        const int my_key = origin_key(gx, gy, gz);
-        T kx[W], ky[W], kz[W];
-#pragma unroll
-        for (int k = 0; k < W; ++k) {
-            const T tx = (T(lx + k) - px) * inv, ty = (T(ly + k) - py) * inv, tz = (T(lz + k) - pz) * inv;
-            kx[k] = es_eval(tx * tx, beta);
-            ky[k] = es_eval(ty * ty, beta);
-            kz[k] = es_eval(tz * tz, beta);
-        }
-        // the values by window column / row / z offset (shifted by d when EXT)
-        auto col = [&](const T(&v)[W], int d, int a) -> T {
-            const T v0 = a < W ? v[a < W ? a : 0] : T(0);
-            if (!EXT) return v0;
-            const T v1 = (a >= 1 && a - 1 < W) ? v[(a >= 1 && a - 1 < W) ? a - 1 : 0] : T(0);
-            return d ? v1 : v0;
-        };
         __syncwarp();  // the previous batch's records have been read
-        T *rec = tab + lane * REC;
-        {
-            T o[8];
-#pragma unroll
-            for (int a = 0; a < 8; ++a) o[a] = col(kx, dx, a);
-            store8(rec, o);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                o[2 * q] = col(ky, dy, q);
-                o[2 * q + 1] = col(ky, dy, q + 4);
-            }
-            store8(rec + 8, o);
-            if (CPLX) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const T z = col(kz, dz, q);
-                    o[2 * q] = z * vr;
-                    o[2 * q + 1] = z * vi;
-                }
-                store8(rec + 16, o);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const T z = col(kz, dz, q + 4);
-                    o[2 * q] = z * vr;
-                    o[2 * q + 1] = z * vi;
-                }
-                store8(rec + 24, o);
-            } else {
-#pragma unroll
-                for (int a = 0; a < 8; ++a) o[a] = col(kz, dz, a) * vr;
-                store8(rec + 16, o);
-            }
-        }
+        const int my_key = tab_prepare<T, W, EXT, CPLX ? 2 : 1>(px, py, pz, beta, vr, vi, tab + lane * REC);
         __syncwarp();
         // ---- the warp adds the batch's points in order
         const int nq = min(32, t1 - base);
@@ -499,7 +508,7 @@ __global__ void __launch_bounds__(256) k_spread_tab(const int *sub_bin, const in
     }
 }
 
-// ------------------------------------------------------------------ interp (type 2)
+// ------------------------------------------------------------------ table-driven interp
 
 // Loads the subproblem's subgrid (padded rows; planar complex) from the fine grid.
 template <typename T, bool CPLX>
@@ -522,6 +531,129 @@ __device__ __forceinline__ void load_subgrid(const T *fine, const SubgridGeom &g
         }
     }
 }
+
+// Shared-memory bytes of k_interp_tab: the staged subgrid(s), then per warp a table of 32
+// records (24 values) and 32 x 8 partial sums (values, or (re, im) pairs).
+template <typename T, bool CPLX>
+__host__ __device__ inline size_t interp_tab_smem(size_t subgrid_bytes, int warps)
+{
+    return ((subgrid_bytes * (CPLX ? 2 : 1) + 15) & ~(size_t)15) +
+           warps * 32 * (24 + 8 * (CPLX ? 2 : 1)) * sizeof(T);
+}
+
+// Table-driven interpolation (kernel width W <= 8 fixed at compile time).  The subproblem's
+// subgrid is staged in shared memory.  Per 32-point batch, lane t prepares point t's record
+// (tab_prepare, no strength); the warp then walks the points in order: a lane keeps in
+// registers the grid values of its cells of the current window (rows bl and bl + 4 at z
+// offset e, all W columns), reloaded from the subgrid when the origin changes, and forms
+// its partial sum kz * sum_b ky sum_a kx G from the record.  Two shuffles add the four row
+// groups; the eight z lanes' sums go to the warp's partial buffer, and after the batch lane
+// t adds point t's eight partials and writes the value in caller order.
+// OUT: 0 complex values from the complex grid, 2 real values from the real grid.
+template <typename T, int OUT, int W>
+__global__ void __launch_bounds__(256) k_interp_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
+                                                    const int *bin_start, const int *perm, const T *ux,
+                                                    const T *uy, const T *uz, const T *fine, SubgridGeom gm, T beta,
+                                                    T *out)
+{
+    static_assert(W >= 2 && W <= 8, "table interpolation needs 2 <= W <= 8");
+    constexpr bool CPLX = OUT == 0;
+    constexpr int EW = 8, BR = 4, RX = (W + BR - 1) / BR, REC = 24, NC = CPLX ? 2 : 1;
+    using T2 = typename cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sg = reinterpret_cast<T *>(smem_raw);
+    const int S = gm.S, P = gm.P, h = W / 2;
+    const int plane = S * P, copy = S * plane;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const size_t sgb = ((size_t)NC * copy * sizeof(T) + 15) & ~(size_t)15;
+    T *tab = reinterpret_cast<T *>(smem_raw + sgb) + warp * 32 * (REC + 8 * NC);
+    T *part = tab + 32 * REC;  // [32 points][8 z lanes] (x NC)
+    const int b = sub_bin[blockIdx.x];
+    load_subgrid<T, CPLX>(fine, gm, b, sg);
+    __syncthreads();
+
+    const int off = sub_off[blockIdx.x];
+    const int cnt = min(gm.maxsub, bin_count[b] - off);
+    const int p0 = bin_start[b] + off;
+    const int e = lane % EW, bl = lane / EW;
+    T gr[RX][W], gi[RX][W];
+    int cur_key = -1;
+    int t0, t1;
+    warp_run(cnt, warp, nwarps, t0, t1);
+    const T cs = (T)gm.cscale;
+    for (int base = t0; base < t1; base += 32) {
+        const int tl = base + lane;
+        const bool valid = tl < t1;
+        const int pos = p0 + (valid ? tl : t0);
+        const T px = ux[pos] * cs, py = uy[pos] * cs, pz = uz[pos] * cs;
+        __syncwarp();  // the previous batch's records and partials have been read
+        const int my_key = tab_prepare<T, W, false, 0>(px, py, pz, beta, T(1), T(0), tab + lane * REC);
+        __syncwarp();
+        const int nq = min(32, t1 - base);
+        for (int q = 0; q < nq; ++q) {
+            const int key = __shfl_sync(0xffffffffu, my_key, q);  // warp-uniform
+            if (key != cur_key) {
+                cur_key = key;
+                const int X0 = (key >> 12) - 16 + h, Y0 = ((key >> 6) & 63) - 16 + h, Z0 = (key & 63) - 16 + h;
+                const int idx0 = (X0 * S + Y0 + bl) * P + Z0 + e;
+#pragma unroll
+                for (int r = 0; r < RX; ++r) {
+                    const bool ok = e < W && bl + r * BR < W;
+#pragma unroll
+                    for (int a = 0; a < W; ++a) {
+                        const int idx = idx0 + a * plane + r * BR * P;
+                        gr[r][a] = ok ? sg[idx] : T(0);
+                        if (CPLX) gi[r][a] = ok ? sg[copy + idx] : T(0);
+                    }
+                }
+            }
+            const T *rq = tab + q * REC;
+            T xv[8];
+            load8(rq, xv);
+            const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
+            const T zv = rq[16 + e];
+            T ar0 = T(0), ai0 = T(0), ar1 = T(0), ai1 = T(0);
+#pragma unroll
+            for (int a = 0; a < W; ++a) {
+                ar0 += xv[a] * gr[0][a];
+                if (CPLX) ai0 += xv[a] * gi[0][a];
+                if (RX > 1) {
+                    ar1 += xv[a] * gr[RX - 1][a];
+                    if (CPLX) ai1 += xv[a] * gi[RX - 1][a];
+                }
+            }
+            T sr = (yv.x * ar0 + yv.y * ar1) * zv;
+            T si = CPLX ? (yv.x * ai0 + yv.y * ai1) * zv : T(0);
+            sr += __shfl_xor_sync(0xffffffffu, sr, 8);
+            sr += __shfl_xor_sync(0xffffffffu, sr, 16);
+            if (CPLX) {
+                si += __shfl_xor_sync(0xffffffffu, si, 8);
+                si += __shfl_xor_sync(0xffffffffu, si, 16);
+            }
+            if (bl == 0) {
+                if (CPLX) reinterpret_cast<T2 *>(part)[q * 8 + e] = T2{sr, si};
+                else part[q * 8 + e] = sr;
+            }
+        }
+        __syncwarp();
+        if (valid) {
+            const int64_t j = perm[pos];
+            T v[8];
+            if (CPLX) {
+                T w2[8];
+                load8(part + lane * 16, v);
+                load8(part + lane * 16 + 8, w2);
+                out[2 * j] = ((v[0] + v[2]) + (v[4] + v[6])) + ((w2[0] + w2[2]) + (w2[4] + w2[6]));
+                out[2 * j + 1] = ((v[1] + v[3]) + (v[5] + v[7])) + ((w2[1] + w2[3]) + (w2[5] + w2[7]));
+            } else {
+                load8(part + lane * 8, v);
+                out[j] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ interp (type 2)
 
 // Register window of the lane (W > 0): grid values of its cells for the current origin.
 template <typename T, bool CPLX, int W>

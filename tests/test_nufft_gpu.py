@@ -214,6 +214,26 @@ def test_table_spread_matches_per_point_kernel(nf, prec, eps, cplx, monkeypatch)
     assert rel_l2(a, on.type1(x, y, z, c, M, eps=1e-13, isign=1)) < max(20 * eps, 1e-5)
 
 
+@pytest.mark.parametrize("prec,eps", [(32, 1e-2), (32, 1e-4), (32, 1e-6), (64, 1e-7), (64, 1e-5)])
+@pytest.mark.parametrize("real_out", [False, True])
+def test_table_interp_matches_per_point_kernel(nf, prec, eps, real_out, monkeypatch):
+    # widths 3..8: the table-driven interpolation kernel equals the per-point kernel and the
+    # oracle, complex output from the complex grid and real output from the real grid
+    rng = np.random.default_rng(24)
+    M, N = 24, 40000
+    x, y, z = _pts(rng, N)
+    f = rng.standard_normal((M,) * 3) + 1j * rng.standard_normal((M,) * 3)
+    pts = [torch.from_numpy(a) for a in (x, y, z)]
+    tab = nf.Plan(2, M, eps=eps, isign=-1, prec=prec).set_pts(*pts)
+    monkeypatch.setenv("CMT_INTERP_TAB", "0")
+    ref_plan = nf.Plan(2, M, eps=eps, isign=-1, prec=prec).set_pts(*pts)
+    a = tab.execute(torch.from_numpy(f), real_out=real_out).cpu().numpy()
+    b = ref_plan.execute(torch.from_numpy(f), real_out=real_out).cpu().numpy()
+    assert rel_l2(a, b) < (1e-6 if prec == 32 else 1e-13)
+    ref = on.type2(x, y, z, f, eps=1e-13, isign=-1)
+    assert rel_l2(a, ref.real if real_out else ref) < max(20 * eps, 1e-5)
+
+
 @pytest.mark.parametrize("prec", [32, 64])
 def test_pair_is_normal_operator(nf, prec):
     rng = np.random.default_rng(11)
