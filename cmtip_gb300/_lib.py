@@ -45,6 +45,13 @@ SIGNATURES = {
     "cmt_plan_profile": [_vp, _i32],
     "cmt_plan_profile_read": [_vp, _vp, _vp, _i32, ctypes.POINTER(_i32)],
     "cmt_plan_prepare_pair": [_vp],
+    "cmt_plan_set_tuning": [_vp, _i32, _i32],
+    "cmt_plan_get_tuning": [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
+    "cmt_batch_create": [_i32, _vp, _vp, ctypes.POINTER(_vp)],
+    "cmt_batch_execute": [_vp, _vp, _vp, _vp, _vp, _i32],
+    "cmt_batch_profile": [_vp, _i32],
+    "cmt_batch_last_ms": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(_i64)],
+    "cmt_batch_destroy": [_vp],
     "cmt_inverse_rotations": [_vp, _i64, _vp, _vp],
     "cmt_cg_create": [_i32, _i32, _i32, _vp, ctypes.POINTER(_vp)],
     "cmt_cg_set_kernel": [_vp, _vp],
@@ -109,3 +116,7 @@ def check(code: int):
 
 def call(name: str, *args):
     check(getattr(load(), name)(*args))
+
+
+def version() -> str:
+    return load().cmt_version().decode()

@@ -804,12 +804,20 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     const int sub_smem = (int)(nsk * sizeof(int) + (size_t)p.maxsub * (sizeof(int) + 3 * sizeof(T)));
     const int64_t nkeys = (int64_t)nbins * kb;
     const int64_t ntiles = (nkeys + 1 + SCAN_TILE - 1) / SCAN_TILE;
-    if (!p.bin_count) {
+    if (!p.dflag) {
+        CMT_TRY_CUDA(cudaMalloc(&p.dflag, sizeof(int) * 4));
+        CMT_TRY_CUDA(cudaMalloc(&p.dtot, sizeof(long long) * 2));
+    }
+    if (nbins > p.cap_bins) {  // first points, or a retuned bin size
+        cudaFree(p.bin_count);
+        cudaFree(p.bin_fill);
+        cudaFree(p.bin_start);
+        p.bin_count = p.bin_fill = p.bin_start = nullptr;
+        p.cap_bins = 0;
         CMT_TRY_CUDA(cudaMalloc(&p.bin_count, sizeof(int) * nbins));
         CMT_TRY_CUDA(cudaMalloc(&p.bin_fill, sizeof(int) * nbins));
         CMT_TRY_CUDA(cudaMalloc(&p.bin_start, sizeof(int) * nbins));
-        CMT_TRY_CUDA(cudaMalloc(&p.dflag, sizeof(int) * 4));
-        CMT_TRY_CUDA(cudaMalloc(&p.dtot, sizeof(long long) * 2));
+        p.cap_bins = nbins;
     }
     if (nkeys + 1 > p.cap_keys) {
         cudaFree(p.key_start);
@@ -895,11 +903,17 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
         return CMT_ERR_STATE;
     }
     p.N = N;
+    ++p.pts_version;
     return CMT_OK;
 }
 
+// Phases of an execute: grid preparation (zeroing; or deconvolution, padding and FFT), the
+// spreading / interpolation kernel, and the FFT and deconvolution after spreading.  A batch
+// of plans runs every plan's preparation, one kernel launch over all plans, then the rest.
+enum { PH_PRE = 1, PH_KERNEL = 2, PH_POST = 4, PH_ALL = 7 };
+
 template <typename T>
-static int exec_type1(Plan &p, const T *c, T *f, const float *support, double scale, int flags)
+static int exec_type1(Plan &p, const T *c, T *f, const float *support, double scale, int flags, int phases = PH_ALL)
 {
     bool real_in = flags & CMT_REAL_IN, real_out = flags & CMT_REAL_OUT, fftord = flags & CMT_MODEORD_FFT;
     cudaStream_t st = p.stream;
@@ -908,10 +922,13 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
     int M = p.M;
     int64_t mt = (int64_t)M * M * M;
     if (real_in) {
-        CMT_TRY(ensure_fft(p, 1));
         int rs = n + 2;
-        CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * (size_t)n * n * rs, st));
-        CMT_TRY(launch_spread(p, c, false, rs));
+        if (phases & PH_PRE) {
+            CMT_TRY(ensure_fft(p, 1));
+            CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * (size_t)n * n * rs, st));
+        }
+        if (phases & PH_KERNEL) CMT_TRY(launch_spread(p, c, false, rs));
+        if (!(phases & PH_POST)) return CMT_OK;
         if (p.prec == 64)
             CMT_TRY_CUFFT(cufftExecD2Z(p.fft_r2c, (double *)p.fine, (cufftDoubleComplex *)p.fine));
         else
@@ -926,9 +943,12 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
                                                               sgn_flip, (T)scale, f);
         CMT_LAUNCH_CHECK();
     } else {
-        CMT_TRY(ensure_fft(p, 0));
-        CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * 2 * (size_t)n * n * n, st));
-        CMT_TRY(launch_spread(p, c, true, n));
+        if (phases & PH_PRE) {
+            CMT_TRY(ensure_fft(p, 0));
+            CMT_TRY_CUDA(cudaMemsetAsync(p.fine, 0, sizeof(T) * 2 * (size_t)n * n * n, st));
+        }
+        if (phases & PH_KERNEL) CMT_TRY(launch_spread(p, c, true, n));
+        if (!(phases & PH_POST)) return CMT_OK;
         int dir = p.isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
         if (p.prec == 64)
             CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
@@ -947,7 +967,7 @@ static int exec_type1(Plan &p, const T *c, T *f, const float *support, double sc
 }
 
 template <typename T>
-static int exec_type2(Plan &p, T *c, const T *f, const float *support, double scale, int flags)
+static int exec_type2(Plan &p, T *c, const T *f, const float *support, double scale, int flags, int phases = PH_ALL)
 {
     bool real_in = flags & CMT_REAL_IN, real_out = flags & CMT_REAL_OUT, fftord = flags & CMT_MODEORD_FFT;
     CMT_CHECK_ARG(scale == 1.0, "type-2 execute takes scale = 1");
@@ -957,6 +977,10 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
     int M = p.M;
     if (real_out) {
         // Re(c) = sum_k g_k e^{isign i k.x} with g the Hermitian part of f: real fine grid
+        if (!(phases & PH_PRE)) {
+            if (phases & PH_KERNEL) CMT_TRY(launch_interp(p, 2, n + 2, c));
+            return CMT_OK;
+        }
         CMT_TRY(ensure_fft(p, 2));
         int64_t tot = (int64_t)n * n * (n / 2 + 1);
         unsigned gb = (unsigned)ceil_div(tot, 256);
@@ -972,8 +996,12 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
             CMT_TRY_CUFFT(cufftExecZ2D(p.fft_c2r, (cufftDoubleComplex *)p.fine, (double *)p.fine));
         else
             CMT_TRY_CUFFT(cufftExecC2R(p.fft_c2r, (cufftComplex *)p.fine, (float *)p.fine));
-        CMT_TRY(launch_interp(p, 2, n + 2, c));
+        if (phases & PH_KERNEL) CMT_TRY(launch_interp(p, 2, n + 2, c));
     } else {
+        if (!(phases & PH_PRE)) {
+            if (phases & PH_KERNEL) CMT_TRY(launch_interp(p, 0, n, c));
+            return CMT_OK;
+        }
         CMT_TRY(ensure_fft(p, 0));
         int64_t tot = (int64_t)n * n * n;
         unsigned gb = (unsigned)ceil_div(tot, 256);
@@ -988,7 +1016,7 @@ static int exec_type2(Plan &p, T *c, const T *f, const float *support, double sc
             CMT_TRY_CUFFT(cufftExecZ2Z(p.fft_c2c, (cufftDoubleComplex *)p.fine, (cufftDoubleComplex *)p.fine, dir));
         else
             CMT_TRY_CUFFT(cufftExecC2C(p.fft_c2c, (cufftComplex *)p.fine, (cufftComplex *)p.fine, dir));
-        CMT_TRY(launch_interp(p, 0, n, c));
+        if (phases & PH_KERNEL) CMT_TRY(launch_interp(p, 0, n, c));
     }
     return CMT_OK;
 }
@@ -1029,6 +1057,13 @@ static void sync_borrowed(Plan &p)
 {
     const Plan *s = p.points_of;
     if (!s) return;
+    if (p.nb != s->nb || p.bs != 2 * s->bs || p.maxsub != s->maxsub) {  // the source was retuned
+        p.bs = 2 * s->bs;
+        p.nb = s->nb;
+        p.S = p.bs + p.w;
+        p.P = padded_pitch(p.S, p.ew);
+        p.maxsub = s->maxsub;
+    }
     p.N = s->N;
     p.nsub = s->nsub;
     p.bin_count = s->bin_count;
@@ -1049,7 +1084,7 @@ static void unborrow(Plan &p)
     p.ux = p.uy = p.uz = nullptr;
     p.dflag = nullptr;
     p.dtot = nullptr;
-    p.cap_pts = p.cap_sub = 0;
+    p.cap_pts = p.cap_sub = p.cap_bins = 0;
     p.N = p.nsub = 0;
     p.points_of = nullptr;
     p.cscale = 1.0;
@@ -1225,6 +1260,53 @@ extern "C" int cmt_plan_info(const cmt_plan *p, int *n_fine, int *width, double 
     return CMT_OK;
 }
 
+// Largest shared-memory need of this plan's kernels (spreading / interpolation of complex
+// values through the point table, the fused pair) for bin size bs.
+static size_t plan_smem_need(const Plan &p, int bs)
+{
+    Plan q = p;
+    q.bs = bs;
+    q.S = bs + p.w;
+    q.P = padded_pitch(q.S, p.ew);
+    size_t need = 4 * sub_bytes(q);  // pair kernel: two complex subgrids
+    need = std::max(need, batch_smem(q, true, true));
+    need = std::max(need, batch_smem(q, false, true));
+    return need;
+}
+
+// Bin size (fine cells per bin edge) and points per subproblem, for the autotuner; the
+// plan's points are dropped (set_pts again).  bin_size 0 / maxsub 0 keep the current value.
+extern "C" int cmt_plan_set_tuning(cmt_plan *p, int bin_size, int maxsub)
+{
+    CMT_CHECK_ARG(p, "null plan");
+    CMT_CHECK_ARG(!p->points_of, "a derived plan follows its source's tuning");
+    if (bin_size == 0) bin_size = p->bs;
+    if (maxsub == 0) maxsub = p->maxsub;
+    CMT_CHECK_ARG(bin_size >= 2 && bin_size <= 32, "bin size %d outside [2, 32]", bin_size);
+    CMT_CHECK_ARG(maxsub >= 256 && maxsub <= (1 << 20), "points per subproblem %d outside [256, 2^20]", maxsub);
+    const size_t need = plan_smem_need(*p, bin_size);
+    CMT_CHECK_ARG(need <= 227 * 1024, "bin size %d needs %zu bytes of shared memory per CTA", bin_size, need);
+    if (bin_size != p->bs || maxsub != p->maxsub) {
+        p->bs = std::min(bin_size, p->n);
+        p->S = p->bs + p->w;
+        p->P = padded_pitch(p->S, p->ew);
+        p->nb = (p->n + p->bs - 1) / p->bs;
+        p->maxsub = maxsub;
+        p->N = 0;
+        p->nsub = 0;
+        ++p->pts_version;
+    }
+    return CMT_OK;
+}
+
+extern "C" int cmt_plan_get_tuning(const cmt_plan *p, int *bin_size, int *maxsub)
+{
+    CMT_CHECK_ARG(p, "null plan");
+    if (bin_size) *bin_size = p->bs;
+    if (maxsub) *maxsub = p->maxsub;
+    return CMT_OK;
+}
+
 extern "C" int cmt_set_pts(cmt_plan *p, int64_t N, const void *x, const void *y, const void *z)
 {
     CMT_CHECK_ARG(p && x && y && z, "null argument");
@@ -1341,6 +1423,219 @@ extern "C" int cmt_plan_destroy(cmt_plan *p)
     if (!p) return CMT_OK;
     destroy(p);
     delete p;
+    return CMT_OK;
+}
+
+// ====================================================================== batches of plans
+
+namespace cmt {
+
+// Several independent plans (one per reconstruction, each with its own modes M, points and
+// fine grid; one precision, type and kernel width) executed together: every plan's grid
+// preparation, then ONE persistent spreading / interpolation launch whose CTAs take work
+// items (plan, bin, offset) from a device counter across all plans, then every plan's FFT
+// and deconvolution.  The batch owns the concatenated work list (rebuilt when a plan gets
+// new points or new tuning) and the per-plan descriptors.
+struct Batch {
+    std::vector<cmt_plan *> plans;
+    std::vector<int64_t> versions;
+    cudaStream_t stream = nullptr;
+    WorkItem *work = nullptr;
+    int64_t cap_work = 0;
+    int nwork = 0;
+    void *inst = nullptr;       // device InstDesc array
+    void *inst_host = nullptr;  // pinned staging of the descriptors
+    cudaEvent_t staged = nullptr;
+    int *next = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+};
+
+__global__ void k_fill_work(WorkItem *work, int inst, const int *sub_bin, const int *sub_off, int64_t nsub)
+{
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nsub) work[s] = WorkItem{inst, sub_bin[s], sub_off[s]};
+}
+
+static int batch_rebuild_work(Batch &b)
+{
+    int64_t total = 0;
+    for (auto *p : b.plans) total += p->nsub;
+    CMT_CHECK_ARG(total < (1LL << 31), "batch work list too long");
+    if (total > b.cap_work) {
+        cudaFree(b.work);
+        b.work = nullptr;
+        b.cap_work = 0;
+        CMT_TRY_CUDA(cudaMalloc(&b.work, sizeof(WorkItem) * std::max<int64_t>(total, 1)));
+        b.cap_work = total;
+    }
+    int64_t base = 0;
+    for (size_t i = 0; i < b.plans.size(); ++i) {
+        Plan &p = *b.plans[i];
+        if (p.nsub > 0)
+            k_fill_work<<<ceil_div(p.nsub, 256), 256, 0, b.stream>>>(b.work + base, (int)i, p.sub_bin, p.sub_off,
+                                                                       p.nsub);
+        CMT_LAUNCH_CHECK();
+        base += p.nsub;
+        b.versions[i] = p.pts_version;
+    }
+    b.nwork = (int)total;
+    return CMT_OK;
+}
+
+template <typename T>
+static int batch_execute(Batch &b, void *const *c, void *const *f, const float *const *support,
+                         const double *scale, int flags)
+{
+    const Plan &p0 = *b.plans[0];
+    const bool t1 = p0.type == 1;
+    const bool real_in = flags & CMT_REAL_IN, real_out = flags & CMT_REAL_OUT;
+    const bool cplx = t1 ? !real_in : !real_out;
+    const int K = (int)b.plans.size();
+    for (int i = 0; i < K; ++i) {
+        Plan &p = *b.plans[i];
+        CMT_CHECK_ARG(p.N > 0, "batch plan %d has no points", i);
+        CMT_CHECK_ARG(c[i] || (t1 && real_in), "batch plan %d: null values", i);
+        CMT_CHECK_ARG(f[i], "batch plan %d: null modes", i);
+    }
+    bool stale = false;
+    for (int i = 0; i < K; ++i) stale |= b.versions[i] != b.plans[i]->pts_version;
+    std::vector<cudaStream_t> own(K);
+    for (int i = 0; i < K; ++i) {
+        own[i] = b.plans[i]->stream;
+        CMT_TRY(cmt_plan_set_stream(b.plans[i], b.stream));
+    }
+    int rc = CMT_OK;
+    auto run = [&]() -> int {
+        if (stale) CMT_TRY(batch_rebuild_work(b));
+        // 1. every plan's grid preparation
+        size_t smem = 0;
+        for (int i = 0; i < K; ++i) {
+            Plan &p = *b.plans[i];
+            if (t1) CMT_TRY(exec_type1<T>(p, (const T *)c[i], (T *)f[i], support ? support[i] : nullptr,
+                                          scale ? scale[i] : 1.0, flags, PH_PRE));
+            else CMT_TRY(exec_type2<T>(p, (T *)c[i], (const T *)f[i], support ? support[i] : nullptr, 1.0, flags,
+                                       PH_PRE));
+            smem = std::max(smem, batch_smem(p, t1, cplx));
+        }
+        // 2. the descriptors and one persistent launch over all plans' subproblems
+        CMT_TRY_CUDA(cudaEventSynchronize(b.staged));  // the previous call's copy has been read
+        InstDesc<T> *h = (InstDesc<T> *)b.inst_host;
+        for (int i = 0; i < K; ++i) {
+            Plan &p = *b.plans[i];
+            const int rs = cplx ? p.n : p.n + 2;
+            h[i] = InstDesc<T>{p.bin_count, p.bin_start, p.perm, p.ux, p.uy, p.uz,
+                               t1 ? (const void *)c[i] : (const void *)p.fine, t1 ? p.fine : c[i], geom(p, rs)};
+        }
+        CMT_TRY_CUDA(cudaMemcpyAsync(b.inst, h, sizeof(InstDesc<T>) * K, cudaMemcpyHostToDevice, b.stream));
+        CMT_TRY_CUDA(cudaEventRecord(b.staged, b.stream));
+        CMT_TRY_CUDA(cudaMemsetAsync(b.next, 0, sizeof(int), b.stream));
+        if (b.timed) CMT_TRY_CUDA(cudaEventRecord(b.ev0, b.stream));
+        if (b.nwork > 0) {
+            if (t1)
+                CMT_TRY(launch_spread_batch(p0.prec, cplx, p0.w, b.work, b.nwork, b.inst, p0.beta, b.next, smem,
+                                            b.stream));
+            else
+                CMT_TRY(launch_interp_batch(p0.prec, cplx ? 0 : 2, p0.w, b.work, b.nwork, b.inst, p0.beta, b.next,
+                                            smem, b.stream));
+        }
+        if (b.timed) CMT_TRY_CUDA(cudaEventRecord(b.ev1, b.stream));
+        // 3. every plan's FFT and deconvolution (type 1)
+        if (t1)
+            for (int i = 0; i < K; ++i)
+                CMT_TRY(exec_type1<T>(*b.plans[i], (const T *)c[i], (T *)f[i], support ? support[i] : nullptr,
+                                      scale ? scale[i] : 1.0, flags, PH_POST));
+        return CMT_OK;
+    };
+    rc = run();
+    for (int i = 0; i < K; ++i) cmt_plan_set_stream(b.plans[i], own[i]);
+    return rc;
+}
+
+}  // namespace cmt
+
+struct cmt_batch : cmt::Batch {};
+
+extern "C" int cmt_batch_destroy(cmt_batch *b);
+
+extern "C" int cmt_batch_create(int n_plans, cmt_plan *const *plans, void *stream, cmt_batch **out)
+{
+    CMT_CHECK_ARG(out && plans && n_plans >= 1, "bad argument");
+    *out = nullptr;
+    const Plan &a = *plans[0];
+    for (int i = 0; i < n_plans; ++i) {
+        CMT_CHECK_ARG(plans[i], "null plan %d", i);
+        const Plan &p = *plans[i];
+        CMT_CHECK_ARG(!p.points_of, "plan %d borrows another plan's points", i);
+        CMT_CHECK_ARG(p.type == a.type && p.prec == a.prec && p.w == a.w && p.isign == a.isign && p.beta == a.beta,
+                      "plan %d differs from plan 0 in type, precision, kernel width or sign", i);
+    }
+    CMT_CHECK_ARG(a.w >= 2 && a.w <= 8, "batches need a kernel width in 2..8 (eps >= 1e-7), got %d", a.w);
+    cmt_batch *b = new (std::nothrow) cmt_batch();
+    if (!b) return CMT_ERR_OOM;
+    b->plans.assign(plans, plans + n_plans);
+    b->versions.assign(n_plans, -1);
+    b->stream = (cudaStream_t)stream;
+    size_t desc = sizeof(InstDesc<double>) * n_plans;
+    int rc = CMT_OK;
+    if (cudaMalloc(&b->inst, desc) != cudaSuccess || cudaMallocHost(&b->inst_host, desc) != cudaSuccess ||
+        cudaMalloc(&b->next, sizeof(int)) != cudaSuccess || cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+        set_error("batch allocation failed");
+        rc = CMT_ERR_OOM;
+    }
+    if (rc == CMT_OK) rc = cudaEventRecord(b->staged, b->stream) == cudaSuccess ? CMT_OK : CMT_ERR_CUDA;
+    if (rc != CMT_OK) {
+        cmt_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return CMT_OK;
+}
+
+// c[i], f[i]: plan i's values and modes, as for cmt_execute (type 1: c in, f out; type 2:
+// f in, c out); support / scale: per-plan arrays or NULL.  Stream-ordered on the batch's
+// stream (each plan's own stream is restored afterwards).
+extern "C" int cmt_batch_execute(cmt_batch *b, void *const *c, void *const *f, const float *const *support,
+                                 const double *scale, int flags)
+{
+    CMT_CHECK_ARG(b && c && f, "null argument");
+    return b->plans[0]->prec == 64 ? batch_execute<double>(*b, c, f, support, scale, flags)
+                                   : batch_execute<float>(*b, c, f, support, scale, flags);
+}
+
+// Time (ms) of the last batched kernel launch when timing is on (CUDA events on the batch
+// stream; synchronises with it).
+extern "C" int cmt_batch_profile(cmt_batch *b, int enable)
+{
+    CMT_CHECK_ARG(b, "null batch");
+    b->timed = enable != 0;
+    return CMT_OK;
+}
+
+extern "C" int cmt_batch_last_ms(cmt_batch *b, float *ms, int64_t *n_work)
+{
+    CMT_CHECK_ARG(b && ms, "null argument");
+    *ms = 0.f;
+    if (n_work) *n_work = b->nwork;
+    if (!b->timed) return CMT_OK;
+    CMT_TRY_CUDA(cudaEventSynchronize(b->ev1));
+    CMT_TRY_CUDA(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    return CMT_OK;
+}
+
+extern "C" int cmt_batch_destroy(cmt_batch *b)
+{
+    if (!b) return CMT_OK;
+    if (b->staged) cudaEventSynchronize(b->staged);
+    cudaFree(b->work);
+    cudaFree(b->inst);
+    cudaFreeHost(b->inst_host);
+    cudaFree(b->next);
+    if (b->staged) cudaEventDestroy(b->staged);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    delete b;
     return CMT_OK;
 }
 

@@ -2,6 +2,8 @@
 #include "cmt_common.cuh"
 #include "nufft_plan.cuh"
 
+#include <algorithm>
+
 namespace cmt {
 
 #include "spread_interp.cuh"
@@ -92,7 +94,53 @@ int run_pair(Plan &p, bool prepare_only)
     return CMT_OK;
 }
 
+template <typename T, int OUT>
+using BatchFn = void (*)(const WorkItem *, int, const InstDesc<T> *, T, int *);
+
+template <typename T, int OUT>
+BatchFn<T, OUT> pick_batch(int w)
+{
+    switch (w) {
+    case 2: return k_interp_tab_batch<T, OUT, 2>;
+    case 3: return k_interp_tab_batch<T, OUT, 3>;
+    case 4: return k_interp_tab_batch<T, OUT, 4>;
+    case 5: return k_interp_tab_batch<T, OUT, 5>;
+    case 6: return k_interp_tab_batch<T, OUT, 6>;
+    case 7: return k_interp_tab_batch<T, OUT, 7>;
+    case 8: return k_interp_tab_batch<T, OUT, 8>;
+    default: return nullptr;
+    }
+}
+
+template <typename T, int OUT>
+int run_batch(int w, const WorkItem *work, int nwork, const void *inst, double beta, int *next, size_t smem,
+              cudaStream_t st)
+{
+    BatchFn<T, OUT> k = pick_batch<T, OUT>(w);
+    CMT_CHECK_ARG(k, "batched interpolation needs a kernel width in 2..8 (got %d)", w);
+    CMT_TRY(prep_smem(k, (int)smem));
+    int per_sm = 0, dev = 0, sms = 0;
+    CMT_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem));
+    CMT_TRY_CUDA(cudaGetDevice(&dev));
+    CMT_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CMT_CHECK_ARG(per_sm > 0, "batched interpolation: %zu bytes of shared memory per CTA do not fit", smem);
+    const int grid = std::max(1, std::min(nwork, per_sm * sms));
+    k<<<grid, 256, smem, st>>>(work, nwork, (const InstDesc<T> *)inst, (T)beta, next);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
 }  // namespace
+
+int launch_interp_batch(int prec, int out_mode, int w, const WorkItem *work, int nwork, const void *inst,
+                        double beta, int *next, size_t smem, cudaStream_t st)
+{
+    if (prec == 64)
+        return out_mode == 0 ? run_batch<double, 0>(w, work, nwork, inst, beta, next, smem, st)
+                             : run_batch<double, 2>(w, work, nwork, inst, beta, next, smem, st);
+    return out_mode == 0 ? run_batch<float, 0>(w, work, nwork, inst, beta, next, smem, st)
+                         : run_batch<float, 2>(w, work, nwork, inst, beta, next, smem, st);
+}
 
 int launch_interp(Plan &p, int out_mode, int rs, void *out)
 {

@@ -20,6 +20,8 @@ struct Plan {
     const Plan *points_of = nullptr;           // set: the point arrays belong to this plan
     double beta = 0.0;
     int maxsub = 8192;                         // points per subproblem (CTA)
+    int64_t pts_version = 0;                   // incremented by every set_pts
+    int64_t cap_bins = 0;                      // bins the bin arrays were allocated for
     cudaStream_t stream = nullptr;
 
     int64_t N = 0;
@@ -100,6 +102,29 @@ int prep_smem(K kernel, int bytes)
 int launch_spread(Plan &p, const void *c, bool cplx, int rs);
 int launch_interp(Plan &p, int out_mode, int rs, void *out);
 int launch_pair(Plan &p, bool prepare_only);
+
+// Batches of plans: one subproblem of one plan, and the plan's arrays and geometry.
+// Spreading: in = strengths (nullptr: ones), out = fine grid; interpolation: in = fine
+// grid, out = values in caller order.
+struct WorkItem {
+    int inst, bin, off;
+};
+template <typename T>
+struct InstDesc {
+    const int *bin_count, *bin_start, *perm;
+    const void *ux, *uy, *uz;  // T
+    const void *in;            // T
+    void *out;                 // T
+    SubgridGeom gm;
+};
+
+// One persistent launch over the work list of a batch (all plans of one precision and
+// kernel width 2..8); smem = the largest plan's shared-memory need (batch_smem).
+int launch_spread_batch(int prec, bool cplx, int w, const WorkItem *work, int nwork, const void *inst, double beta,
+                        int *next, size_t smem, cudaStream_t st);
+int launch_interp_batch(int prec, int out_mode, int w, const WorkItem *work, int nwork, const void *inst,
+                        double beta, int *next, size_t smem, cudaStream_t st);
+size_t batch_smem(const Plan &p, bool spread, bool cplx);
 
 }  // namespace cmt
 

@@ -2,6 +2,8 @@
 #include "cmt_common.cuh"
 #include "nufft_plan.cuh"
 
+#include <algorithm>
+
 namespace cmt {
 
 #include "spread_interp.cuh"
@@ -75,7 +77,64 @@ int dispatch(Plan &p, const void *c, bool cplx, int rs)
     return run<T>(p, pick<T, false, false>(p.w), c, rs, 256, one);
 }
 
+template <typename T, bool CPLX>
+using BatchFn = void (*)(const WorkItem *, int, const InstDesc<T> *, T, int *);
+
+template <typename T, bool CPLX>
+BatchFn<T, CPLX> pick_batch(int w)
+{
+    switch (w) {
+    case 2: return k_spread_tab_batch<T, CPLX, 2>;
+    case 3: return k_spread_tab_batch<T, CPLX, 3>;
+    case 4: return k_spread_tab_batch<T, CPLX, 4>;
+    case 5: return k_spread_tab_batch<T, CPLX, 5>;
+    case 6: return k_spread_tab_batch<T, CPLX, 6>;
+    case 7: return k_spread_tab_batch<T, CPLX, 7>;
+    case 8: return k_spread_tab_batch<T, CPLX, 8>;
+    default: return nullptr;
+    }
+}
+
+template <typename T, bool CPLX>
+int run_batch(int w, const WorkItem *work, int nwork, const void *inst, double beta, int *next, size_t smem,
+              cudaStream_t st)
+{
+    BatchFn<T, CPLX> k = pick_batch<T, CPLX>(w);
+    CMT_CHECK_ARG(k, "batched spreading needs a kernel width in 2..8 (got %d)", w);
+    CMT_TRY(prep_smem(k, (int)smem));
+    int per_sm = 0, dev = 0, sms = 0;
+    CMT_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem));
+    CMT_TRY_CUDA(cudaGetDevice(&dev));
+    CMT_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CMT_CHECK_ARG(per_sm > 0, "batched spreading: %zu bytes of shared memory per CTA do not fit", smem);
+    const int grid = std::max(1, std::min(nwork, per_sm * sms));
+    k<<<grid, 256, smem, st>>>(work, nwork, (const InstDesc<T> *)inst, (T)beta, next);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
 }  // namespace
+
+int launch_spread_batch(int prec, bool cplx, int w, const WorkItem *work, int nwork, const void *inst, double beta,
+                        int *next, size_t smem, cudaStream_t st)
+{
+    if (prec == 64)
+        return cplx ? run_batch<double, true>(w, work, nwork, inst, beta, next, smem, st)
+                    : run_batch<double, false>(w, work, nwork, inst, beta, next, smem, st);
+    return cplx ? run_batch<float, true>(w, work, nwork, inst, beta, next, smem, st)
+                : run_batch<float, false>(w, work, nwork, inst, beta, next, smem, st);
+}
+
+// Shared memory of the batched kernels for plan p (the batch takes the largest).
+size_t batch_smem(const Plan &p, bool spread, bool cplx)
+{
+    const size_t one = sub_bytes(p);
+    if (spread)
+        return p.prec == 64 ? (cplx ? spread_tab_smem<double, true>(one, 8) : spread_tab_smem<double, false>(one, 8))
+                            : (cplx ? spread_tab_smem<float, true>(one, 8) : spread_tab_smem<float, false>(one, 8));
+    return p.prec == 64 ? (cplx ? interp_tab_smem<double, true>(one, 8) : interp_tab_smem<double, false>(one, 8))
+                        : (cplx ? interp_tab_smem<float, true>(one, 8) : interp_tab_smem<float, false>(one, 8));
+}
 
 // Widths 2..8 spread through the per-warp point table (k_spread_tab; on a derived plan's
 // doubled grid with the extended register window); wider kernels, or a plan that asks for

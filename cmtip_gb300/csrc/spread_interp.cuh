@@ -370,10 +370,9 @@ __host__ __device__ inline size_t spread_tab_smem(size_t subgrid_bytes, int warp
 // per dimension, and the owner lane writes its values already shifted by d, so runs span
 // whole groups.  NX = W + 1 (EXT) or W columns, NX <= 8.
 template <typename T, bool CPLX, int W, bool EXT>
-__global__ void __launch_bounds__(256) k_spread_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
-                                                    const int *bin_start, const int *perm, const T *ux,
-                                                    const T *uy, const T *uz, const T *c, SubgridGeom gm, T beta,
-                                                    T *fine)
+__device__ __forceinline__ void spread_tab_sub(int b, int off, const int *bin_count, const int *bin_start,
+                                               const int *perm, const T *ux, const T *uy, const T *uz, const T *c,
+                                               const SubgridGeom &gm, T beta, T *fine)
 {
     constexpr int NX = EXT ? W + 1 : W;
     static_assert(W >= 2 && NX <= 8, "table spreading needs a window of at most 8 columns");
@@ -391,8 +390,6 @@ __global__ void __launch_bounds__(256) k_spread_tab(const int *sub_bin, const in
     for (int i = threadIdx.x; i < nch * copy; i += blockDim.x) sg[i] = T(0);
     __syncthreads();
 
-    const int b = sub_bin[blockIdx.x];
-    const int off = sub_off[blockIdx.x];
     const int cnt = min(gm.maxsub, bin_count[b] - off);
     const int p0 = bin_start[b] + off;
     const int e = lane % EW, bl = lane / EW;
@@ -508,6 +505,47 @@ __global__ void __launch_bounds__(256) k_spread_tab(const int *sub_bin, const in
     }
 }
 
+// One subproblem per CTA (sub_bin / sub_off list of one plan).
+template <typename T, bool CPLX, int W, bool EXT>
+__global__ void __launch_bounds__(256) k_spread_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
+                                                    const int *bin_start, const int *perm, const T *ux,
+                                                    const T *uy, const T *uz, const T *c, SubgridGeom gm, T beta,
+                                                    T *fine)
+{
+    spread_tab_sub<T, CPLX, W, EXT>(sub_bin[blockIdx.x], sub_off[blockIdx.x], bin_count, bin_start, perm, ux, uy, uz,
+                                    c, gm, beta, fine);
+}
+
+// ------------------------------------------------------------------ batches of plans
+
+// Persistent CTAs take the next work item from a device counter until the list is done.
+// Returns the item index (all threads of the CTA see the same value).
+__device__ __forceinline__ int next_item(int *next)
+{
+    __shared__ int item;
+    __syncthreads();  // every thread is done with the previous item
+    if (threadIdx.x == 0) item = atomicAdd(next, 1);
+    __syncthreads();
+    return item;
+}
+
+// Spreading over the subproblems of all plans of a batch (same precision, strength type and
+// kernel width; bin size, grid size and points per plan), one persistent launch.
+template <typename T, bool CPLX, int W>
+__global__ void __launch_bounds__(256) k_spread_tab_batch(const WorkItem *work, int nwork, const InstDesc<T> *inst,
+                                                          T beta, int *next)
+{
+    for (;;) {
+        const int it = next_item(next);
+        if (it >= nwork) return;
+        const WorkItem wk = work[it];
+        const InstDesc<T> d = inst[wk.inst];
+        spread_tab_sub<T, CPLX, W, false>(wk.bin, wk.off, d.bin_count, d.bin_start, d.perm, (const T *)d.ux,
+                                          (const T *)d.uy, (const T *)d.uz, (const T *)d.in, d.gm, beta,
+                                          (T *)d.out);
+    }
+}
+
 // ------------------------------------------------------------------ table-driven interp
 
 // Loads the subproblem's subgrid (padded rows; planar complex) from the fine grid.
@@ -551,10 +589,9 @@ __host__ __device__ inline size_t interp_tab_smem(size_t subgrid_bytes, int warp
 // t adds point t's eight partials and writes the value in caller order.
 // OUT: 0 complex values from the complex grid, 2 real values from the real grid.
 template <typename T, int OUT, int W>
-__global__ void __launch_bounds__(256) k_interp_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
-                                                    const int *bin_start, const int *perm, const T *ux,
-                                                    const T *uy, const T *uz, const T *fine, SubgridGeom gm, T beta,
-                                                    T *out)
+__device__ __forceinline__ void interp_tab_sub(int b, int off, const int *bin_count, const int *bin_start,
+                                               const int *perm, const T *ux, const T *uy, const T *uz, const T *fine,
+                                               const SubgridGeom &gm, T beta, T *out)
 {
     static_assert(W >= 2 && W <= 8, "table interpolation needs 2 <= W <= 8");
     constexpr bool CPLX = OUT == 0;
@@ -568,11 +605,9 @@ __global__ void __launch_bounds__(256) k_interp_tab(const int *sub_bin, const in
     const size_t sgb = ((size_t)NC * copy * sizeof(T) + 15) & ~(size_t)15;
     T *tab = reinterpret_cast<T *>(smem_raw + sgb) + warp * 32 * (REC + 8 * NC);
     T *part = tab + 32 * REC;  // [32 points][8 z lanes] (x NC)
-    const int b = sub_bin[blockIdx.x];
     load_subgrid<T, CPLX>(fine, gm, b, sg);
     __syncthreads();
 
-    const int off = sub_off[blockIdx.x];
     const int cnt = min(gm.maxsub, bin_count[b] - off);
     const int p0 = bin_start[b] + off;
     const int e = lane % EW, bl = lane / EW;
@@ -650,6 +685,32 @@ __global__ void __launch_bounds__(256) k_interp_tab(const int *sub_bin, const in
                 out[j] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
             }
         }
+    }
+}
+
+// One subproblem per CTA (sub_bin / sub_off list of one plan).
+template <typename T, int OUT, int W>
+__global__ void __launch_bounds__(256) k_interp_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
+                                                    const int *bin_start, const int *perm, const T *ux,
+                                                    const T *uy, const T *uz, const T *fine, SubgridGeom gm, T beta,
+                                                    T *out)
+{
+    interp_tab_sub<T, OUT, W>(sub_bin[blockIdx.x], sub_off[blockIdx.x], bin_count, bin_start, perm, ux, uy, uz, fine,
+                              gm, beta, out);
+}
+
+// Interpolation over the subproblems of all plans of a batch, one persistent launch.
+template <typename T, int OUT, int W>
+__global__ void __launch_bounds__(256) k_interp_tab_batch(const WorkItem *work, int nwork, const InstDesc<T> *inst,
+                                                          T beta, int *next)
+{
+    for (;;) {
+        const int it = next_item(next);
+        if (it >= nwork) return;
+        const WorkItem wk = work[it];
+        const InstDesc<T> d = inst[wk.inst];
+        interp_tab_sub<T, OUT, W>(wk.bin, wk.off, d.bin_count, d.bin_start, d.perm, (const T *)d.ux,
+                                  (const T *)d.uy, (const T *)d.uz, (const T *)d.in, d.gm, beta, (T *)d.out);
     }
 }
 

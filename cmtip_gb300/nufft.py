@@ -122,6 +122,17 @@ class Plan:
                   ctypes.byref(bs), ctypes.byref(nsub))
         return dict(n_fine=n.value, width=w.value, beta=beta.value, bin_size=bs.value, n_subproblems=nsub.value)
 
+    # -- tuning (bin size, points per subproblem); drops the points
+    def set_tuning(self, bin_size: int = 0, maxsub: int = 0) -> "Plan":
+        _lib.call("cmt_plan_set_tuning", self._h, int(bin_size), int(maxsub))
+        self.N = 0
+        return self
+
+    def tuning(self) -> dict:
+        bs, ms = ctypes.c_int(), ctypes.c_int()
+        _lib.call("cmt_plan_get_tuning", self._h, ctypes.byref(bs), ctypes.byref(ms))
+        return dict(bin_size=bs.value, maxsub=ms.value)
+
     # -- points
     def set_pts(self, x, y, z):
         dt = _real_dtype(self.prec)

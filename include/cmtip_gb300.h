@@ -119,6 +119,32 @@ int cmt_plan_set_stream(cmt_plan *plan, void *stream);
  * later cmt_execute_pair allocates nothing (e.g. inside CUDA graph capture). */
 int cmt_plan_prepare_pair(cmt_plan *plan);
 
+/* Tuning of a plan (the autotuner's knobs): bin_size = fine cells per bin edge (2..32; the
+ * shared-memory subgrid of a subproblem is (bin_size + w)^3), maxsub = points per
+ * subproblem (one CTA; 256..2^20).  0 keeps a value.  Drops the plan's points (call
+ * cmt_set_pts / cmt_set_pts_quat again).  CMT_ERR_ARG if the subgrid does not fit in shared
+ * memory.  No counterpart in the reference (finufft picks its bins internally). */
+int cmt_plan_set_tuning(cmt_plan *plan, int bin_size, int maxsub);
+int cmt_plan_get_tuning(const cmt_plan *plan, int *bin_size, int *maxsub);
+
+/* ---------------------------------------------------------------- batches of plans
+ * Many independent reconstructions in one launch per stage: a batch holds plans of one
+ * type, precision, sign and kernel width (2..8, i.e. eps >= 1e-7) but its own modes M,
+ * points, tuning and fine grid each.  cmt_batch_execute runs every plan's grid preparation,
+ * ONE persistent spreading (type 1) or interpolation (type 2) kernel over the subproblems
+ * of all plans, then every plan's FFT and deconvolution; c[i], f[i], support[i], scale[i]
+ * mean what they mean for cmt_execute on plan i (support, scale may be NULL).  Plans are
+ * borrowed (they must outlive the batch); a plan given new points or tuning is picked up
+ * by the next execute.  Stream-ordered on the batch's stream.  No counterpart in the
+ * reference, which reconstructs one particle per process. */
+typedef struct cmt_batch cmt_batch;
+int cmt_batch_create(int n_plans, cmt_plan *const *plans, void *stream, cmt_batch **batch);
+int cmt_batch_execute(cmt_batch *batch, void *const *c, void *const *f, const float *const *support,
+                      const double *scale, int flags);
+int cmt_batch_profile(cmt_batch *batch, int enable);
+int cmt_batch_last_ms(cmt_batch *batch, float *ms, int64_t *n_work);
+int cmt_batch_destroy(cmt_batch *batch);
+
 /* ---------------------------------------------------------------- CG solve
  * Solver of W x = d, W = alambda * S.conv(T, S x) + rlambda * x + flambda * S.Re(IFFT(FFT(S x).A))
  * (cmtip/autocorrelation/autocorrelation.py:113-173 setup_linops, :150-155 W_matvec) with

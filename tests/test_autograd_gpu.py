@@ -83,7 +83,7 @@ def test_chunked_least_squares_recomputes_slices(ag):
         f = torch.from_numpy(f0).cuda().requires_grad_(True)
         loss = ag.sliced_least_squares(f, quats, ppr.reshape(3, -1), rext, data, chunk=chunk, eps=1e-12)
         loss.backward()
-        out.append((float(loss), f.grad.cpu().numpy()))
+        out.append((float(loss.detach()), f.grad.cpu().numpy()))
     assert abs(out[0][0] - out[1][0]) <= 1e-10 * abs(out[0][0])
     assert rel_l2(out[1][1], out[0][1]) < 1e-10
     # same as slicing everything at once through Slice
