@@ -322,6 +322,7 @@ def gpu_arm(args):
             extras.update(pair_and_nufft(torch, nf, acm, ws, cfg, dev, N, args))
             extras.update(fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_step))
             extras["align"] = align_bench(torch, nf, alm, args)
+            extras["batch"] = batch_bench(torch, args)
         out["extras"] = extras
 
         # ---------------- end to end through the public API with host buffers
@@ -460,6 +461,138 @@ def align_bench(torch, nf, alm, args):
     return res
 
 
+# ------------------------------------------------------------------ batched reconstructions
+
+BATCH_CFG = dict(n_inst=16, seed=11, n_ref=5000, cg_iterations=20, eps=1e-6)
+
+
+def batch_instances(cfg):
+    """The seeded draw of independent reconstructions: 50-400 unit Gaussians in a sphere of
+    radius 8-20 voxels, odd M in 41..121, 200-5000 images of 4 x P^2 pixels with binning
+    8 / 4 / 2 (P = 64 / 128 / 256), uniform-random orientations."""
+    from cmtip_gb300 import geometry
+    from cmtip_gb300.batch import Instance
+    rng = np.random.default_rng(cfg["seed"])
+    inst, acs = [], []
+    for _ in range(cfg["n_inst"]):
+        n_atoms = int(rng.integers(50, 401))
+        radius = float(rng.uniform(8.0, 20.0))
+        M = int(rng.choice(np.arange(41, 122, 2)))
+        n_img = int(rng.integers(200, 5001))
+        P = 512 // int(rng.choice([8, 4, 2]))
+        rho = geometry.gaussian_particle(M, n_atoms, min(radius, 0.45 * M), rng)
+        ac = geometry.autocorrelation_of(rho).astype(np.float32)
+        ppr, rext = geometry.ewald_detector(P)
+        q = geometry.random_quaternions(n_img, rng).astype(np.float32)
+        inst.append(Instance(M, ppr.reshape(3, -1), rext / 0.9, None, q))
+        acs.append(ac)
+    return inst, acs
+
+
+def batch_bench(torch, args):
+    """Batched uneven reconstructions: every instance's slicing, orientation matching against
+    n_ref references and a fixed-iteration autocorrelation solve, one launch per NUFFT stage
+    across instances; aggregate points/s per stage and per-instance errors against the FP64
+    forms (FP64 plans at eps 1e-12 on the first images of each instance for the slices; the
+    FP64 matcher on the first 64 images; the FP64 solve for the smallest instances)."""
+    import cmtip_gb300.alignment as alm
+    import cmtip_gb300.autocorrelation as acm
+    import cmtip_gb300.nufft as nf
+    from cmtip_gb300.batch import BatchedReconstruction
+    cfg = dict(BATCH_CFG)
+    if args.small:
+        cfg.update(n_inst=4, n_ref=500)
+    inst, acs = batch_instances(cfg)
+    acs_d = [torch.from_numpy(a).cuda() for a in acs]
+    br = BatchedReconstruction(inst, eps=cfg["eps"])
+    res = {"instances": [dict(M=x.M, n_img=int(x.orientations.shape[0]), n_pix=x.n_pix) for x in inst]}
+    # warm-up of the kernels on the smallest instance
+    BatchedReconstruction(inst[:1], eps=cfg["eps"]).slices(acs_d[:1])
+    br.stats.clear()
+    sl = br.slices(acs_d)
+    for x, s in zip(inst, sl):
+        x.images = s.reshape(-1, x.n_pix)
+    matched = br.match(acs_d, cfg["n_ref"])
+    sol = br.solve(maxiter=cfg["cg_iterations"])
+    st = dict(br.stats)
+    res["stages"] = {
+        "slices": dict(s=st["slices_s"], points=st["slices_points"], pts_per_s=st["slices_points"] / st["slices_s"]),
+        "match": dict(s=st["match_slices_s"] + st["match_gemm_s"], slice_s=st["match_slices_s"],
+                      gemm_s=st["match_gemm_s"], points=st["match_slices_points"],
+                      img_per_s=sum(r["n_img"] for r in res["instances"]) / (st["match_slices_s"] + st["match_gemm_s"])),
+        "solve": dict(s=st["solve_s"], points=st["solve_points"], cg_iterations=cfg["cg_iterations"]),
+    }
+    tot_pts = st["slices_points"] + st["match_slices_points"] + st["solve_points"]
+    tot_s = st["slices_s"] + st["match_slices_s"] + st["match_gemm_s"] + st["solve_s"]
+    res["aggregate_pts_per_s"] = tot_pts / tot_s
+    res["total_s"] = tot_s
+    # errors against the FP64 forms
+    errs = []
+    order = np.argsort([x.orientations.shape[0] * x.n_pix for x in inst])
+    oracle = set(order[: max(1, len(inst) // 4)].tolist())  # FP64-oracle checks: the smallest instances
+    for i, (x, ac) in enumerate(zip(inst, acs)):
+        e = {}
+        k = min(8, x.orientations.shape[0])
+        ref = alm.compute_slices(x.orientations[:k], x.ppr.numpy(), x.rext, torch.from_numpy(ac).double().cuda(),
+                                 eps=1e-12, prec=64)
+        got = sl[i][: k * x.n_pix].double()
+        e["slices_rel_l2"] = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+        # matching, on the first k images of the instance (the data/model scale s_b is a
+        # statistic of the matched image set, so both sides match the same k images): the BF16
+        # matcher against the FP64 matcher on the same FP32 reference slices (isolates the
+        # distance GEMM and re-scoring; disagreements allowed only at FP32-rounding ties), and
+        # match_orientations in BF16 (FP32 slices at eps 1e-6) against FP64 (FP64 slices at
+        # eps 1e-12), which adds the slices' own error (disagreements expected only where the
+        # oracle's two best distances are within that error)
+        k = min(64, x.orientations.shape[0])
+        imgs = x.images[:k]
+        w = alm.generate_weights(x.ppr.numpy().reshape(3, 1, -1), order=0)
+        model = alm.compute_slices(matched[i][1]["refs"], x.ppr.numpy(), x.rext, acs_d[i], eps=cfg["eps"])
+        out = {}
+        for mode, dt in (("bf16", torch.float32), ("fp64", torch.float64)):
+            mt = alm.Matcher(x.n_pix, mode)
+            mt.set_data(imgs.to(dt), w)
+            mt.set_refs(model.to(dt).reshape(-1, x.n_pix))
+            r = mt.run()
+            out[mode] = [t.cpu().numpy() if torch.is_tensor(t) else t for t in r]
+            mt.close()
+        del model
+        diff = out["bf16"][0] != out["fp64"][0]
+        b64, s64 = out["fp64"][1], out["fp64"][2]
+        e["argmin_disagree_same_slices"] = int(diff.sum())
+        e["disagree_same_slices_outside_fp32_ties"] = int((diff & (s64 - b64 > b64 * 2.0 ** -23)).sum())
+        if i not in oracle:
+            errs.append(e)
+            continue
+        kw = dict(return_info=True)
+        _, i32 = alm.match_orientations(0, x.ppr.numpy().reshape(3, 1, -1), x.rext, imgs.reshape(k, 1, x.n_pix),
+                                        acs_d[i], cfg["n_ref"], mode="bf16", eps=cfg["eps"], **kw)
+        _, i64 = alm.match_orientations(0, x.ppr.numpy().reshape(3, 1, -1), x.rext, imgs.reshape(k, 1, x.n_pix),
+                                        acs_d[i], cfg["n_ref"], mode="fp64", eps=1e-12, **kw)
+        diff = i32["index"] != i64["index"]
+        gap = (i64["second"] - i64["best"]) / i64["best"]
+        e["argmin_disagree_vs_fp64_oracle"] = int(diff.sum())
+        e["disagree_vs_oracle_gap_above_1e-5"] = int((diff & (gap > 1e-5)).sum())
+        s64 = acm.solve_ac(0, x.ppr.numpy().reshape(3, 1, -1), x.rext, x.images.reshape(-1, 1, x.n_pix), x.M,
+                           orientations=x.orientations, maxiter=cfg["cg_iterations"], rtol=0.0, prec=64,
+                           eps=1e-12, verbose=False)
+        e["solve_rel_l2_vs_fp64"] = float(torch.linalg.norm(sol[i] - s64) / torch.linalg.norm(s64))
+        e["near_ties"] = matched[i][1]["near_ties"]
+        errs.append(e)
+    res["errors"] = errs
+    res["max_slices_rel_l2"] = max(e["slices_rel_l2"] for e in errs)
+    res["max_solve_rel_l2_vs_fp64"] = max(e["solve_rel_l2_vs_fp64"] for e in errs if "solve_rel_l2_vs_fp64" in e)
+    for key in ("argmin_disagree_same_slices", "disagree_same_slices_outside_fp32_ties",
+                "argmin_disagree_vs_fp64_oracle", "disagree_vs_oracle_gap_above_1e-5"):
+        res[key] = sum(e.get(key, 0) for e in errs)
+    res["argmin_checked_same_slices"] = sum(min(64, x.orientations.shape[0]) for x in inst)
+    res["argmin_checked_vs_oracle"] = sum(min(64, inst[i].orientations.shape[0]) for i in oracle)
+    res["oracle_instances"] = sorted(int(i) for i in oracle)
+    acm.clear_workspaces()
+    torch.cuda.empty_cache()
+    return res
+
+
 # ------------------------------------------------------------------ small kernel cases (profiling)
 
 def kernel_cases(size="small"):
@@ -530,11 +663,16 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip pair/NUFFT/FP64/alignment extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--align", action="store_true", help="run only the orientation-matching leg and exit")
+    ap.add_argument("--batch", action="store_true", help="run only the batched-reconstructions leg and exit")
     ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full"],
                     help="run one case of each hot kernel (for ncu captures) and exit")
     args = ap.parse_args()
     if args.kernels:
         kernel_cases(args.kernels)
+        return
+    if args.batch:
+        import torch
+        print(json.dumps({"batch": batch_bench(torch, args)}), flush=True)
         return
     if args.align:
         import torch

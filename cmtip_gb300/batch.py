@@ -111,3 +111,199 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Instance:
+    """One reconstruction of a batch: modes M, detector q-vectors ppr (3, n_pix) float64, the
+    reciprocal extent, measured images (n_img, n_pix) and, when known, their orientations
+    (n_img, 4) float32 quaternions."""
+
+    def __init__(self, M, ppr, reciprocal_extent, images=None, orientations=None):
+        self.M = int(M)
+        self.ppr = torch.as_tensor(np.asarray(ppr, dtype=np.float64) if not torch.is_tensor(ppr) else ppr,
+                                   dtype=torch.float64).reshape(3, -1)
+        self.rext = float(reciprocal_extent)
+        self.images = images
+        self.orientations = orientations
+
+    @property
+    def n_pix(self):
+        return self.ppr.shape[-1]
+
+
+class BatchedReconstruction:
+    """The stages of several independent reconstructions (cmtip's reconstruct loop,
+    reconstruct.py:52-87, for many particles at once), one launch per NUFFT stage:
+
+    * ``slices(acs, orientations)``: model slices Re(A_i ac_i) of every instance at the given
+      orientations (align.py:39-65), one batched type-2 launch;
+    * ``match(acs, n_ref)``: orientation matching of every instance's images against n_ref
+      reference orientations (align.py:68-132): the references' slices of a group of
+      instances in one batched launch (groups bounded by ``max_points``), then each
+      instance's tensor-core distance GEMM and exact re-scoring;
+    * ``solve(maxiter, estimates)``: every instance's autocorrelation solve
+      (autocorrelation.py:176-248 with a fixed iteration count): the Toeplitz kernels (unit
+      strengths onto 2M modes) in one batched launch, the right-hand sides (data onto M
+      modes) in another, then each instance's graph-captured CG.
+
+    ``tuning``: None (defaults), "auto" (``tune.autotune`` per instance and transform), or a
+    list of dicts (bin_size, maxsub) per instance.
+    """
+
+    def __init__(self, instances, eps=1e-6, prec=32, tuning=None, max_points=2_000_000_000, stream=None):
+        self.inst = list(instances)
+        self.eps, self.prec = float(eps), int(prec)
+        self.tuning = tuning
+        self.max_points = int(max_points)
+        self.stream = stream
+        self.stats = {}
+
+    # ---------------------------------------------------------------- helpers
+    def _tuned(self, plan, i, kind, set_points, data):
+        if self.tuning is None:
+            return plan
+        if self.tuning == "auto":
+            from . import tune
+            cfg = tune.autotune(plan.type, plan.M, set_points, data, prec=self.prec, eps=self.eps, isign=plan.isign,
+                                tag=kind)
+        else:
+            cfg = self.tuning[i]
+        return plan.set_tuning(int(cfg["bin_size"]), int(cfg["maxsub"]))
+
+    def _timed(self, name, fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        self.stats[name] = self.stats.get(name, 0.0) + e0.elapsed_time(e1) / 1e3
+        return out
+
+    # ---------------------------------------------------------------- stages
+    def _slice_group(self, idx, acs, quats, stat):
+        """Batched type-2 slices of instances idx (acs, quats aligned with idx)."""
+        from .nufft import inverse_rotations
+        rt = torch.float64 if self.prec == 64 else torch.float32
+        plans, modes = [], []
+        for k, i in enumerate(idx):
+            x = self.inst[i]
+            inv, ppr = inverse_rotations(quats[k]), x.ppr.cuda()
+            modes.append(torch.as_tensor(acs[k]).cuda().to(rt).reshape(-1))
+            p = Plan(2, x.M, eps=self.eps, isign=-1, prec=self.prec)
+            self._tuned(p, i, "slices", lambda pl, inv=inv, ppr=ppr, x=x: pl.set_pts_quat(inv, ppr, x.rext),
+                        modes[-1])
+            plans.append(p)
+
+        def run():
+            for k, i in enumerate(idx):
+                x = self.inst[i]
+                plans[k].set_pts_quat(inverse_rotations(quats[k]), x.ppr.cuda(), x.rext)
+            b = Batch(plans, stream=self.stream)
+            out = b.execute(modes, real_out=True)
+            b.close()
+            return out
+        out = self._timed(stat, run)
+        key = stat[:-2] + "_points"  # "<stage>_s" -> "<stage>_points"
+        self.stats[key] = self.stats.get(key, 0) + sum(p.N for p in plans)
+        for p in plans:
+            p.close()
+        return out
+
+    def slices(self, acs, orientations=None):
+        """Re(type-2 NUFFT of ac_i) at inv(R(q)) . ppr_i * pi / extent_i for every instance
+        (orientations default to the instances' own); list of (n_i * n_pix_i,) tensors."""
+        quats = orientations if orientations is not None else [x.orientations for x in self.inst]
+        return self._slice_group(list(range(len(self.inst))), acs, quats, "slices_s")
+
+    def match(self, acs, n_ref, mode="bf16", ref_orientations=None):
+        """Best reference orientation of every image of every instance: list of
+        (quaternions (n_img, 4) float32 numpy, info dict)."""
+        from .alignment import Matcher, generate_weights, reference_orientations
+        refs = reference_orientations(n_ref, ref_orientations=ref_orientations)  # float32, as match_orientations
+        results = [None] * len(self.inst)
+        groups, cur, pts = [], [], 0
+        for i in range(len(self.inst)):  # groups whose reference slices fit the point budget
+            n = len(refs) * self.inst[i].n_pix
+            if cur and pts + n > self.max_points:
+                groups.append(cur)
+                cur, pts = [], 0
+            cur.append(i)
+            pts += n
+        if cur:
+            groups.append(cur)
+        for g in groups:
+            models = self._slice_group(g, [acs[i] for i in g], [refs] * len(g), "match_slices_s")
+
+            def run(models=models, g=g):
+                for k, i in enumerate(g):
+                    x = self.inst[i]
+                    mt = Matcher(x.n_pix, mode)
+                    w = generate_weights(x.ppr.cpu().numpy().reshape(3, 1, -1), order=0)
+                    mt.set_data(torch.as_tensor(x.images).cuda().reshape(-1, x.n_pix), w)
+                    mt.set_refs(models[k].reshape(len(refs), x.n_pix))
+                    idx, d1, d2, tie, n_near = mt.run()
+                    index = idx.cpu().numpy().astype(np.int64)
+                    results[i] = (refs[index], dict(index=index, best=d1.cpu().numpy(), second=d2.cpu().numpy(),
+                                                    near_ties=int(n_near), refs=refs))
+                    mt.close()
+            self._timed("match_gemm_s", run)
+            del models
+        return results
+
+    def solve(self, maxiter=20, estimates=None, rtol=0.0, data=None, orientations=None):
+        """Every instance's autocorrelation solve (solve_ac with a fixed iteration count and
+        the instances' known orientations); list of float64 (M, M, M) tensors."""
+        from .autocorrelation import TOEPLITZ, CGSolver, support_from_estimate, toeplitz_kernel
+        from .nufft import inverse_rotations
+        K = len(self.inst)
+        rt = torch.float64 if self.prec == 64 else torch.float32
+        quats = orientations if orientations is not None else [x.orientations for x in self.inst]
+        plans_M, plans_2M, solvers, sups, x0s, datas, rl = [], [], [], [], [], [], []
+        for i, x in enumerate(self.inst):
+            M, Mtot = x.M, x.M ** 3
+            img = torch.as_tensor(data[i] if data is not None else x.images).cuda().reshape(-1)
+            N = img.numel()
+            p = Plan(1, M, eps=self.eps, isign=1, prec=self.prec)
+            inv = inverse_rotations(quats[i])
+            ppr = x.ppr.cuda()
+            self._tuned(p, i, "solve", lambda pl, inv=inv, ppr=ppr, x=x: pl.set_pts_quat(inv, ppr, x.rext),
+                        img.to(rt))
+            plans_M.append(p)
+            plans_2M.append(p.derive(1, 2 * M, isign=1))
+            s = CGSolver(M, prec=self.prec, op=TOEPLITZ)
+            solvers.append(s)
+            if estimates is None or estimates[i] is None:
+                sups.append(torch.ones(Mtot, dtype=torch.float32, device="cuda"))
+                x0s.append(torch.zeros(Mtot, dtype=torch.float64, device="cuda"))
+            else:
+                est = torch.as_tensor(estimates[i]).cuda().to(torch.float32).contiguous()
+                sups.append(support_from_estimate(est, inplace=True).reshape(-1))
+                x0s.append(est.reshape(-1).to(torch.float64))
+            datas.append(img.to(rt))
+            rl.append(Mtot / N / 1000)
+
+        def run():
+            for p, x, q in zip(plans_M, self.inst, quats):
+                p.set_pts_quat(inverse_rotations(q), x.ppr.cuda(), x.rext)
+            b2 = Batch(plans_2M, stream=self.stream)
+            kernels = b2.execute(None, real_out=True, fft_order=True,
+                                 scale=[1.0 / float(2 * x.M) ** 3 for x in self.inst])
+            bM = Batch(plans_M, stream=self.stream)
+            adbs = bM.execute(datas, real_out=True, support=sups, scale=[1.0 / float(x.M) ** 3 for x in self.inst])
+            outs = []
+            for i in range(K):
+                solvers[i].set_operator(sups[i], 1.0, rl[i], 1e3)
+                solvers[i].set_kernel(kernels[i])
+                d = adbs[i].reshape(-1).to(torch.float64) + rl[i] * x0s[i]
+                xsol, _ = solvers[i].solve(d, x0s[i], maxiter=maxiter, rtol=rtol)
+                outs.append(xsol.to(torch.float64).reshape((self.inst[i].M,) * 3))
+            b2.close()
+            bM.close()
+            return outs
+        out = self._timed("solve_s", run)
+        self.stats["solve_points"] = 2 * sum(p.N for p in plans_M)
+        for s in solvers:
+            s.close()
+        for p in plans_2M + plans_M:
+            p.close()
+        return out

@@ -1477,7 +1477,7 @@ static int batch_rebuild_work(Batch &b)
                                                                        p.nsub);
         CMT_LAUNCH_CHECK();
         base += p.nsub;
-        b.versions[i] = p.pts_version;
+        b.versions[i] = p.points_of ? p.points_of->pts_version : p.pts_version;
     }
     b.nwork = (int)total;
     return CMT_OK;
@@ -1494,12 +1494,18 @@ static int batch_execute(Batch &b, void *const *c, void *const *f, const float *
     const int K = (int)b.plans.size();
     for (int i = 0; i < K; ++i) {
         Plan &p = *b.plans[i];
+        sync_borrowed(p);
         CMT_CHECK_ARG(p.N > 0, "batch plan %d has no points", i);
         CMT_CHECK_ARG(c[i] || (t1 && real_in), "batch plan %d: null values", i);
         CMT_CHECK_ARG(f[i], "batch plan %d: null modes", i);
     }
     bool stale = false;
-    for (int i = 0; i < K; ++i) stale |= b.versions[i] != b.plans[i]->pts_version;
+    for (int i = 0; i < K; ++i) {
+        Plan &p = *b.plans[i];
+        sync_borrowed(p);  // a derived plan follows its source's points and tuning
+        const int64_t v = p.points_of ? p.points_of->pts_version : p.pts_version;
+        stale |= b.versions[i] != v;
+    }
     std::vector<cudaStream_t> own(K);
     for (int i = 0; i < K; ++i) {
         own[i] = b.plans[i]->stream;
@@ -1566,7 +1572,6 @@ extern "C" int cmt_batch_create(int n_plans, cmt_plan *const *plans, void *strea
     for (int i = 0; i < n_plans; ++i) {
         CMT_CHECK_ARG(plans[i], "null plan %d", i);
         const Plan &p = *plans[i];
-        CMT_CHECK_ARG(!p.points_of, "plan %d borrows another plan's points", i);
         CMT_CHECK_ARG(p.type == a.type && p.prec == a.prec && p.w == a.w && p.isign == a.isign && p.beta == a.beta,
                       "plan %d differs from plan 0 in type, precision, kernel width or sign", i);
     }

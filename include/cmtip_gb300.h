@@ -135,7 +135,8 @@ int cmt_plan_get_tuning(const cmt_plan *plan, int *bin_size, int *maxsub);
  * of all plans, then every plan's FFT and deconvolution; c[i], f[i], support[i], scale[i]
  * mean what they mean for cmt_execute on plan i (support, scale may be NULL).  Plans are
  * borrowed (they must outlive the batch); a plan given new points or tuning is picked up
- * by the next execute.  Stream-ordered on the batch's stream.  No counterpart in the
+ * by the next execute.  Derived plans (cmt_plan_create_derived) may be batched: they
+ * spread through the batch kernel without their extended register window.  Stream-ordered on the batch's stream.  No counterpart in the
  * reference, which reconstructs one particle per process. */
 typedef struct cmt_batch cmt_batch;
 int cmt_batch_create(int n_plans, cmt_plan *const *plans, void *stream, cmt_batch **batch);

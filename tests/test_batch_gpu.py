@@ -111,3 +111,39 @@ def test_autotuner_picks_a_valid_tuning(nf, tmp_path, monkeypatch):
     p = tune.apply(nf.Plan(1, 31), res).set_pts_quat(inv, pprd, rext)
     q = nf.Plan(1, 31).set_pts_quat(inv, pprd, rext)
     assert rel_l2(p.execute(data, real_out=True).cpu().numpy(), q.execute(data, real_out=True).cpu().numpy()) < 1e-6
+
+
+def test_batched_reconstruction_equals_per_instance_stages(nf):
+    # three reconstructions of different size through the batched stages, against the
+    # single-instance entry points (compute_slices, match_orientations, solve_ac)
+    from cmtip_gb300 import alignment, autocorrelation, geometry
+    from cmtip_gb300.batch import BatchedReconstruction, Instance
+    rng = np.random.default_rng(44)
+    inst, acs = [], []
+    for M, P, n_img in ((21, 16, 40), (25, 8, 60), (31, 16, 25)):
+        ppr, rext = geometry.ewald_detector(P)
+        rext /= 0.9
+        rho = geometry.gaussian_particle(M, 40, 0.3 * M, rng)
+        ac = geometry.autocorrelation_of(rho).astype(np.float32)
+        q = geometry.random_quaternions(n_img, rng).astype(np.float32)
+        inst.append(Instance(M, ppr.reshape(3, -1), rext, None, q))
+        acs.append(ac)
+    br = BatchedReconstruction(inst, eps=1e-6)
+    sl = br.slices(acs)
+    for x, ac, s in zip(inst, acs, sl):
+        ref = alignment.compute_slices(x.orientations, x.ppr.numpy(), x.rext, torch.from_numpy(ac).cuda())
+        assert rel_l2(s.cpu().numpy(), ref.cpu().numpy()) < 1e-6
+        x.images = s.reshape(-1, x.n_pix)
+    refs = geometry.uniform_quaternions(300)
+    res = br.match(acs, 300, ref_orientations=refs)
+    for x, ac, (q, info) in zip(inst, acs, res):
+        q1, info1 = alignment.match_orientations(0, x.ppr.numpy().reshape(3, 1, -1), x.rext,
+                                                 x.images.reshape(-1, 1, x.n_pix), torch.from_numpy(ac).cuda(), 300,
+                                                 ref_orientations=refs, return_info=True)
+        assert np.array_equal(info["index"], info1["index"])
+    sol = br.solve(maxiter=10)
+    for x, s in zip(inst, sol):
+        ref = autocorrelation.solve_ac(0, x.ppr.numpy().reshape(3, 1, -1), x.rext,
+                                       x.images.reshape(-1, 1, x.n_pix), x.M, orientations=x.orientations,
+                                       maxiter=10, rtol=0.0, verbose=False)
+        assert rel_l2(s.cpu().numpy(), ref.cpu().numpy() if torch.is_tensor(ref) else ref) < 1e-4
