@@ -322,6 +322,7 @@ def gpu_arm(args):
             extras.update(pair_and_nufft(torch, nf, acm, ws, cfg, dev, N, args))
             extras.update(fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_step))
             extras["align"] = align_bench(torch, nf, alm, args)
+            extras["tikhonov"] = tikhonov_bench(torch, args)
             extras["batch"] = batch_bench(torch, args)
         out["extras"] = extras
 
@@ -458,6 +459,59 @@ def align_bench(torch, nf, alm, args):
         res[mode]["argmin_disagree_vs_fp64"] = int(diff.sum())
         res[mode]["disagree_outside_fp32_ties"] = int((diff & ~tie).sum())
     res["speedup_bf16_vs_fp64_form"] = res["fp64"]["s"] / res["bf16"]["s"]
+    return res
+
+
+# ------------------------------------------------------------------ weighted Tikhonov solve
+
+TIKH_CFG = dict(M=101, n_img=5000, P=128, maxiter=50, lam=1e-3, eps=1e-6, seed=13)
+
+
+def tikhonov_bench(torch, args):
+    """Weighted-L2 + Tikhonov (lam = 1e-3) autocorrelation solve at M = 101 from 5000 images x
+    4 x 128^2 pixels with known orientations, 50 CG iterations: the mixed-precision Toeplitz
+    form, its FP64 form (eps 1e-12) and the slice-recomputing pair form (unweighted)."""
+    import cmtip_gb300.alignment as alm
+    import cmtip_gb300.autocorrelation as acm
+    from cmtip_gb300 import geometry
+    cfg = dict(TIKH_CFG)
+    if args.small:
+        cfg.update(n_img=200, M=41)
+    rng = np.random.default_rng(cfg["seed"])
+    M = cfg["M"]
+    ppr, rext = geometry.ewald_detector(cfg["P"])
+    rext /= 0.9
+    rho = geometry.gaussian_particle(M, CFG["n_atoms"], CFG["radius"], rng)
+    ac = geometry.autocorrelation_of(rho).astype(np.float32)
+    quats = geometry.random_quaternions(cfg["n_img"], rng).astype(np.float32)
+    b = alm.compute_slices(torch.from_numpy(quats), ppr, rext, torch.from_numpy(ac).cuda(), eps=1e-7)
+    n_pix = ppr.shape[-1]
+    b = b.reshape(cfg["n_img"], 1, n_pix)
+    w = rng.uniform(0.5, 2.0, n_pix)
+    res = {"M": M, "n_images": cfg["n_img"], "pixels_per_image": n_pix, "points": cfg["n_img"] * n_pix,
+           "cg_iterations": cfg["maxiter"], "lam": cfg["lam"], "weights": "per pixel, uniform in [0.5, 2]"}
+
+    def timed(**kw):
+        acm.solve_tikhonov(ppr, rext, b, M, quats, lam=cfg["lam"], maxiter=2, **kw)  # warm-up (plans, graph)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        x = acm.solve_tikhonov(ppr, rext, b, M, quats, lam=cfg["lam"], maxiter=cfg["maxiter"], **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        return x, e0.elapsed_time(e1) / 1e3
+
+    x32, t32 = timed(weights=w, prec=32, eps=cfg["eps"])
+    x64, t64 = timed(weights=w, prec=64, eps=1e-12)
+    acm.clear_workspaces()
+    xu, tu = timed(weights=None, prec=32, eps=cfg["eps"])
+    xp, tp = timed(weights=None, prec=32, eps=cfg["eps"], operator="pair")
+    acm.clear_workspaces()
+    rel = lambda a, r: float(torch.linalg.norm(a - r) / torch.linalg.norm(r))
+    res.update(solve_s=t32, s_per_iteration=t32 / cfg["maxiter"], fp64_solve_s=t64, speedup_vs_fp64_form=t64 / t32,
+               rel_l2_mixed_vs_fp64=rel(x32, x64), pair_solve_s=tp, pair_s_per_iteration=tp / cfg["maxiter"],
+               unweighted_toeplitz_solve_s=tu, rel_l2_pair_vs_toeplitz=rel(xp, xu))
+    torch.cuda.empty_cache()
     return res
 
 
@@ -664,11 +718,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--align", action="store_true", help="run only the orientation-matching leg and exit")
     ap.add_argument("--batch", action="store_true", help="run only the batched-reconstructions leg and exit")
+    ap.add_argument("--tikhonov", action="store_true", help="run only the weighted Tikhonov solve leg and exit")
     ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full"],
                     help="run one case of each hot kernel (for ncu captures) and exit")
     args = ap.parse_args()
     if args.kernels:
         kernel_cases(args.kernels)
+        return
+    if args.tikhonov:
+        import torch
+        print(json.dumps({"tikhonov": tikhonov_bench(torch, args)}), flush=True)
         return
     if args.batch:
         import torch

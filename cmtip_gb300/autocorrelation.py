@@ -266,3 +266,70 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
     if return_info:
         return out, {"iterations": iters, "d": d, "x0": x0, "solver": solver}
     return out
+
+
+def solve_tikhonov(pixel_position_reciprocal, reciprocal_extent, slices_, M, orientations, weights=None, lam=1e-3,
+                   maxiter=50, rtol=0.0, prec=32, eps=DEFAULT_EPS, operator="toeplitz", x0=None, use_graph=True,
+                   return_info=False):
+    """Weighted least squares with Tikhonov regularisation for the autocorrelation, on the GPU:
+
+        argmin_x  1/(2 M^3) sum_j w_j (Re(A x)_j - b_j)^2 + lam/2 |x|^2
+
+    with A the slicing operator of align.py:39-65 (type 2, isign -1, without its 1/M^3) at
+    the rotated q-points inv(R(q)) . ppr * pi / extent, x real on M^3 modes, by CG on the
+    normal equations (A^H W A / M^3 + lam I) x = Re(A^H W b) / M^3 -- the operator family of
+    autocorrelation.py:113-173 (setup_linops) with weights on both sides, lam as the ridge
+    term, no Fourier-domain term, and consistent scaling.  For the centrosymmetric real x an
+    autocorrelation is, Re(A^H W A) x equals Re(A)^T W Re(A) x, so the CG iterates (started
+    from a symmetric x0) solve the real least-squares problem.
+
+    weights: per pixel (n_pix,) or per point (n_img * n_pix,); None means 1.
+    operator "toeplitz": A^H W A as the (2M)^3 convolution with the type-1 transform of the
+    weights (one spread of N weights, then no N-sized work per iteration); "pair": A^H A
+    applied by the fused type-2 -> type-1 pair each iteration, recomputing the slices on the
+    fly instead of storing them (unweighted only).  FP64 dot products, norms and step
+    scalars in both precisions; the iteration is captured in a CUDA graph."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    numpy_io = not torch.is_tensor(slices_)
+    Mtot = M ** 3
+    rt = torch.float64 if prec == 64 else torch.float32
+    ppr = _as_device(pixel_position_reciprocal, torch.float64).reshape(3, -1)
+    n_pix = ppr.shape[-1]
+    quats = orientations if torch.is_tensor(orientations) else np.asarray(orientations, dtype=np.float32)
+    inv_rot = inverse_rotations(quats, device=dev)
+    data = _as_device(slices_, torch.float32).reshape(-1)
+    N = data.numel()
+    w = None
+    if weights is not None:
+        w = _as_device(weights, torch.float64).reshape(-1)
+        if w.numel() == n_pix:
+            w = w.repeat(N // n_pix)
+        if w.numel() != N:
+            raise ValueError(f"weights must have n_pix ({n_pix}) or N ({N}) entries")
+    op = PAIR if operator == "pair" else TOEPLITZ
+    if op == PAIR and w is not None:
+        raise ValueError("the pair operator applies unweighted A^H A; use operator='toeplitz' with weights")
+    x0 = torch.zeros(Mtot, dtype=torch.float64, device=dev) if x0 is None else \
+        _as_device(x0, torch.float64).reshape(-1).clone()
+    ws = _workspace(M, prec, op, eps, dev)
+    solver, plan_M, plan_2M = ws.solver, ws.plan_M, ws.plan_2M
+    ones = torch.ones(Mtot, dtype=torch.float32, device=dev)
+    # W = alambda * A^H W A / (8 M^3) (the Toeplitz kernel and the pair carry 1/(2M)^3) + lam I
+    solver.set_operator(ones, 8.0, float(lam), 0.0)
+    plan_M.set_pts_quat(inv_rot, ppr, float(reciprocal_extent))
+    if op == TOEPLITZ:
+        M2 = 2 * M
+        kern = plan_2M.execute(None if w is None else w.to(rt), scale=1.0 / float(M2) ** 3, real_out=True,
+                               fft_order=True)
+        solver.set_kernel(kern)
+    else:
+        solver.set_pair_plan(plan_M)
+    wb = data.to(torch.float64) * w if w is not None else data
+    adb = plan_M.execute(wb.to(rt), scale=1.0 / float(M) ** 3, real_out=True).reshape(-1)
+    d = adb.to(torch.float64)
+    x, iters = solver.solve(d, x0, maxiter=maxiter, rtol=rtol, use_graph=use_graph)
+    out = x.to(torch.float64).reshape((M,) * 3)
+    out = out.cpu().numpy() if numpy_io else out
+    if return_info:
+        return out, {"iterations": iters, "d": d}
+    return out

@@ -122,3 +122,43 @@ def test_converged_early_stops_like_scipy(ac_mod, golden):
     x, it = W.solver.solve(torch.from_numpy(d), torch.from_numpy(s["x0"].astype(np.float64)), maxiter=200, rtol=1e-3)
     assert it == count[0]
     assert rel_l2(x.cpu().numpy(), xr) < 1e-9
+
+
+@pytest.mark.parametrize("operator,weighted", [("toeplitz", True), ("toeplitz", False), ("pair", False)])
+def test_tikhonov_solve_matches_dense_normal_equations(ac_mod, operator, weighted):
+    # weighted L2 + Tikhonov (config 3's objective) against the dense normal equations built
+    # from exact direct sums: (Re(A)^T W Re(A) / M^3 + lam I) x = Re(A)^T W b / M^3
+    from cmtip_gb300 import geometry
+    from oracle import nufft as on
+    rng = np.random.default_rng(61)
+    M, P, n_img, lam = 9, 8, 12, 1e-3
+    ppr, rext = geometry.ewald_detector(P)
+    rext /= 0.9
+    quats = geometry.random_quaternions(n_img, rng).astype(np.float32)
+    H, K, L = rp.gen_nonuniform_positions(quats, ppr)
+    # the reference's chain float32(H) / extent * pi, evaluated in float64 (extent is float64)
+    x, y, z = [a.astype(np.float32).ravel().astype(np.float64) / np.float64(rext) * np.pi for a in (H, K, L)]
+    k = on.modes(M).astype(np.float64)
+    ex, ey, ez = (np.exp(-1j * np.multiply.outer(a, k)) for a in (x, y, z))
+    Ar = np.einsum("ja,jb,jc->jabc", ex, ey, ez).reshape(x.size, M ** 3).real
+    rho = geometry.gaussian_particle(M, 10, 2.5, rng)
+    b = Ar @ geometry.autocorrelation_of(rho).ravel()
+    b *= 1.0 + 0.01 * rng.standard_normal(b.size)
+    n_pix = ppr.shape[-1]
+    w_pix = rng.uniform(0.5, 2.0, n_pix) if weighted else np.ones(n_pix)
+    w = np.tile(w_pix, n_img)
+    lhs = Ar.T @ (w[:, None] * Ar) / M ** 3 + lam * np.eye(M ** 3)
+    xd = np.linalg.solve(lhs, Ar.T @ (w * b) / M ** 3)
+    got, info = ac_mod.solve_tikhonov(ppr, rext, b.reshape(n_img, 1, n_pix), M, quats,
+                                      weights=w_pix if weighted else None, lam=lam, maxiter=2000, rtol=1e-13,
+                                      prec=64, eps=1e-12, operator=operator, return_info=True)
+    assert rel_l2(got, xd.reshape((M,) * 3)) < 1e-7, info["iterations"]
+    # The mixed-precision form after 50 fixed iterations against FP64.  At lam = 1e-3 this
+    # 729-unknown problem has condition ~4e3 and CG is far from converged after 50 iterations,
+    # where FP32 rounding of the operator moves the iterate by ~1e-3; lam = 0.1 gives the
+    # conditioning of the full-size problem (M = 101 from 3.3e8 points, checked at 1e-4 by
+    # the benchmark's Tikhonov leg).
+    kw = dict(weights=w_pix if weighted else None, lam=0.1, maxiter=50, operator=operator)
+    g32 = ac_mod.solve_tikhonov(ppr, rext, b.reshape(n_img, 1, n_pix), M, quats, prec=32, eps=1e-6, **kw)
+    g64 = ac_mod.solve_tikhonov(ppr, rext, b.reshape(n_img, 1, n_pix), M, quats, prec=64, eps=1e-12, **kw)
+    assert rel_l2(g32, g64) < TOL_AC
