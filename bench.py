@@ -459,6 +459,21 @@ def align_bench(torch, nf, alm, args):
         res[mode]["argmin_disagree_vs_fp64"] = int(diff.sum())
         res[mode]["disagree_outside_fp32_ties"] = int((diff & ~tie).sum())
     res["speedup_bf16_vs_fp64_form"] = res["fp64"]["s"] / res["bf16"]["s"]
+    # multi-conformation matching (align.py:135-213): the same images against two volumes
+    # (the particle and a second one), the references sorted once
+    rho2 = geometry.gaussian_particle(cfg["M"], CFG["n_atoms"], CFG["radius"], np.random.default_rng(cfg["seed"] + 1))
+    vols = [acd, torch.from_numpy(geometry.autocorrelation_of(rho2).astype(np.float32)).cuda()]
+    kw = dict(ref_orientations=refs, mode="bf16", return_info=True)
+    alm.match_orientations_mult(0, ppr, rext, img, vols, cfg["n_ref"], **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    q, conf, info = alm.match_orientations_mult(0, ppr, rext, img, vols, cfg["n_ref"], **kw)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    res["multi_conformation_2vol"] = {"img_per_s": cfg["n_img"] / t, "s": t,
+                                      "assigned_to_true_volume": float(np.mean(conf == 0)),
+                                      "argmin_equal_to_single_volume_bf16": int(np.sum(info["index"] == idx["bf16"]["index"])),
+                                      "volume_ties": info["volume_ties"]}
     return res
 
 

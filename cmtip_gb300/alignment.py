@@ -166,3 +166,50 @@ def match_orientations(generation, pixel_position_reciprocal, reciprocal_extent,
         return out, dict(index=index, best=d1.cpu().numpy(), second=d2.cpu().numpy(),
                          near_ties=int(n_near), refs=refs)
     return out
+
+
+def match_orientations_mult(generation, pixel_position_reciprocal, reciprocal_extent, slices_, ac_mult,
+                            n_ref_orientations, nbatches=1, order=0, use_gpu=True, true_orientations=None, *,
+                            ref_orientations=None, mode="bf16", eps=DEFAULT_EPS, return_info=False):
+    """align.py:135-213 on the GPU: every image matched against each volume of ``ac_mult``
+    (n_volumes, M, M, M), then assigned to the volume with the smallest best distance (first
+    index on ties) and that volume's best reference.  The references are sorted once for all
+    volumes and the images' operands built once; each volume costs one type-2 execute, one
+    distance GEMM and one re-scoring.  Returns (quaternions float32 numpy, conformations
+    int64 numpy)."""
+    refs = reference_orientations(n_ref_orientations, nbatches, true_orientations, ref_orientations)
+    n_ref = refs.shape[0]
+    n_pix = int(np.asarray(pixel_position_reciprocal).shape[-1]) if not torch.is_tensor(pixel_position_reciprocal) \
+        else int(pixel_position_reciprocal.shape[-1])
+    prec = 64 if mode == "fp64" else 32
+    rt = torch.float64 if prec == 64 else torch.float32
+    vols = [a if torch.is_tensor(a) else torch.from_numpy(np.ascontiguousarray(a)) for a in ac_mult]
+    M = vols[0].shape[0]
+    plan = get_plan(2, M, eps=eps, isign=-1, prec=prec)
+    plan.set_pts_quat(inverse_rotations(refs), _ppr2d(pixel_position_reciprocal), float(reciprocal_extent))
+    data = slices_ if torch.is_tensor(slices_) else torch.from_numpy(np.ascontiguousarray(slices_))
+    data = data.to("cuda").reshape(-1, n_pix)
+    weights = generate_weights(pixel_position_reciprocal if not torch.is_tensor(pixel_position_reciprocal)
+                               else pixel_position_reciprocal.cpu().numpy(), order=order)
+    mt = _matcher(n_pix, mode)
+    mt.set_data(data, weights)
+    idx_all, best_all, near_all = [], [], []
+    for v in vols:
+        model = plan.execute(v.to("cuda", rt).reshape(-1), real_out=True)
+        mt.set_refs(model.reshape(n_ref, n_pix), nbatches=nbatches)
+        idx, d1, d2, tie, n_near = mt.run()
+        for s in mt.stats()[:-1]:
+            print(f"Data/Model std ratio: {s}.", flush=True)
+        idx_all.append(idx.cpu().numpy().astype(np.int64))
+        best_all.append(d1.cpu().numpy())
+        near_all.append(int(n_near))
+    best = np.stack(best_all)
+    conformations = np.argmin(best, axis=0)
+    index = np.stack(idx_all)[conformations, np.arange(best.shape[1])]
+    out = refs[index], conformations
+    if return_info:
+        srt = np.sort(best, axis=0)
+        # volumes whose best distances are within one FP32 rounding of each other
+        vol_ties = int(np.sum(srt[1] - srt[0] <= srt[0] * 2.0 ** -23)) if best.shape[0] > 1 else 0
+        return out + (dict(index=index, best=best, near_ties=near_all, volume_ties=vol_ties, refs=refs),)
+    return out

@@ -211,3 +211,21 @@ def match_orientations(pixel_position_reciprocal, reciprocal_extent, slices_, ac
     if return_distances:
         return ref_orientations[index], index, distances
     return ref_orientations[index], index
+
+
+def match_orientations_mult(pixel_position_reciprocal, reciprocal_extent, slices_, ac_mult, ref_orientations,
+                            nbatches=1, order=0, eps=NUFFT_EPS):
+    """align.py:135-213 on given reference orientations: every image matched against each
+    volume (match_orientations per volume), then the volume with the smallest best distance
+    (first index on ties) and that volume's best reference.  Returns (quats, conformations)."""
+    n_img = slices_.shape[0]
+    indices = np.zeros((len(ac_mult), n_img), dtype=np.int64)
+    min_dists = np.zeros((len(ac_mult), n_img))
+    for k, ac in enumerate(ac_mult):
+        _, idx, dist = match_orientations(pixel_position_reciprocal, reciprocal_extent, slices_, ac,
+                                          ref_orientations, nbatches=nbatches, order=order, eps=eps,
+                                          return_distances=True)
+        indices[k], min_dists[k] = idx, dist.min(axis=0)
+    conformations = np.argmin(min_dists, axis=0)
+    index = indices[conformations, np.arange(n_img)]
+    return ref_orientations[index], conformations

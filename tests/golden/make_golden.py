@@ -149,6 +149,26 @@ def main():
                         slices=case["slices"], w0=w0, w2=w2, w1=w1, slices_model=sl,
                         ref_q=ref_q, dist=dist, matched=matched, shuffled_refs=ref_list)
     out["alignment"] = (matched.shape,)
+
+    # 4. multi-conformation alignment (align.py:135-213): images of two particles, each
+    #    matched against both volumes; true orientations spliced into the references
+    ca = synthetic_case(M=21, n_img=4, P=8, n_atoms=20, radius=4.0, seed=31)
+    cb = synthetic_case(M=21, n_img=4, P=8, n_atoms=25, radius=5.0, seed=32)
+    slices_m = np.concatenate([ca["slices"], cb["slices"]])
+    quats_m = np.concatenate([ca["quats"], cb["quats"]])
+    ac_mult = np.stack([ca["ac"], cb["ac"]])
+    np.random.seed(7)
+    q_mult, conf = ref_al.match_orientations_mult(0, ca["ppr"], ca["rext"], slices_m.copy(), ac_mult, 60,
+                                                  nbatches=2, order=0, use_gpu=False,
+                                                  true_orientations=quats_m)
+    np.random.seed(7)
+    ref_m = geometry.uniform_quaternions(60).astype(np.float32)
+    ref_m = np.vstack((ref_m[:-len(quats_m)], quats_m))
+    np.random.shuffle(ref_m)
+    np.savez_compressed(os.path.join(HERE, "alignment_mult.npz"),
+                        ppr=ca["ppr"], rext=ca["rext"], slices=slices_m, quats=quats_m, ac_mult=ac_mult,
+                        shuffled_refs=ref_m, matched=q_mult, conformations=conf)
+    out["alignment_mult"] = (q_mult.shape, conf.tolist())
     print(out)
 
 

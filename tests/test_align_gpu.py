@@ -122,3 +122,15 @@ def test_bf16_matches_fp32_form_larger(al):
     tie = (a["second"] - a["best"]) <= a["best"] * 2.0 ** -22
     assert not (diff & ~tie).any()
     assert np.allclose(a["best"], b["best"], rtol=1e-6)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_multi_conformation_matches_reference(al, golden, mode):
+    # align.py:135-213 through the unmodified reference: two volumes, nbatches 2
+    g = golden("alignment_mult")
+    np.random.seed(7)
+    q, conf = al.match_orientations_mult(0, g["ppr"], g["rext"], g["slices"], g["ac_mult"], 60, nbatches=2,
+                                         order=0, true_orientations=g["quats"],
+                                         ref_orientations=geometry.uniform_quaternions(60), mode=mode)
+    assert np.array_equal(conf, g["conformations"])
+    assert np.array_equal(q, g["matched"])

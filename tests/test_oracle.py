@@ -128,3 +128,15 @@ def test_alignment_matches_reference(golden):
     q, idx = rp.match_orientations(g["ppr"], g["rext"], g["slices"], g["ac"], refs, nbatches=2)
     assert np.array_equal(q, g["matched"])
     assert np.array_equal(q, g["quats"])  # cmtip/tests/test_align.py:60: true orientations recovered
+
+
+def test_multi_conformation_alignment_matches_reference(golden):
+    # align.py:135-213: two volumes, true orientations spliced into 60 references, nbatches 2
+    g = golden("alignment_mult")
+    rng = np.random.RandomState(7)
+    refs = rp.reference_orientations(60, nbatches=2, true_orientations=g["quats"],
+                                     ref_orientations=geometry.uniform_quaternions(60), shuffle_rng=rng)
+    assert np.array_equal(refs, g["shuffled_refs"])
+    q, conf = rp.match_orientations_mult(g["ppr"], g["rext"], g["slices"], g["ac_mult"], refs, nbatches=2)
+    assert np.array_equal(conf, g["conformations"])
+    assert np.array_equal(q, g["matched"])
