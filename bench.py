@@ -322,6 +322,7 @@ def gpu_arm(args):
             extras.update(pair_and_nufft(torch, nf, acm, ws, cfg, dev, N, args))
             extras.update(fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_step))
             extras["align"] = align_bench(torch, nf, alm, args)
+            extras["prep"] = prep_bench(torch, slices, ppr, cfg)
             extras["tikhonov"] = tikhonov_bench(torch, args)
             extras["batch"] = batch_bench(torch, args)
         out["extras"] = extras
@@ -475,6 +476,37 @@ def align_bench(torch, nf, alm, args):
                                       "argmin_equal_to_single_volume_bf16": int(np.sum(info["index"] == idx["bf16"]["index"])),
                                       "volume_ties": info["volume_ties"]}
     return res
+
+
+# ------------------------------------------------------------------ data preparation
+
+def prep_bench(torch, slices, ppr, cfg):
+    """Detector binning (2 x 2) fused with resolution clipping of the step's image stack
+    (5000 x 4 x 256^2 float32, 5.2 GB) on the device; HBM fraction of the pass."""
+    from cmtip_gb300 import prep
+    det_shape = (4, cfg["P"], cfg["P"])
+    ppr_b = prep.bin_data(ppr, 2, det_shape)
+    res = 1e10 / np.linalg.norm(ppr_b, axis=0)
+    res_limit = float(np.quantile(res, 0.25))  # keeps the three quarters of lower resolution
+    keep = prep.kept_indices(ppr_b, res_limit)
+    x = slices.reshape(slices.shape[0], -1)
+    run = lambda: prep._bin_clip_dev(x, 4, cfg["P"], cfg["P"], 2, keep)
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record()
+    for _ in range(reps):
+        out = run()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / reps
+    n_img = x.shape[0]
+    alg = n_img * len(keep) * (4 + 1) * 4  # 2 x 2 source values read + 1 written per kept pixel
+    peaks = measured_peaks()
+    return {"images": n_img, "pixels_in": x.shape[1], "pixels_kept": int(len(keep)), "bin": 2,
+            "s": t, "GB_per_s": alg / t / 1e9, "hbm_frac": alg / t / 1e9 / peaks["hbm_gbs"],
+            "note": "bin_data + clip_data in one pass (keep indices synchronise once per call)"}
 
 
 # ------------------------------------------------------------------ weighted Tikhonov solve

@@ -52,6 +52,7 @@ SIGNATURES = {
     "cmt_batch_profile": [_vp, _i32],
     "cmt_batch_last_ms": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(_i64)],
     "cmt_batch_destroy": [_vp],
+    "cmt_bin_clip": [_i32, _vp, _i64, _i32, _i32, _i32, _i32, _vp, _i64, _vp, _vp],
     "cmt_inverse_rotations": [_vp, _i64, _vp, _vp],
     "cmt_cg_create": [_i32, _i32, _i32, _vp, ctypes.POINTER(_vp)],
     "cmt_cg_set_kernel": [_vp, _vp],

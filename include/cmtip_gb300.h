@@ -127,6 +127,17 @@ int cmt_plan_prepare_pair(cmt_plan *plan);
 int cmt_plan_set_tuning(cmt_plan *plan, int bin_size, int maxsub);
 int cmt_plan_get_tuning(const cmt_plan *plan, int *bin_size, int *maxsub);
 
+/* ---------------------------------------------------------------- data preparation
+ * Detector binning and resolution clipping in one pass (cmtip/prep_data.py:181-212 bin_data,
+ * :149-163 clip_data): in = (n_img, n_panels, px, py) values of precision prec (32 | 64);
+ * each panel is averaged over bin x bin blocks in numpy's summation order (results equal
+ * numpy's bit for bit), then the binned pixels keep[0 .. n_keep) (indices into the binned
+ * (panel, x, y) order; NULL keeps all) are written to out = (n_img, n_keep).  Indices
+ * outside the binned range give CMT_ERR_ARG (and zeros, never an out-of-range read).
+ * Synchronises with the stream when keep is given. */
+int cmt_bin_clip(int prec, const void *in, int64_t n_img, int n_panels, int px, int py, int bin,
+                 const int64_t *keep, int64_t n_keep, void *out, void *stream);
+
 /* ---------------------------------------------------------------- batches of plans
  * Many independent reconstructions in one launch per stage: a batch holds plans of one
  * type, precision, sign and kernel width (2..8, i.e. eps >= 1e-7) but its own modes M,

@@ -169,6 +169,37 @@ def main():
                         ppr=ca["ppr"], rext=ca["rext"], slices=slices_m, quats=quats_m, ac_mult=ac_mult,
                         shuffled_refs=ref_m, matched=q_mult, conformations=conf)
     out["alignment_mult"] = (q_mult.shape, conf.tolist())
+
+    # 5. data preparation (prep_data.py:96-229): binning, clipping and trimming of a
+    #    4-panel detector assembled as 2 x 2 quadrants
+    import importlib
+    sys.modules["h5py"] = types.ModuleType("h5py")
+    sys.modules["cmtip.phasing"] = types.ModuleType("cmtip.phasing")
+    ref_prep = importlib.import_module("cmtip.prep_data")
+    P = 32  # trim_dataset needs an assembled detector wider than 2 x 20 pixels
+    ppr_d, _ = geometry.ewald_detector(P)
+    det_shape = (4, P, P)
+    index_map = np.zeros((4, P, P, 2), dtype=np.int64)
+    xx, yy = np.meshgrid(np.arange(P), np.arange(P), indexing="ij")
+    for lp in range(4):
+        index_map[lp, :, :, 0] = (lp // 2) * P + xx
+        index_map[lp, :, :, 1] = (lp % 2) * P + yy
+    rng = np.random.default_rng(51)
+    imgs = (rng.random((5, 1, 4 * P * P)) * 1e3).astype(np.float32)
+    res = 1e10 / np.linalg.norm(ppr_d, axis=0)
+    res_limit = float(np.quantile(res, 0.5))
+    b2 = ref_prep.bin_data(imgs, 2, det_shape)
+    b4 = ref_prep.bin_data(imgs, 4, det_shape)
+    b8 = ref_prep.bin_data(imgs, 8, det_shape)
+    q2 = ref_prep.bin_data(ppr_d, 2, det_shape)
+    c_img = ref_prep.clip_data(imgs, ppr_d, res_limit)
+    c_ppr = ref_prep.clip_data(ppr_d, ppr_d, res_limit)
+    t_ppr, t_img = ref_prep.trim_dataset(index_map, ppr_d, imgs, det_shape, res_limit)
+    im2 = ref_prep.bin_pixel_index_map(index_map, 2)
+    np.savez_compressed(os.path.join(HERE, "prep.npz"), ppr=ppr_d, index_map=index_map, imgs=imgs,
+                        res_limit=res_limit, bin2=b2, bin4=b4, bin8=b8, ppr_bin2=q2, clip_img=c_img,
+                        clip_ppr=c_ppr, trim_ppr=t_ppr, trim_img=t_img, index_map_bin2=im2)
+    out["prep"] = (b2.shape, c_img.shape, t_img.shape, t_img.dtype)
     print(out)
 
 
