@@ -154,7 +154,8 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
     } else if (sizeof(T) == 4) {
         // the chain below in double-float: H = inv(R) . p, float32(H), * (pi / extent), with
         // the rotations and q-vectors pre-split into (hi, lo) float pairs
-        int64_t img = j / q.n_pix, pix = j - img * q.n_pix;
+        // N < 2^31 (set_pts_impl), so 32-bit index arithmetic
+        const unsigned img = (unsigned)j / (unsigned)q.n_pix, pix = (unsigned)j - img * (unsigned)q.n_pix;
         const float2 *R = q.rot_df + 9 * img;
         float2 a0 = q.ppr_df[pix], a1 = q.ppr_df[q.n_pix + pix], a2 = q.ppr_df[2 * q.n_pix + pix];
         DF p0{a0.x, a0.y}, p1{a1.x, a1.y}, p2{a2.x, a2.y};
@@ -173,7 +174,8 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
     } else {
         // float32(inv(R) . p) / reciprocal_extent * pi, as in align.py:52-57 and
         // autocorrelation.py:27,210 + setup_linops :133-135 (products not fused).
-        int64_t img = j / q.n_pix, pix = j - img * q.n_pix;
+        // N < 2^31 (set_pts_impl), so 32-bit index arithmetic
+        const unsigned img = (unsigned)j / (unsigned)q.n_pix, pix = (unsigned)j - img * (unsigned)q.n_pix;
         const double *R = q.inv_rot + 9 * img;
         double p0 = q.ppr[pix], p1 = q.ppr[q.n_pix + pix], p2 = q.ppr[2 * q.n_pix + pix];
         double h = __dadd_rn(__dadd_rn(__dmul_rn(R[0], p0), __dmul_rn(R[1], p1)), __dmul_rn(R[2], p2));
@@ -248,10 +250,36 @@ struct SortGeom {
     int n, bs, nb, w, fine_sort;
 };
 
-// Pass 1: per-key counts (warp-aggregated atomics), range check.
+// A point between the two counting passes: its sort key (-1: out of range) and its
+// bin-relative fine-grid coordinates, written by pass 1 in caller order so that pass 2
+// does not evaluate the coordinate chain again.
+template <typename T> struct PtRec;
+template <> struct __align__(16) PtRec<float> {
+    int key;
+    float x, y, z;
+};
+template <> struct __align__(16) PtRec<double> {
+    long long key;
+    double x, y, z;
+};
+
+// A point in key order after pass 2: coordinates and caller index in one 16-byte (FP32) or
+// 32-byte (FP64) record, so the scatter writes one stream per key instead of four.
+template <typename T> struct SortedRec;
+template <> struct __align__(16) SortedRec<float> {
+    float x, y, z;
+    int perm;
+};
+template <> struct __align__(16) SortedRec<double> {
+    double x, y, z;
+    int perm, pad;
+};
+
+// Pass 1: coordinates, bin and key of every point (range check), stored as records; per-key
+// counts with warp-aggregated atomics.
 template <typename T>
 __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q, T s_hi, T s_lo,
-                            SortGeom sg, int *count, int *flag)
+                            SortGeom sg, int *count, PtRec<T> *rec, int *flag)
 {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t base = (int64_t)blockIdx.x * blockDim.x;
@@ -259,7 +287,7 @@ __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T
         int64_t j = base + threadIdx.x;
         long long key = -1;
         if (j < N) {
-            T px, py, pz, rx, ry, rz;
+            T px, py, pz, rx = 0, ry = 0, rz = 0;
             bool bad;
             point_coords<T>(mode, j, x, y, z, q, px, py, pz, bad);
             if (bad) {
@@ -268,6 +296,12 @@ __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T
                 int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.bs, sg.nb, rx, ry, rz);
                 key = point_key<T>(b, rx, ry, rz, sg.w, sg.bs, sg.fine_sort);
             }
+            PtRec<T> r;
+            r.key = key;
+            r.x = rx;
+            r.y = ry;
+            r.z = rz;
+            rec[j] = r;
         }
         unsigned peers = __match_any_sync(0xffffffffu, key);
         int leader = __ffs(peers) - 1;
@@ -275,11 +309,10 @@ __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T
     }
 }
 
-// Pass 2: scatter permutation and bin-relative coordinates into key order.  next[key]
-// starts at the key's first position; start[key + 1] bounds it.
+// Pass 2: scatter permutation and coordinates into key order.  next[key] starts at the
+// key's first position; start[key + 1] bounds it.
 template <typename T>
-__global__ void k_bin_scatter(int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q, T s_hi,
-                              T s_lo, SortGeom sg, const int *start, int *next, int *perm, T *ux, T *uy, T *uz,
+__global__ void k_bin_scatter(int64_t N, const PtRec<T> *rec, const int *start, int *next, SortedRec<T> *out,
                               int *flag)
 {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -287,15 +320,10 @@ __global__ void k_bin_scatter(int mode, int64_t N, const T *x, const T *y, const
     for (; base < N; base += stride) {
         int64_t j = base + threadIdx.x;
         long long key = -1;
-        T rx = 0, ry = 0, rz = 0;
+        PtRec<T> r{};
         if (j < N) {
-            T px, py, pz;
-            bool bad;
-            point_coords<T>(mode, j, x, y, z, q, px, py, pz, bad);
-            if (!bad) {
-                int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.bs, sg.nb, rx, ry, rz);
-                key = point_key<T>(b, rx, ry, rz, sg.w, sg.bs, sg.fine_sort);
-            }
+            r = rec[j];
+            key = r.key;
         }
         unsigned peers = __match_any_sync(0xffffffffu, key);
         int lane = threadIdx.x & 31;
@@ -305,15 +333,31 @@ __global__ void k_bin_scatter(int mode, int64_t N, const T *x, const T *y, const
         off = __shfl_sync(peers, off, leader);
         if (key >= 0) {
             int pos = off + __popc(peers & lanemask_lt());
-            if (pos >= start[key + 1]) {  // pass 1 and 2 disagree: never write out of the key's range
+            if (pos >= start[key + 1]) {  // counts and keys disagree: never write out of the key's range
                 atomicOr(flag, 2);
                 continue;
             }
-            perm[pos] = (int)j;
-            ux[pos] = rx;
-            uy[pos] = ry;
-            uz[pos] = rz;
+            SortedRec<T> o{};
+            o.x = r.x;
+            o.y = r.y;
+            o.z = r.z;
+            o.perm = (int)j;
+            out[pos] = o;
         }
+    }
+}
+
+// Records -> the plan's coordinate and permutation arrays without reordering (plans whose
+// subproblem sort does not fit in shared memory).
+template <typename T>
+__global__ void k_rec_to_arrays(int64_t N, const SortedRec<T> *in, int *perm, T *ux, T *uy, T *uz)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const SortedRec<T> r = in[i];
+        perm[i] = r.perm;
+        ux[i] = r.x;
+        uy[i] = r.y;
+        uz[i] = r.z;
     }
 }
 
@@ -391,22 +435,22 @@ __global__ void k_add_tile_offsets(int *out, int64_t n, const int *tile_off)
     if (i < n) out[i] += tile_off[i / SCAN_TILE];
 }
 
-// Within-subproblem sort by window origin (one CTA per subproblem).  The global passes sort
-// by bin and (when the key space is small enough) by window origin on this grid; this pass
-// stages each subproblem's points in shared memory and counting-sorts them by the window
-// origin and its offset on a twice finer grid (point_key's refinement), so runs of points
-// sharing a window on this grid or on a derived plan's grid are contiguous for the
-// spreading / interpolation kernels.
-// smem: nsk counters + maxsub * (4 + 3 sizeof(T)) bytes of staging.
+// Within-subproblem sort by window origin (one CTA per subproblem), out of place: reads the
+// subproblem's records as the global passes left them and writes them, counting-sorted by
+// the window origin on this grid and its offset on a twice finer grid (point_key's
+// refinement), to the same positions of the plan's coordinate and permutation arrays.  The global
+// passes order by bin and by x, y origin; runs of points sharing a window on this grid or on
+// a derived plan's grid become contiguous for the spreading / interpolation kernels.
+// smem: nsk counters + maxsub 16-bit keys.  Keys repeat along the input, so the atomics are
+// warp-aggregated (__match_any_sync).
 template <typename T>
 __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin_count, const int *bin_start, int w,
-                          int bs, int maxsub, int nsk, int *perm, T *ux, T *uy, T *uz)
+                          int bs, int maxsub, int nsk, const SortedRec<T> *in, int *perm_o, T *ux_o, T *uy_o,
+                          T *uz_o)
 {
     extern __shared__ unsigned char smem_raw[];
     int *cnt_s = reinterpret_cast<int *>(smem_raw);
-    int *sp = cnt_s + nsk;
-    T *sx = reinterpret_cast<T *>(sp + maxsub);
-    T *sy = sx + maxsub, *sz = sy + maxsub;
+    unsigned short *skey = reinterpret_cast<unsigned short *>(cnt_s + nsk);
     const int b = sub_bin[blockIdx.x];
     const int off = sub_off[blockIdx.x];
     const int cnt = min(maxsub, bin_count[b] - off);
@@ -414,13 +458,17 @@ __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin
     for (int i = threadIdx.x; i < nsk; i += blockDim.x) cnt_s[i] = 0;
     __syncthreads();
     const int64_t kb = (int64_t)nsk;
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-        const T x = ux[p0 + i], y = uy[p0 + i], z = uz[p0 + i];
-        sp[i] = perm[p0 + i];
-        sx[i] = x;
-        sy[i] = y;
-        sz[i] = z;
-        atomicAdd(&cnt_s[(int)(point_key<T>(0, x, y, z, w, bs, 1) % kb)], 1);
+    const int lane = threadIdx.x & 31;
+    const int cnt_up = (cnt + 31) & ~31;
+    for (int i = threadIdx.x; i < cnt_up; i += blockDim.x) {
+        int key = -1;
+        if (i < cnt) {
+            const SortedRec<T> r = in[p0 + i];
+            key = (int)(point_key<T>(0, r.x, r.y, r.z, w, bs, 1) % kb);
+            skey[i] = (unsigned short)key;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt_s[key], __popc(peers));
     }
     __syncthreads();
     // exclusive scan of the nsk counters: per-thread contiguous ranges + block scan
@@ -437,13 +485,21 @@ __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin
         run += c;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-        const T x = sx[i], y = sy[i], z = sz[i];
-        const int pos = p0 + atomicAdd(&cnt_s[(int)(point_key<T>(0, x, y, z, w, bs, 1) % kb)], 1);
-        perm[pos] = sp[i];
-        ux[pos] = x;
-        uy[pos] = y;
-        uz[pos] = z;
+    for (int i = threadIdx.x; i < cnt_up; i += blockDim.x) {
+        const int key = i < cnt ? (int)skey[i] : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        int base = 0;
+        if (key >= 0 && lane == leader) base = atomicAdd(&cnt_s[key], __popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (key >= 0) {
+            const SortedRec<T> r = in[p0 + i];
+            const int dst = p0 + base + __popc(peers & lanemask_lt());
+            perm_o[dst] = r.perm;
+            ux_o[dst] = r.x;
+            uy_o[dst] = r.y;
+            uz_o[dst] = r.z;
+        }
     }
 }
 
@@ -780,6 +836,42 @@ static int grid_for(int64_t N)
     return (int)std::min<int64_t>(std::max<int64_t>(blocks, 1), 152 * 16);
 }
 
+// The scratch block comes from the device's default stream-ordered memory pool.  By default
+// the pool hands freed memory back to the system at every synchronisation, so each set_pts
+// would map its scratch anew; this process keeps freed pool memory for reuse instead (a
+// setting of this process's pool, not of the device).
+static void keep_pool_memory()
+{
+    static bool done[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done[dev] = true;
+}
+
+// one block of sorted points for capacity C: coordinates x | y | z (C values each), then the
+// permutation (C ints); the T arrays come first so every array stays aligned
+template <typename T>
+static size_t pts_block_bytes(int64_t C)
+{
+    // also holds C sorted records (16 / 32 bytes) while the points are being sorted
+    return (size_t)C * std::max(3 * sizeof(T) + sizeof(int), sizeof(SortedRec<T>));
+}
+
+template <typename T>
+static void set_pts_pointers(Plan &p, void *block, int64_t C)
+{
+    T *b = reinterpret_cast<T *>(block);
+    p.ux = b;
+    p.uy = b + C;
+    p.uz = b + 2 * C;
+    p.perm = reinterpret_cast<int *>(b + 3 * C);
+}
+
 template <typename T>
 static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, const T *z, QuatSrc q)
 {
@@ -787,21 +879,22 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     p.N = 0;
     CMT_CHECK_ARG(N > 0 && N <= 0x7fffffffLL, "number of points %lld outside [1, 2^31-1]", (long long)N);
     int nbins = p.nb * p.nb * p.nb;
-    // Global passes sort by bin and by the x and y window origin on this grid ((bs+1)^2 keys
-    // per bin), so a dense bin's subproblems hold contiguous ranges of origins and points that
-    // share a window mostly land in one subproblem; k_subsort then orders each subproblem by
-    // origin and refinement (point_key).  Keying z as well lengthens runs a little more but
-    // the scatter's write streams (4 arrays x keys) then overflow L2.  CMT_SORT_KEYS = 1..3
-    // sets the number of origin coordinates keyed, for comparison.  Plans without
-    // sort_origin, and grids with too many keys, sort by bin only.
+    // Global passes sort by bin and by the window origin on this grid ((bs+1)^3 keys per bin,
+    // a few million counters that stay in L2), so a dense bin's subproblems hold contiguous
+    // ranges of origins and points that share a window land next to each other; k_subsort
+    // then orders each subproblem by origin and refinement (point_key).  The scatter writes
+    // one 16-byte record per point, one write stream per key, which L2 still merges at this
+    // key count.  CMT_SORT_KEYS = 1..3 sets the number of origin coordinates keyed, for
+    // comparison.  Plans without sort_origin, and grids with too many keys, sort by bin only.
     const int64_t O = p.bs + 1;
-    int kd = 2;
+    int kd = 3;
     if (const char *env = getenv("CMT_SORT_KEYS")) kd = std::min(3, std::max(1, atoi(env)));
     const int64_t kbo = kd == 1 ? O : (kd == 2 ? O * O : O * O * O);
     const int fine_sort = p.sort_origin && (int64_t)nbins * kbo < (1LL << 27) ? 1 + kd : 0;
     const int64_t kb = fine_sort ? kbo : 1;
     const int nsk = (int)(O * O * O * 8);
-    const int sub_smem = (int)(nsk * sizeof(int) + (size_t)p.maxsub * (sizeof(int) + 3 * sizeof(T)));
+    const int sub_smem = (int)(nsk * sizeof(int) + (size_t)p.maxsub * sizeof(unsigned short));
+    const bool do_subsort = nsk <= 65535 && sub_smem <= 200 * 1024;
     const int64_t nkeys = (int64_t)nbins * kb;
     const int64_t ntiles = (nkeys + 1 + SCAN_TILE - 1) / SCAN_TILE;
     if (!p.dflag) {
@@ -830,21 +923,33 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
         CMT_TRY_CUDA(cudaMalloc(&p.tile_sums, sizeof(int) * ntiles));
         p.cap_keys = nkeys + 1;
     }
+    // Sorted points live in one block (x, y, z coordinates, then the permutation).  A scratch
+    // block of the same capacity holds the pass-1 records, then receives the subproblem sort's
+    // output, after which the two blocks swap and the old one is freed.
+    const size_t blk = pts_block_bytes<T>(N);
+    const size_t scratch_bytes = std::max(blk, sizeof(PtRec<T>) * (size_t)N);
+    // pass 1 writes records (caller order) to the scratch block, pass 2 sorted records to the
+    // plan block, the subproblem sort (or a plain copy) the final arrays to the scratch block,
+    // and the blocks swap
     if (N > p.cap_pts) {
-        cudaFree(p.perm);
-        cudaFree(p.ux);
-        cudaFree(p.uy);
-        cudaFree(p.uz);
+        cudaFree(p.pts_block);
+        p.pts_block = nullptr;
         p.perm = nullptr;
         p.ux = p.uy = p.uz = nullptr;
         p.cap_pts = 0;
-        CMT_TRY_CUDA(cudaMalloc(&p.perm, sizeof(int) * N));
-        CMT_TRY_CUDA(cudaMalloc(&p.ux, sizeof(T) * N));
-        CMT_TRY_CUDA(cudaMalloc(&p.uy, sizeof(T) * N));
-        CMT_TRY_CUDA(cudaMalloc(&p.uz, sizeof(T) * N));
+        CMT_TRY_CUDA(cudaMalloc(&p.pts_block, blk));
         p.cap_pts = N;
     }
+    set_pts_pointers<T>(p, p.pts_block, p.cap_pts);
     cudaStream_t st = p.stream;
+    keep_pool_memory();
+    void *scratch = nullptr;
+    CMT_TRY_CUDA(cudaMallocAsync(&scratch, scratch_bytes, st));
+    struct ScratchGuard {
+        void *&ptr;
+        cudaStream_t st;
+        ~ScratchGuard() { if (ptr) cudaFreeAsync(ptr, st); }
+    } guard{scratch, st};
     CMT_TRY_CUDA(cudaMemsetAsync(p.key_next, 0, sizeof(int) * (nkeys + 1), st));
     CMT_TRY_CUDA(cudaMemsetAsync(p.dflag, 0, sizeof(int) * 4, st));
     double s = p.n / (2.0 * kPi);
@@ -853,7 +958,8 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     int g = grid_for(N);
     // pass 1: counts per key (into key_next), then key_start = exclusive scan (with the total
     // at key_start[nkeys])
-    k_bin_count<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, sgeo, p.key_next, p.dflag);
+    k_bin_count<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, sgeo, p.key_next, (PtRec<T> *)scratch,
+                                      p.dflag);
     CMT_LAUNCH_CHECK();
     k_scan_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, st>>>(p.key_next, p.key_start, nkeys + 1, p.tile_sums);
     k_scan_single<<<1, 1024, 0, st>>>(p.tile_sums, (int)ntiles);
@@ -886,15 +992,24 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     CMT_LAUNCH_CHECK();
     // pass 2: scatter, key_next starting at each key's first position
     CMT_TRY_CUDA(cudaMemcpyAsync(p.key_next, p.key_start, sizeof(int) * (nkeys + 1), cudaMemcpyDeviceToDevice, st));
-    k_bin_scatter<T><<<g, 256, 0, st>>>(mode, N, x, y, z, q, s_hi, s_lo, sgeo, p.key_start, p.key_next, p.perm,
-                                        (T *)p.ux, (T *)p.uy, (T *)p.uz, p.dflag);
+    SortedRec<T> *srec = reinterpret_cast<SortedRec<T> *>(p.pts_block);
+    k_bin_scatter<T><<<g, 256, 0, st>>>(N, (const PtRec<T> *)scratch, p.key_start, p.key_next, srec, p.dflag);
     CMT_LAUNCH_CHECK();
-    if (sub_smem <= 200 * 1024 && p.nsub > 0) {
-        CMT_TRY(prep_smem(k_subsort<T>, sub_smem));
-        k_subsort<T><<<(unsigned)p.nsub, 512, sub_smem, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.w,
-                                                              p.bs, p.maxsub, nsk, p.perm, (T *)p.ux, (T *)p.uy,
-                                                              (T *)p.uz);
+    {
+        Plan o = p;
+        set_pts_pointers<T>(o, scratch, N);
+        if (do_subsort && p.nsub > 0) {
+            CMT_TRY(prep_smem(k_subsort<T>, sub_smem));
+            k_subsort<T><<<(unsigned)p.nsub, 512, sub_smem, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start,
+                                                                  p.w, p.bs, p.maxsub, nsk, srec, o.perm, (T *)o.ux,
+                                                                  (T *)o.uy, (T *)o.uz);
+        } else {
+            k_rec_to_arrays<T><<<g, 256, 0, st>>>(N, srec, o.perm, (T *)o.ux, (T *)o.uy, (T *)o.uz);
+        }
         CMT_LAUNCH_CHECK();
+        std::swap(p.pts_block, scratch);  // the guard frees the old block after the kernels
+        p.cap_pts = N;
+        set_pts_pointers<T>(p, p.pts_block, N);
     }
     CMT_TRY_CUDA(cudaMemcpyAsync(&flag, p.dflag, sizeof flag, cudaMemcpyDeviceToHost, st));
     CMT_TRY_CUDA(cudaStreamSynchronize(st));
@@ -1102,10 +1217,7 @@ static void destroy(Plan *p)
     cudaFree(p->bin_start);
     cudaFree(p->sub_bin);
     cudaFree(p->sub_off);
-    cudaFree(p->perm);
-    cudaFree(p->ux);
-    cudaFree(p->uy);
-    cudaFree(p->uz);
+    cudaFree(p->pts_block);
     cudaFree(p->dflag);
     cudaFree(p->dtot);
     cudaFree(p->fine);

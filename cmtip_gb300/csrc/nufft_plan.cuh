@@ -32,6 +32,7 @@ struct Plan {
     int64_t cap_keys = 0;
     int *perm = nullptr;
     void *ux = nullptr, *uy = nullptr, *uz = nullptr;  // bin-relative sorted coordinates
+    void *pts_block = nullptr;                          // owns ux | uy | uz | perm (not when borrowed)
     int64_t cap_pts = 0, cap_sub = 0;
     int *dflag = nullptr;      // device: range error flag, totals
     long long *dtot = nullptr; // device: [total subproblems]

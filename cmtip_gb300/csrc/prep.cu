@@ -41,32 +41,34 @@ __device__ __forceinline__ T row_sum(const T *a, int n)
 // kept indices outside the binned pixel range seen by the last call (the host reads it back)
 static __device__ int g_bad_index;
 
+// Grid: x over the kept pixels, y over image slabs.  A thread decomposes its pixel's index
+// once and then walks the images, so the index arithmetic is amortised and every image's
+// reads and writes are contiguous across the warp.
 template <typename T>
 __global__ void k_bin_clip(const T *in, int64_t n_img, int n_panels, int px, int py, int b, const int64_t *keep,
                            int64_t n_keep, T *out)
 {
     const int bx_n = px / b, by_n = py / b;
+    const int64_t n_binned = (int64_t)n_panels * bx_n * by_n;
     const int64_t per_img_in = (int64_t)n_panels * px * py;
-    const int64_t total = n_img * n_keep;
     const T inv = T(b);
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t img = t / n_keep, q = t - img * n_keep;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n_keep; q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t k = keep ? keep[q] : q;  // index into the binned (panel, bx, by) pixels
-        if (k < 0 || k >= (int64_t)n_panels * bx_n * by_n) {  // never read outside the stack
+        if (k < 0 || k >= n_binned) {          // never read outside the stack
             g_bad_index = 1;
-            out[t] = T(0);
+            for (int64_t img = blockIdx.y; img < n_img; img += gridDim.y) out[img * n_keep + q] = T(0);
             continue;
         }
         const int panel = (int)(k / ((int64_t)bx_n * by_n));
         const int rem = (int)(k - (int64_t)panel * bx_n * by_n);
         const int bx = rem / by_n, by = rem - bx * by_n;
-        const T *src = in + img * per_img_in + ((int64_t)panel * px + (int64_t)bx * b) * py + (int64_t)by * b;
-        T acc = T(0);
-        for (int i = 0; i < b; ++i) {
-            const T *r = src + (int64_t)i * py;
-            acc += row_sum(r, b) / inv;
+        const int64_t off = ((int64_t)panel * px + (int64_t)bx * b) * py + (int64_t)by * b;
+        for (int64_t img = blockIdx.y; img < n_img; img += gridDim.y) {
+            const T *src = in + img * per_img_in + off;
+            T acc = T(0);
+            for (int i = 0; i < b; ++i) acc += row_sum(src + (int64_t)i * py, b) / inv;
+            out[img * n_keep + q] = acc / inv;
         }
-        out[t] = acc / inv;
     }
 }
 
@@ -90,8 +92,9 @@ extern "C" int cmt_bin_clip(int prec, const void *in, int64_t n_img, int n_panel
     int dev = 0, sms = 0;
     CMT_TRY_CUDA(cudaGetDevice(&dev));
     CMT_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int64_t total = n_img * n_keep;
-    const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 8);
+    const int gx = (int)std::min<int64_t>((n_keep + 255) / 256, (int64_t)sms * 8);
+    const int gy = (int)std::max<int64_t>(1, std::min<int64_t>(n_img, ((int64_t)sms * 8 + gx - 1) / gx));
+    const dim3 grid(gx, gy);
     cudaStream_t st = (cudaStream_t)stream;
     int *bad = nullptr;
     CMT_TRY_CUDA(cudaGetSymbolAddress((void **)&bad, g_bad_index));
