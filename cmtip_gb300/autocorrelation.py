@@ -150,6 +150,24 @@ def _as_device(a, dtype, device="cuda"):
     return t.to(device=device, dtype=dtype)
 
 
+def _as_device_async(a, dtype):
+    """(device tensor, event): a host tensor in pinned memory is copied on a side stream so
+    the copy overlaps the device work issued before the event is waited on; anything else
+    is converted on the current stream (event None)."""
+    if torch.is_tensor(a) and not a.is_cuda and a.is_pinned() and a.dtype == dtype and a.is_contiguous():
+        main = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            t = torch.empty(a.shape, dtype=dtype, device="cuda")
+            t.copy_(a, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(side)
+        t.record_stream(main)
+        return t, ev
+    return _as_device(a, dtype), None
+
+
 def setup_linops(H, K, L, data, ac_support, weights, x0, M, Mtot, N, reciprocal_extent,
                  alambda, rlambda, flambda, use_gpu=True, use_recip_sym=True, prec=32,
                  operator="toeplitz", eps=DEFAULT_EPS):
@@ -232,7 +250,10 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
     ppr = _as_device(pixel_position_reciprocal, torch.float64).reshape(3, -1)
     quats = orientations if torch.is_tensor(orientations) else np.asarray(orientations, dtype=np.float32)
     inv_rot = inverse_rotations(quats, device=dev)
-    data = _as_device(slices_, torch.float32).reshape(-1)
+    # the intensities are first needed by the right-hand side, after the point sort and the
+    # Toeplitz kernel: from pinned host memory their copy overlaps that work
+    data, data_ready = _as_device_async(slices_, torch.float32)
+    data = data.reshape(-1)
     if ac_estimate is None:
         sup = torch.ones(Mtot, dtype=torch.float32, device=dev)
         x0 = torch.zeros(Mtot, dtype=torch.float64, device=dev)
@@ -255,6 +276,8 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
         solver.set_kernel(toeplitz_kernel(plan_2M, M))
     else:
         solver.set_pair_plan(plan_M)
+    if data_ready is not None:
+        torch.cuda.current_stream().wait_event(data_ready)
     adb = plan_M.execute(data if data.dtype == rt else data.to(rt), support=sup, scale=1.0 / float(M) ** 3,
                          real_out=True).reshape(-1)
     d = alambda * adb.to(torch.float64) + rlambda * x0

@@ -162,3 +162,19 @@ def test_tikhonov_solve_matches_dense_normal_equations(ac_mod, operator, weighte
     g32 = ac_mod.solve_tikhonov(ppr, rext, b.reshape(n_img, 1, n_pix), M, quats, prec=32, eps=1e-6, **kw)
     g64 = ac_mod.solve_tikhonov(ppr, rext, b.reshape(n_img, 1, n_pix), M, quats, prec=64, eps=1e-12, **kw)
     assert rel_l2(g32, g64) < TOL_AC
+
+
+def test_solve_ac_from_pinned_host_intensities(ac_mod, golden):
+    # the intensities' copy from pinned host memory overlaps the sort and the Toeplitz kernel;
+    # the right-hand side built from them equals the one from device intensities up to the
+    # order of the spreading kernels' floating-point atomics (which differs between any two
+    # runs; this small, underdetermined generation-0 system amplifies it through the CG
+    # iterations, so the solutions themselves are compared at the FP32 bar of the fixtures)
+    g = golden("autocorrelation")
+    M = int(g["M"])
+    kw = dict(orientations=g["quats"], maxiter=10, rtol=0.0, verbose=False, return_info=True)
+    dev, idev = ac_mod.solve_ac(0, g["ppr"], g["rext"], torch.from_numpy(g["slices"]).cuda(), M, **kw)
+    host, ihost = ac_mod.solve_ac(0, g["ppr"], g["rext"], torch.from_numpy(g["slices"]).pin_memory(), M, **kw)
+    assert torch.is_tensor(host) and host.is_cuda
+    assert rel_l2(ihost["d"].cpu().numpy(), idev["d"].cpu().numpy()) < 1e-6
+    assert rel_l2(host.cpu().numpy(), dev.cpu().numpy()) < 2e-3
