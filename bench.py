@@ -325,6 +325,7 @@ def gpu_arm(args):
             extras["prep"] = prep_bench(torch, slices, ppr, cfg)
             extras["tikhonov"] = tikhonov_bench(torch, args)
             extras["batch"] = batch_bench(torch, args)
+            extras["phase"] = phase_bench(torch, args)
         out["extras"] = extras
 
         # ---------------- end to end through the public API with host buffers
@@ -507,6 +508,64 @@ def prep_bench(torch, slices, ppr, cfg):
     return {"images": n_img, "pixels_in": x.shape[1], "pixels_kept": int(len(keep)), "bin": 2,
             "s": t, "GB_per_s": alg / t / 1e9, "hbm_frac": alg / t / 1e9 / peaks["hbm_gbs"],
             "note": "bin_data + clip_data in one pass (keep indices synchronise once per call)"}
+
+
+# ------------------------------------------------------------------ phasing
+
+PHASE_CFG = dict(M=81, n_atoms=150, radius=12.0, seed=2024, n_iterations=10, nER=50, nHIO=25)
+
+
+def phase_bench(torch, args):
+    """Phase retrieval (cmtip/phasing/phase.py:165-219) of the M = 81 autocorrelation of the
+    step's 150-Gaussian particle with the reference's default schedule (10 cycles of ER 50,
+    HIO 25, ER 50, shrink-wrap; a final ER 50: 1300 iterations, each a forward and an
+    inverse M^3 transform), FP64 and FP32, against the oracle's numpy restatement of the
+    reference timed on 2 ER iterations of the same grid and scaled to the schedule."""
+    from cmtip_gb300 import geometry, phasing
+    from oracle import reference_port as rp
+    cfg = dict(PHASE_CFG)
+    if args.small:
+        cfg.update(M=41, radius=6.0, n_atoms=60)
+    M = cfg["M"]
+    rng = np.random.default_rng(cfg["seed"])
+    rho_true = geometry.gaussian_particle(M, cfg["n_atoms"], cfg["radius"], rng)
+    ac = geometry.autocorrelation_of(rho_true)
+    n_iter = cfg["n_iterations"] * (2 * cfg["nER"] + cfg["nHIO"]) + cfg["nER"]
+    ac_d = torch.from_numpy(ac).cuda()
+    res = {"M": M, "iterations": n_iter, "schedule": "10 x (ER 50, HIO 25, ER 50, shrink-wrap) + ER 50"}
+    rel = lambda a, b: float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+    outs = {}
+    for prec in (64, 32):
+        np.random.seed(5)
+        phasing.phase(0, ac_d, n_iterations=1, nER=2, nHIO=2, prec=prec)  # plans, graphs
+        torch.cuda.synchronize()
+        np.random.seed(7)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record()
+        a, s, r = phasing.phase(0, ac_d, n_iterations=cfg["n_iterations"], nER=cfg["nER"], nHIO=cfg["nHIO"],
+                                prec=prec)
+        e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        t = e0.elapsed_time(e1) / 1e3
+        outs[prec] = a.cpu().numpy()
+        res[f"fp{prec}"] = {"s": t, "wall_s": wall, "s_per_iteration": t / n_iter,
+                            "rel_l2_vs_true_ac": rel(outs[prec], ac)}
+    res["rel_l2_fp32_vs_fp64"] = rel(outs[32], outs[64])
+    # the reference's arithmetic on the host: 2 ER iterations of the oracle restatement
+    ac_filt_, amp = rp.phase_amplitudes(ac)
+    sup = rp.phase_create_support(ac_filt_, M, int((M - 1) / 4))
+    rho = sup * np.random.default_rng(3).random(sup.shape)
+    mask = np.ones((M,) * 3, dtype=np.bool_)
+    mask[0, 0, 0] = False
+    t0 = time.perf_counter()
+    rp.phase_er(rho, amp, mask, sup, np.inf, 2)
+    t_it = (time.perf_counter() - t0) / 2
+    res["cpu_reference"] = {"s_per_iteration": t_it, "schedule_s_est": t_it * n_iter, "cores": cores(),
+                            "sample": "2 ER iterations (numpy FFTs, one thread per transform)"}
+    res["speedup_fp64_vs_cpu"] = t_it / res["fp64"]["s_per_iteration"]
+    return res
 
 
 # ------------------------------------------------------------------ weighted Tikhonov solve
@@ -766,11 +825,16 @@ def main():
     ap.add_argument("--align", action="store_true", help="run only the orientation-matching leg and exit")
     ap.add_argument("--batch", action="store_true", help="run only the batched-reconstructions leg and exit")
     ap.add_argument("--tikhonov", action="store_true", help="run only the weighted Tikhonov solve leg and exit")
+    ap.add_argument("--phase", action="store_true", help="run only the phasing leg and exit")
     ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full"],
                     help="run one case of each hot kernel (for ncu captures) and exit")
     args = ap.parse_args()
     if args.kernels:
         kernel_cases(args.kernels)
+        return
+    if args.phase:
+        import torch
+        print(json.dumps({"phase": phase_bench(torch, args)}), flush=True)
         return
     if args.tikhonov:
         import torch

@@ -63,6 +63,18 @@ SIGNATURES = {
     "cmt_cg_destroy": [_vp],
     "cmt_support_from_estimate": [_vp, _i32, _vp, _vp, _i32, _vp],
     "cmt_support_from_estimate_noalloc": [_vp, _i32, _vp, _i32, _vp],
+    "cmt_phase_create": [_i32, _i32, _vp, ctypes.POINTER(_vp)],
+    "cmt_phase_set_stream": [_vp, _vp],
+    "cmt_phase_amplitudes": [_vp, _vp, _vp, _i32, _vp, _vp],
+    "cmt_phase_create_support": [_vp, _vp, _i32, _vp],
+    "cmt_phase_step": [_vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "cmt_phase_er": [_vp, _vp, _vp, _vp, _vp, _f64, _i32],
+    "cmt_phase_hio": [_vp, _f64, _vp, _vp, _vp, _vp, _f64, _i32],
+    "cmt_phase_shrink_wrap": [_vp, _f64, _vp, _i32, _vp, _vp],
+    "cmt_phase_center_of_mass": [_vp, _vp, _vp, _vp],
+    "cmt_phase_roll": [_vp, _vp, _vp, _i32, _i32, _i32],
+    "cmt_phase_autocorrelation": [_vp, _vp, _vp],
+    "cmt_phase_destroy": [_vp],
     "cmt_match_create": [_i64, _i32, _vp, ctypes.POINTER(_vp)],
     "cmt_match_set_data": [_vp, _i64, _vp, _vp],
     "cmt_match_set_refs": [_vp, _i64, _vp, _i32],

@@ -238,6 +238,62 @@ int cmt_match_stats(cmt_match *match, double *host_out);
 
 int cmt_match_destroy(cmt_match *match);
 
+/* ---------------------------------------------------------------- phasing
+ * Phase retrieval of an oversampled autocorrelation (cmtip/phasing/phase.py:11-219).  Arrays
+ * are M^3 in C order; "FFT order" (the reference's trailing underscore) has the DC term at
+ * the corner.  prec 64: density, amplitudes and transforms in double (the reference's
+ * arithmetic); prec 32: float density, amplitudes and transforms, double reductions.
+ * Supports and masks are uint8 (0 / nonzero), i.e. the bytes of a bool tensor.  The
+ * phaser owns only its workspace (half spectrum, filter scratch, reduction partials,
+ * cuFFT plans, the captured iteration graphs); every call is stream-ordered on its stream
+ * with no host synchronisation. */
+typedef struct cmt_phaser cmt_phaser;
+
+int cmt_phase_create(int M, int prec, void *stream, cmt_phaser **phaser);
+int cmt_phase_set_stream(cmt_phaser *phaser, void *stream);
+
+/* phase.py:186-192: ac_filt_ = ifftshift(gaussian_filter(max(ac, 0), mode='constant')) and
+ * amplitudes_ = sqrt(|fftn(ac_filt_)|) (prec).  ac: centred, double.  weights: the
+ * 2 * radius + 1 normalised Gaussian taps (host), radius <= 8. */
+int cmt_phase_amplitudes(cmt_phaser *phaser, const double *ac, const double *weights, int radius,
+                         double *ac_filt_, void *amplitudes_);
+
+/* create_support_ (phase.py:47-64): centred cube [Mquat, M - Mquat)^3, ifftshifted, and
+ * ac_filt_ > 1e-2 * max(ac_filt_). */
+int cmt_phase_create_support(cmt_phaser *phaser, const double *ac_filt_, int mquat, uint8_t *support_);
+
+/* step_phase (phase.py:122-144): rho_mod_ = Re(ifftn(amplitude-replaced fftn(rho_))),
+ * support_star_ = support_ & rho_mod_ > 0. */
+int cmt_phase_step(cmt_phaser *phaser, const void *rho_, const void *amplitudes_, const uint8_t *amp_mask_,
+                   const uint8_t *support_, void *rho_mod_, uint8_t *support_star_);
+
+/* ER_loop / ER (phase.py:67-72, 83-99) and HIO_loop / HIO (:75-80, 102-119): n_loops
+ * iterations updating rho_ in place.  amplitudes_ (prec) and amp_mask_ are full M^3 arrays
+ * in FFT order.  rho_max: +inf for none (the reference's np.infty). */
+int cmt_phase_er(cmt_phaser *phaser, void *rho_, const void *amplitudes_, const uint8_t *amp_mask_,
+                 const uint8_t *support_, double rho_max, int n_loops);
+int cmt_phase_hio(cmt_phaser *phaser, double beta, void *rho_, const void *amplitudes_, const uint8_t *amp_mask_,
+                  const uint8_t *support_, double rho_max, int n_loops);
+
+/* shrink_wrap (phase.py:147-162): support_ = gaussian_filter(|rho_|, mode='wrap') >
+ * max|rho_| * cutoff.  weights / radius as for cmt_phase_amplitudes. */
+int cmt_phase_shrink_wrap(cmt_phaser *phaser, double cutoff, const double *weights, int radius, const void *rho_,
+                          uint8_t *support_);
+
+/* center_of_mass sums (phase.py:20-22) into sums[4] (device, double): sum |rho_| hkl_a for
+ * a = 0, 1, 2 and sum |rho_|.  hkl_: 3 x M^3 doubles, or NULL for recenter's grid
+ * (phase.py:34-38). */
+int cmt_phase_center_of_mass(cmt_phaser *phaser, const void *rho_, const double *hkl_, double *sums);
+
+/* recenter's rolls (phase.py:41-44): np.roll(a, -s_axis, axis) on all three axes, in place,
+ * for rho_ (prec) and support_ (either may be NULL). */
+int cmt_phase_roll(cmt_phaser *phaser, void *rho_, uint8_t *support_, int s0, int s1, int s2);
+
+/* phase.py:214-217: ac_phased = fftshift(|ifftn(|fftn(rho_)|^2)|), double, centred. */
+int cmt_phase_autocorrelation(cmt_phaser *phaser, const void *rho_, double *ac_phased);
+
+int cmt_phase_destroy(cmt_phaser *phaser);
+
 /* inv(R(q)) for n float32 quaternions (w, x, y, z), skopi convention (element products
  * rounded to float32 as with float32 quaternions), into n x 3 x 3 float64. */
 int cmt_inverse_rotations(const float *quat, int64_t n, double *inv_rot, void *stream);

@@ -229,3 +229,100 @@ def match_orientations_mult(pixel_position_reciprocal, reciprocal_extent, slices
     conformations = np.argmin(min_dists, axis=0)
     index = indices[conformations, np.arange(n_img)]
     return ref_orientations[index], conformations
+
+
+# ------------------------------------------------------------ cmtip/phasing
+
+def phase_recenter_grid(M):
+    """phase.py:34-38: per-axis midpoints of linspace(-1, 1, M + 1) on an ij mesh, each
+    coordinate ifftshifted; shape (3, M, M, M)."""
+    edges = np.linspace(-1, 1, M + 1)
+    mids = (edges[:-1] + edges[1:]) / 2
+    return np.stack([np.fft.ifftshift(c) for c in np.meshgrid(mids, mids, mids, indexing="ij")])
+
+
+def phase_center_of_mass(rho_, hkl_, M):
+    """phase.py:11-23: rounded |rho_|-weighted mean of hkl_, in voxels (M / 2 per unit)."""
+    w = np.abs(rho_)
+    return np.round((w * hkl_).sum(axis=(1, 2, 3)) / w.sum() * M / 2)
+
+
+def phase_recenter(rho_, support_, M):
+    """phase.py:26-44: roll both arrays (in place) by minus the centre of mass, axis by axis."""
+    shifts = phase_center_of_mass(rho_, phase_recenter_grid(M), M)
+    for axis in range(3):
+        s = int(shifts[axis])
+        rho_[:] = np.roll(rho_, -s, axis)
+        support_[:] = np.roll(support_, -s, axis)
+
+
+def phase_create_support(ac_, M, Mquat):
+    """phase.py:47-64: centred cube [Mquat, M - Mquat)^3 (ifftshifted) and ac_ above 1% of its max."""
+    cube = np.zeros((M, M, M), dtype=np.bool_)
+    cube[Mquat:M - Mquat, Mquat:M - Mquat, Mquat:M - Mquat] = Mquat > 0
+    return np.fft.ifftshift(cube) & (ac_ > 1e-2 * ac_.max())
+
+
+def phase_amplitudes(ac):
+    """phase.py:186-192: ac_filt_ (ifftshifted Gaussian-filtered positive part) and
+    amplitudes_ = sqrt(|fftn(ac_filt_)|)."""
+    filt = gaussian_filter(np.maximum(ac.real, 0), mode="constant", sigma=1, truncate=2)
+    ac_filt_ = np.fft.ifftshift(filt)
+    return ac_filt_, np.sqrt(np.abs(np.fft.fftn(ac_filt_)))
+
+
+def phase_step(rho_, amplitudes_, amp_mask_, support_):
+    """phase.py:122-144: replace the masked Fourier moduli by amplitudes_, keep the phases,
+    back-transform (real part) and intersect the support with positivity."""
+    spec = np.fft.fftn(rho_)
+    spec = np.where(amp_mask_, amplitudes_ * np.exp(1j * np.angle(spec)), spec)
+    rho_mod_ = np.fft.ifftn(spec).real
+    return rho_mod_, np.logical_and(support_, rho_mod_ > 0)
+
+
+def phase_er(rho_, amplitudes_, amp_mask_, support_, rho_max, n_loops=1):
+    """phase.py:67-72, 83-99: Error Reduction, rho_ in place."""
+    for _ in range(n_loops):
+        rho_mod_, star = phase_step(rho_, amplitudes_, amp_mask_, support_)
+        rho_[:] = np.where(star, rho_mod_, 0)
+        rho_[rho_mod_ > rho_max] = rho_max
+
+
+def phase_hio(beta, rho_, amplitudes_, amp_mask_, support_, rho_max, n_loops=1):
+    """phase.py:75-80, 102-119: Hybrid Input-Output, rho_ in place."""
+    for _ in range(n_loops):
+        rho_mod_, star = phase_step(rho_, amplitudes_, amp_mask_, support_)
+        rho_[:] = np.where(star, rho_mod_, rho_ - beta * rho_mod_)
+        over = rho_mod_ > rho_max
+        rho_[over] += 2 * beta * rho_mod_[over] - rho_max
+
+
+def phase_shrink_wrap(cutoff, sigma, rho_, support_):
+    """phase.py:147-162: support_ (in place) where the periodic Gaussian-smoothed |rho_|
+    exceeds cutoff * max|rho_|."""
+    a = np.absolute(rho_)
+    support_[:] = gaussian_filter(a, mode="wrap", sigma=sigma, truncate=2) > a.max() * cutoff
+
+
+def phase(generation, ac, support_=None, rho_=None, n_iterations=10, nER=50, nHIO=25):
+    """phase.py:165-219: ER / HIO(0.3) / ER / shrink-wrap(5e-2, 1) cycles, a final ER loop,
+    recentring, and fftshift(|ifftn(|fftn(rho_)|^2)|).  The random start uses numpy's
+    global generator, as the reference's."""
+    M = ac.shape[0]
+    Mquat = int((M - 1) / 4)
+    ac_filt_, amplitudes_ = phase_amplitudes(ac)
+    amp_mask_ = np.ones((M, M, M), dtype=np.bool_)
+    amp_mask_[0, 0, 0] = False
+    if support_ is None:
+        support_ = phase_create_support(ac_filt_, M, Mquat)
+    if rho_ is None:
+        rho_ = support_ * np.random.rand(*support_.shape)
+    for _ in range(n_iterations):
+        phase_er(rho_, amplitudes_, amp_mask_, support_, np.inf, nER)
+        phase_hio(0.3, rho_, amplitudes_, amp_mask_, support_, np.inf, nHIO)
+        phase_er(rho_, amplitudes_, amp_mask_, support_, np.inf, nER)
+        phase_shrink_wrap(5e-2, 1, rho_, support_)
+    phase_er(rho_, amplitudes_, amp_mask_, support_, np.inf, nER)
+    phase_recenter(rho_, support_, M)
+    ac_phased_ = np.abs(np.fft.ifftn(np.abs(np.fft.fftn(rho_)) ** 2))
+    return np.fft.fftshift(ac_phased_), support_, rho_

@@ -14,7 +14,7 @@ The package ``cmtip`` is registered without executing ``cmtip/__init__.py`` (whi
 pulls in h5py/mrcfile/skopi-GPU drivers); only the hot-path submodules are loaded.
 Outputs: small ``.npz`` files holding inputs and the reference's outputs.
 
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py  (``--phasing``: only the phasing fixture)
 """
 from __future__ import annotations
 
@@ -201,7 +201,80 @@ def main():
                         clip_ppr=c_ppr, trim_ppr=t_ppr, trim_img=t_img, index_map_bin2=im2)
     out["prep"] = (b2.shape, c_img.shape, t_img.shape, t_img.dtype)
     print(out)
+    phasing_fixtures()
+
+
+def phasing_fixtures():
+    """6. phasing (cmtip/phasing/phase.py): seeded phase() runs (short, medium, with a given
+    support and density, even M, the full default schedule) and each function on random
+    inputs, including an asymmetric amplitude mask and a finite rho_max."""
+    import importlib
+    _install_stubs()
+    pk = sys.modules.get("cmtip.phasing") or types.ModuleType("cmtip.phasing")
+    pk.__path__ = [os.path.join(REF, "cmtip", "phasing")]  # skip __init__ (maps.py needs mrcfile/h5py)
+    sys.modules["cmtip.phasing"] = pk
+    ph = importlib.import_module("cmtip.phasing.phase")
+    from oracle import reference_port as rp
+
+    def particle(M, n_atoms, radius, seed):
+        rng = np.random.default_rng(seed)
+        rho = geometry.gaussian_particle(M, n_atoms, radius, rng)
+        return rho, geometry.autocorrelation_of(rho)
+
+    M = 25
+    rho_true, ac = particle(M, 30, 4.0, 61)
+    res = dict(M=M, ac=ac, rho_true=rho_true)
+    for tag, seed, kw in (("a", 21, dict(n_iterations=1, nER=5, nHIO=5)),
+                          ("b", 22, dict(n_iterations=2, nER=20, nHIO=10)),
+                          ("e", 23, dict())):
+        np.random.seed(seed)
+        a, s, r = ph.phase(0, ac.copy(), **kw)
+        res.update({tag + "_seed": seed, tag + "_ac": a, tag + "_sup": s, tag + "_rho": r})
+    rng = np.random.default_rng(62)
+    sup_in = res["b_sup"].copy()
+    rho_in = sup_in * rng.random((M, M, M))
+    res.update(c_sup_in=sup_in.copy(), c_rho_in=rho_in.copy())
+    a, s, r = ph.phase(1, ac.copy(), support_=sup_in, rho_=rho_in, n_iterations=1, nER=4, nHIO=4)
+    res.update(c_ac=a, c_sup=s, c_rho=r)
+    M2 = 20
+    _, ac2 = particle(M2, 20, 3.0, 63)
+    np.random.seed(24)
+    a, s, r = ph.phase(0, ac2.copy(), n_iterations=1, nER=3, nHIO=3)
+    res.update(f_ac_in=ac2, f_ac=a, f_sup=s, f_rho=r, f_seed=24)
+
+    # single functions on random inputs
+    ac_filt_, amp = rp.phase_amplitudes(ac)
+    rho0 = rng.standard_normal((M, M, M)) * 0.1 + np.fft.ifftshift(rho_true)
+    sup0 = rng.random((M, M, M)) > 0.4
+    mask_sym = np.ones((M, M, M), dtype=np.bool_)
+    mask_sym[0, 0, 0] = False
+    mask_rand = rng.random((M, M, M)) > 0.2
+    amp_rand = amp * (1 + 0.3 * rng.random((M, M, M)))
+    rmod, star = ph.step_phase(rho0, amp_rand, mask_rand, sup0)
+    rho_max = 0.5 * float(ph.step_phase(rho0, amp, mask_sym, sup0)[0].max())  # exercises the over-maximum branch
+    er = rho0.copy()
+    ph.ER(er, amp, mask_sym, sup0, rho_max)
+    hio = rho0.copy()
+    ph.HIO(0.3, hio, amp, mask_sym, sup0, rho_max)
+    sw1 = sup0.copy()
+    ph.shrink_wrap(5e-2, 1, rho0, sw1)
+    sw15 = sup0.copy()
+    ph.shrink_wrap(0.2, 1.5, rho0, sw15)
+    cs = ph.create_support_(ac_filt_, M, int((M - 1) / 4), 0)
+    hkl = rp.phase_recenter_grid(M)
+    com = ph.center_of_mass(rho0, hkl, M)
+    rc_rho, rc_sup = np.roll(rho0, (3, -2, 5), (0, 1, 2)), sup0.copy()
+    ph.recenter(rc_rho, rc_sup, M)
+    res.update(ac_filt_=ac_filt_, amplitudes_=amp, rho0=rho0, sup0=sup0, mask_rand=mask_rand,
+               amp_rand=amp_rand, step_rmod=rmod, step_star=star, rho_max=rho_max, er=er, hio=hio,
+               sw1=sw1, sw15=sw15, create_support=cs, com=com,
+               rc_in=np.roll(rho0, (3, -2, 5), (0, 1, 2)), rc_rho=rc_rho, rc_sup=rc_sup)
+    np.savez_compressed(os.path.join(HERE, "phasing.npz"), **res)
+    print("phasing", {k: getattr(v, "shape", v) for k, v in res.items() if k.endswith("_ac")})
 
 
 if __name__ == "__main__":
-    main()
+    if "--phasing" in sys.argv:
+        phasing_fixtures()
+    else:
+        main()
