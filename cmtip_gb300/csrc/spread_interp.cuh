@@ -446,9 +446,17 @@ __device__ __forceinline__ void spread_tab_sub(int b, int off, const int *bin_co
         __syncwarp();  // the previous batch's records have been read
         const int my_key = tab_prepare<T, W, EXT, CPLX ? 2 : 1>(px, py, pz, beta, vr, vi, tab + lane * REC);
         __syncwarp();
-        // ---- the warp adds the batch's points in order
+        // ---- the warp adds the batch's points in order, run by run: bit q of `starts` marks
+        // a point whose window origin differs from its predecessor's, so each run of equal
+        // origins is one branch-free loop (the flush test happens once per run)
         const int nq = min(32, t1 - base);
-        for (int q = 0; q < nq; ++q) {
+        const int prev_key = __shfl_up_sync(0xffffffffu, my_key, 1);
+        unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || my_key != prev_key);
+        starts &= nq >= 32 ? 0xffffffffu : ((1u << nq) - 1u);
+        int q = 0;
+        while (q < nq) {
+            const unsigned later = starts & ~((2u << q) - 1u);  // starts after q (2u << 31 wraps to 0)
+            const int qe = later ? __ffs(later) - 1 : nq;
             const int key = __shfl_sync(0xffffffffu, my_key, q);  // warp-uniform
             if (key != cur_key) {
                 flush();
@@ -458,30 +466,35 @@ __device__ __forceinline__ void spread_tab_sub(int b, int off, const int *bin_co
                 Z0 = (key & 63) - 16 + h;
             }
             const T *rq = tab + q * REC;
-            T xv[8];
-            load8(rq, xv);
-            const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
-            if (CPLX) {
-                const T2 zv = reinterpret_cast<const T2 *>(rq + 16)[e];
-                const T wr0 = yv.x * zv.x, wi0 = yv.x * zv.y, wr1 = yv.y * zv.x, wi1 = yv.y * zv.y;
+            const T *const rend = tab + qe * REC;
+#pragma unroll 4
+            for (; rq < rend; rq += REC) {
+                T xv[8];
+                load8(rq, xv);
+                const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
+                if (CPLX) {
+                    const T2 zv = reinterpret_cast<const T2 *>(rq + 16)[e];
+                    const T wr0 = yv.x * zv.x, wi0 = yv.x * zv.y, wr1 = yv.y * zv.x, wi1 = yv.y * zv.y;
 #pragma unroll
-                for (int a = 0; a < NX; ++a) {
-                    acc[0][a] += xv[a] * wr0;
-                    aci[0][a] += xv[a] * wi0;
-                    if (RX > 1) {
-                        acc[RX - 1][a] += xv[a] * wr1;
-                        aci[RX - 1][a] += xv[a] * wi1;
+                    for (int a = 0; a < NX; ++a) {
+                        acc[0][a] += xv[a] * wr0;
+                        aci[0][a] += xv[a] * wi0;
+                        if (RX > 1) {
+                            acc[RX - 1][a] += xv[a] * wr1;
+                            aci[RX - 1][a] += xv[a] * wi1;
+                        }
+                    }
+                } else {
+                    const T zv = rq[16 + e];
+                    const T w0 = yv.x * zv, w1 = yv.y * zv;
+#pragma unroll
+                    for (int a = 0; a < NX; ++a) {
+                        acc[0][a] += xv[a] * w0;
+                        if (RX > 1) acc[RX - 1][a] += xv[a] * w1;
                     }
                 }
-            } else {
-                const T zv = rq[16 + e];
-                const T w0 = yv.x * zv, w1 = yv.y * zv;
-#pragma unroll
-                for (int a = 0; a < NX; ++a) {
-                    acc[0][a] += xv[a] * w0;
-                    if (RX > 1) acc[RX - 1][a] += xv[a] * w1;
-                }
             }
+            q = qe;
         }
     }
     flush();
@@ -625,7 +638,14 @@ __device__ __forceinline__ void interp_tab_sub(int b, int off, const int *bin_co
         const int my_key = tab_prepare<T, W, false, 0>(px, py, pz, beta, T(1), T(0), tab + lane * REC);
         __syncwarp();
         const int nq = min(32, t1 - base);
-        for (int q = 0; q < nq; ++q) {
+        // runs of equal window origins (as in spread_tab_sub): one reload test per run
+        const int prev_key = __shfl_up_sync(0xffffffffu, my_key, 1);
+        unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || my_key != prev_key);
+        starts &= nq >= 32 ? 0xffffffffu : ((1u << nq) - 1u);
+        int q = 0;
+        while (q < nq) {
+            const unsigned later = starts & ~((2u << q) - 1u);
+            const int qe = later ? __ffs(later) - 1 : nq;
             const int key = __shfl_sync(0xffffffffu, my_key, q);  // warp-uniform
             if (key != cur_key) {
                 cur_key = key;
@@ -642,32 +662,35 @@ __device__ __forceinline__ void interp_tab_sub(int b, int off, const int *bin_co
                     }
                 }
             }
-            const T *rq = tab + q * REC;
-            T xv[8];
-            load8(rq, xv);
-            const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
-            const T zv = rq[16 + e];
-            T ar0 = T(0), ai0 = T(0), ar1 = T(0), ai1 = T(0);
+#pragma unroll 2
+            for (; q < qe; ++q) {
+                const T *rq = tab + q * REC;
+                T xv[8];
+                load8(rq, xv);
+                const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
+                const T zv = rq[16 + e];
+                T ar0 = T(0), ai0 = T(0), ar1 = T(0), ai1 = T(0);
 #pragma unroll
-            for (int a = 0; a < W; ++a) {
-                ar0 += xv[a] * gr[0][a];
-                if (CPLX) ai0 += xv[a] * gi[0][a];
-                if (RX > 1) {
-                    ar1 += xv[a] * gr[RX - 1][a];
-                    if (CPLX) ai1 += xv[a] * gi[RX - 1][a];
+                for (int a = 0; a < W; ++a) {
+                    ar0 += xv[a] * gr[0][a];
+                    if (CPLX) ai0 += xv[a] * gi[0][a];
+                    if (RX > 1) {
+                        ar1 += xv[a] * gr[RX - 1][a];
+                        if (CPLX) ai1 += xv[a] * gi[RX - 1][a];
+                    }
                 }
-            }
-            T sr = (yv.x * ar0 + yv.y * ar1) * zv;
-            T si = CPLX ? (yv.x * ai0 + yv.y * ai1) * zv : T(0);
-            sr += __shfl_xor_sync(0xffffffffu, sr, 8);
-            sr += __shfl_xor_sync(0xffffffffu, sr, 16);
-            if (CPLX) {
-                si += __shfl_xor_sync(0xffffffffu, si, 8);
-                si += __shfl_xor_sync(0xffffffffu, si, 16);
-            }
-            if (bl == 0) {
-                if (CPLX) reinterpret_cast<T2 *>(part)[q * 8 + e] = T2{sr, si};
-                else part[q * 8 + e] = sr;
+                T sr = (yv.x * ar0 + yv.y * ar1) * zv;
+                T si = CPLX ? (yv.x * ai0 + yv.y * ai1) * zv : T(0);
+                sr += __shfl_xor_sync(0xffffffffu, sr, 8);
+                sr += __shfl_xor_sync(0xffffffffu, sr, 16);
+                if (CPLX) {
+                    si += __shfl_xor_sync(0xffffffffu, si, 8);
+                    si += __shfl_xor_sync(0xffffffffu, si, 16);
+                }
+                if (bl == 0) {
+                    if (CPLX) reinterpret_cast<T2 *>(part)[q * 8 + e] = T2{sr, si};
+                    else part[q * 8 + e] = sr;
+                }
             }
         }
         __syncwarp();
