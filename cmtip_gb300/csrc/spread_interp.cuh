@@ -293,12 +293,24 @@ __device__ __forceinline__ int tab_prepare(T px, T py, T pz, T beta, T vr, T vi,
     }
     const int dx = lx - gx, dy = ly - gy, dz = lz - gz;  // 0 or 1 (EXT), else 0
     T kx[W], ky[W], kz[W];
+    if constexpr (sizeof(T) == 4) {
+        // t_k = t_0 + k (2 / W): one FMA per kernel argument, branch-free evaluation
+        const T ax = (T(lx) - px) * inv, ay = (T(ly) - py) * inv, az = (T(lz) - pz) * inv;
+        const T bl2e = beta * T(1.4426950408889634);
 #pragma unroll
-    for (int k = 0; k < W; ++k) {
-        const T tx = (T(lx + k) - px) * inv, ty = (T(ly + k) - py) * inv, tz = (T(lz + k) - pz) * inv;
-        kx[k] = es_eval(tx * tx, beta);
-        ky[k] = es_eval(ty * ty, beta);
-        kz[k] = es_eval(tz * tz, beta);
+        for (int k = 0; k < W; ++k) {
+            kx[k] = es_eval_tab(fmaf(T(k), inv, ax), bl2e);
+            ky[k] = es_eval_tab(fmaf(T(k), inv, ay), bl2e);
+            kz[k] = es_eval_tab(fmaf(T(k), inv, az), bl2e);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            const T tx = (T(lx + k) - px) * inv, ty = (T(ly + k) - py) * inv, tz = (T(lz + k) - pz) * inv;
+            kx[k] = es_eval(tx * tx, beta);
+            ky[k] = es_eval(ty * ty, beta);
+            kz[k] = es_eval(tz * tz, beta);
+        }
     }
     // the values by window column / row / z offset (shifted by d when EXT)
     auto col = [&](const T(&v)[W], int d, int a) -> T {
