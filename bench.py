@@ -23,6 +23,7 @@ q-points, that autocorrelation with 5% noise as the estimate.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import os
 import statistics
@@ -814,6 +815,16 @@ def kernel_cases(size="small"):
 # ------------------------------------------------------------------ main
 
 def main():
+    # the library's reference-compatible progress prints (e.g. match_orientations' std ratio)
+    # go to stderr: stdout carries only the JSON line
+    out = sys.stdout
+    with contextlib.redirect_stdout(sys.stderr):
+        line = _run()
+    if line is not None:
+        print(json.dumps(line), file=out, flush=True)
+
+
+def _run():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -831,25 +842,21 @@ def main():
     args = ap.parse_args()
     if args.kernels:
         kernel_cases(args.kernels)
-        return
+        return None
     if args.phase:
         import torch
-        print(json.dumps({"phase": phase_bench(torch, args)}), flush=True)
-        return
+        return {"phase": phase_bench(torch, args)}
     if args.tikhonov:
         import torch
-        print(json.dumps({"tikhonov": tikhonov_bench(torch, args)}), flush=True)
-        return
+        return {"tikhonov": tikhonov_bench(torch, args)}
     if args.batch:
         import torch
-        print(json.dumps({"batch": batch_bench(torch, args)}), flush=True)
-        return
+        return {"batch": batch_bench(torch, args)}
     if args.align:
         import torch
         import cmtip_gb300.nufft as nf
         import cmtip_gb300.alignment as alm
-        print(json.dumps({"align": align_bench(torch, nf, alm, args)}), flush=True)
-        return
+        return {"align": align_bench(torch, nf, alm, args)}
     rank, world, _ = rank_info()
     metric = "CG-iter s & align img/s, 5k imgs M=81: mixed-prec vs FP64 GPU at ≤1e-5 err"
     cfg = dict(CFG)
@@ -863,7 +870,7 @@ def main():
               "l2": "inputs larger than L2 (5.2 GB intensities, 21 GB sorted points per plan)"}
     if args.impl == "reference":
         if rank != 0:
-            return
+            return None
         v, det = cpu_reference_step(cfg)
         line = {"impl": "reference", "metric": metric, "value": v, "unit": "s/CG-iteration", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * cfg["maxiter"] * 1e3,
@@ -874,11 +881,10 @@ def main():
                                            f"{det['scale']:.0f}; 2 CG iterations scaled to {cfg['maxiter']}",
                                  "details": det},
                 "e2e": {"value": v, "unit": "s/CG-iteration", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return
+        return line
     t_step, cfg_used, out, N = gpu_arm(args)
     if rank != 0:
-        return
+        return None
     line = {"metric": metric, "value": t_step / cfg["maxiter"], "unit": "s/CG-iteration", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 dots/norms/alpha/beta)",
@@ -892,7 +898,7 @@ def main():
                                 "sample": f"{det['sample_images']} of {cfg['n_img']} images' spreads scaled "
                                           f"x{det['scale']:.0f}; 2 CG iterations scaled to {cfg['maxiter']}",
                                 "details": det}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 if __name__ == "__main__":
