@@ -295,6 +295,8 @@ def gpu_arm(args):
         peaks = measured_peaks()
         achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
         traffic = profile_traffic("k_spread_tab_5000img_M81.md", f"dram_bytes_per_launch_{dom_key}")
+        issue = profile_traffic("k_spread_tab_5000img_M81.md", f"issue_active_frac_{dom_key}")
+        fma = profile_traffic("k_spread_tab_5000img_M81.md", f"fma_pipe_frac_{dom_key}")
         label = {"2M": "k_spread_tab<float, real, w=7, extended window>: ones onto the 2M-mode Toeplitz grid "
                        f"(n = {info2['n_fine']})",
                  "M": f"k_spread_tab<float, real, w=7>: data onto the M-mode grid (n = {infoM['n_fine']})"}[dom_key]
@@ -303,8 +305,10 @@ def gpu_arm(args):
                            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
                            "peak_source": peaks["source"],
                            "launch_ms": round(dom["ms"], 3), "algorithmic_bytes": dom["bytes"],
-                           "note": "instruction-issue bound (w^3 = 343 window updates per point spread over "
-                                   "32 lanes, plus each point's table set-up), not HBM bound"}
+                           "issue_active_frac": issue, "fma_pipe_frac": fma,
+                           "note": "instruction-issue bound (w^3 window updates per point spread over 32 lanes, "
+                                   "plus each point's table set-up), not HBM bound: issue_active_frac and "
+                                   "fma_pipe_frac are the ncu fractions of peak for this kernel"}
         out["spread_kernels"] = spread
         out["clocks"] = clk
 
@@ -787,7 +791,9 @@ def kernel_cases(size="small"):
     N = cfg["n_img"] * ppr.shape[-1]
     g = torch.Generator(device=dev).manual_seed(0)
     data = torch.randn(N, device=dev, generator=g)
-    p1 = nf.Plan(1, M, eps=cfg["eps"]).set_pts_quat(inv, pprd, rext)
+    # the type-1 plan with the tuning of solve_ac's Toeplitz workspace (bins of 5 cells,
+    # 16384 points per subproblem), so the captures match the bench step's kernels
+    p1 = nf.Plan(1, M, eps=cfg["eps"]).set_tuning(5, 16384).set_pts_quat(inv, pprd, rext)
     p1.execute(data, real_out=True)
     p2m = p1.derive(1, 2 * M)  # the Toeplitz-kernel plan of the solve: borrows p1's points
     p2m.execute(None, real_out=True)
