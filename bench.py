@@ -47,6 +47,17 @@ def rank_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(value, dist=None, device="cpu"):
+    """The largest per-rank value over all ranks of the process group (every rank gets it);
+    the value itself without a process group.  The timed region is the slowest replica's."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t)
+
+
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons during a timed region."""
 
@@ -269,10 +280,7 @@ def gpu_arm(args):
     barrier()
     clk = clocks.stop()
     t_step = ev0.elapsed_time(ev1) / 1e3 / args.steps
-    if dist is not None:
-        tt = torch.tensor([t_step], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt)
+    t_step = max_over_ranks(t_step, dist, dev)
     prof = {"2M": ws.plan_2M.profile_read(), "M": ws.plan_M.profile_read()}
     info2, infoM = ws.plan_2M.info(), ws.plan_M.info()
 
