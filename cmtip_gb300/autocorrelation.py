@@ -150,13 +150,27 @@ def _as_device(a, dtype, device="cuda"):
     return t.to(device=device, dtype=dtype)
 
 
+_COPY_STREAMS = {}
+
+
+def _copy_stream(device):
+    """One side stream per device for host-to-device copies: the caching allocator reuses a
+    freed block only on the stream that allocated it, so a fresh stream per call would
+    allocate the (multi-GB) destination anew every time."""
+    key = torch.device(device).index
+    s = _COPY_STREAMS.get(key)
+    if s is None:
+        s = _COPY_STREAMS[key] = torch.cuda.Stream(device=device)
+    return s
+
+
 def _as_device_async(a, dtype):
     """(device tensor, event): a host tensor in pinned memory is copied on a side stream so
     the copy overlaps the device work issued before the event is waited on; anything else
     is converted on the current stream (event None)."""
     if torch.is_tensor(a) and not a.is_cuda and a.is_pinned() and a.dtype == dtype and a.is_contiguous():
         main = torch.cuda.current_stream()
-        side = torch.cuda.Stream()
+        side = _copy_stream(main.device)
         side.wait_stream(main)
         with torch.cuda.stream(side):
             t = torch.empty(a.shape, dtype=dtype, device="cuda")
