@@ -69,8 +69,14 @@ class CGSolver:
     def set_operator(self, support, alambda, rlambda, flambda, mask_fft=None):
         sup = torch.as_tensor(support, device=self.device).to(torch.float32).contiguous()
         if mask_fft is None:
-            mask_fft = np.fft.ifftshift(gen_F_antisupport(self.M))
-        mask = torch.as_tensor(np.asarray(mask_fft, dtype=np.float32), device=self.device).contiguous()
+            # the antisupport depends on M only: built on the host (~10 ms at M = 81) and
+            # uploaded once per solver
+            mask = self._keep.get("default_mask")
+            if mask is None:
+                m = np.asarray(np.fft.ifftshift(gen_F_antisupport(self.M)), dtype=np.float32)
+                mask = self._keep["default_mask"] = torch.from_numpy(m).to(self.device).contiguous()
+        else:
+            mask = torch.as_tensor(np.asarray(mask_fft, dtype=np.float32), device=self.device).contiguous()
         with torch.cuda.device(self.device):
             _lib.call("cmt_cg_set_operator", self._h, _ptr(mask), _ptr(sup), float(alambda), float(rlambda),
                       float(flambda))

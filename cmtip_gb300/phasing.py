@@ -11,7 +11,11 @@ updated in place when they already have the working type.
 Every operation runs in the CUDA kernels of ``csrc/phase.cu`` (cuFFT for the transforms);
 an ER or HIO loop replays one captured graph per iteration.  The working precision follows
 the density's dtype in the single-step functions (float64 -> the reference's double
-arithmetic, float32 -> single) and the ``prec`` keyword in ``phase`` (default 64).
+arithmetic, float32 -> single) and the ``prec`` keyword in ``phase``: 32 by default, as the
+rest of this library (the reference's 1300-iteration schedule at M = 81 in 0.036 s against
+0.245 s for ``prec=64``; GB300's double-precision FFTs are slow), 64 for the reference's
+arithmetic.  ER / HIO from a random start are chaotic, so the two forms follow different
+trajectories from the first rounding difference and reach solutions of the same quality.
 ``phase`` draws its random initial density from numpy's global generator exactly as the
 reference does (phase.py:200-201), so a seeded reference run and this one start alike.
 """
@@ -25,7 +29,7 @@ import torch
 from . import _lib
 from .nufft import _ptr, _stream_ptr
 
-DEFAULT_PREC = 64
+DEFAULT_PREC = 32  # phase(); the single-step functions follow the density's dtype
 
 _PHASERS: dict = {}
 
@@ -293,8 +297,9 @@ def phase(generation, ac, support_=None, rho_=None, n_iterations=10, nER=50, nHI
     Returns ``(ac_phased, support_, rho_)``: float64 centred autocorrelation, bool support
     and float64 density (FFT order).  numpy ``ac`` -> numpy results; a CUDA tensor ``ac``
     -> tensors on its device.  A caller's ``support_`` / ``rho_`` are updated in place and
-    returned.  ``prec=32`` runs the iterations in single precision (a rounding-level change
-    that the iteration, chaotic over many HIO steps, amplifies like any other)."""
+    returned.  ``prec=64`` runs the reference's double arithmetic; the default ``prec=32``
+    runs the iterations in single precision (a rounding-level change that the iteration,
+    chaotic over many HIO steps, amplifies like any other)."""
     M = int(ac.shape[0])
     Mquat = int((M - 1) / 4)
     dev = _device_of(ac, support_, rho_)

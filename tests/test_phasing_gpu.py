@@ -54,7 +54,8 @@ def test_phase_seeded_runs(ph, g, tag, prec):
 
 def test_phase_given_support_and_density_in_place(ph, g):
     sup, rho = g["c_sup_in"].copy(), g["c_rho_in"].copy()
-    ac_p, sup_o, rho_o = ph.phase(1, g["ac"].copy(), support_=sup, rho_=rho, n_iterations=1, nER=4, nHIO=4)
+    ac_p, sup_o, rho_o = ph.phase(1, g["ac"].copy(), support_=sup, rho_=rho, n_iterations=1, nER=4, nHIO=4,
+                                  prec=64)
     assert sup_o is sup and rho_o is rho
     assert np.array_equal(sup, g["c_sup"])
     assert rel_l2(rho, g["c_rho"]) < 1e-7 and rel_l2(ac_p, g["c_ac"]) < 1e-8
@@ -65,16 +66,24 @@ def test_phase_tensors_stay_on_device(ph, g):
     rho = torch.from_numpy(g["c_rho_in"]).cuda()
     ptr = rho.data_ptr()
     ac_p, sup_o, rho_o = ph.phase(1, torch.from_numpy(g["ac"]).cuda(), support_=sup, rho_=rho,
-                                  n_iterations=1, nER=4, nHIO=4)
+                                  n_iterations=1, nER=4, nHIO=4, prec=64)
     assert torch.is_tensor(ac_p) and ac_p.is_cuda and ac_p.dtype == torch.float64
     assert sup_o is sup and rho_o is rho and rho.data_ptr() == ptr
     assert np.array_equal(sup.cpu().numpy(), g["c_sup"])
     assert rel_l2(rho.cpu().numpy(), g["c_rho"]) < 1e-7
 
 
+def test_phase_default_is_single_precision(ph, g):
+    sup, rho = g["c_sup_in"].copy(), g["c_rho_in"].copy()
+    ac_p, sup_o, rho_o = ph.phase(1, g["ac"].copy(), support_=sup, rho_=rho, n_iterations=1, nER=4, nHIO=4)
+    assert ph.DEFAULT_PREC == 32 and rho_o is rho and rho.dtype == np.float64
+    assert np.array_equal(sup, g["c_sup"])
+    assert rel_l2(rho, g["c_rho"]) < TOL[32][0] and rel_l2(ac_p, g["c_ac"]) < TOL[32][1]
+
+
 def test_phase_even_grid(ph, g):
     np.random.seed(int(g["f_seed"]))
-    ac_p, sup, rho = ph.phase(0, g["f_ac_in"].copy(), n_iterations=1, nER=3, nHIO=3)
+    ac_p, sup, rho = ph.phase(0, g["f_ac_in"].copy(), n_iterations=1, nER=3, nHIO=3, prec=64)
     assert np.array_equal(sup, g["f_sup"])
     assert rel_l2(rho, g["f_rho"]) < 1e-7 and rel_l2(ac_p, g["f_ac"]) < 1e-8
 
