@@ -1,6 +1,7 @@
 """The bench's multi-rank host logic on CPU (gloo, world size 2): replicas time their own
 step and the line reports the slowest replica; the reference arm runs on rank 0 only."""
 import os
+import socket
 import sys
 
 import pytest
@@ -29,7 +30,9 @@ def _worker(rank, world, port, out):
 def test_max_over_ranks_and_reference_rank_gating():
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    port = 29500 + os.getpid() % 1000
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as sock:  # a free rendezvous port
+        sock.bind(("127.0.0.1", 0))
+        port = sock.getsockname()[1]
     procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
