@@ -117,10 +117,26 @@ __device__ __forceinline__ void cell_and_frac(T x, T s_hi, T s_lo, int n, int &c
     int c = (int)fp;
     if (f >= T(1)) { f -= T(1); c += 1; }
     if (f < T(0)) { f += T(1); c -= 1; }
-    c %= n;
+    // c mod n: two corrections cover [-n, 2n) (|x| < pi); the division only beyond
     if (c < 0) c += n;
+    if (c >= n) c -= n;
+    if ((unsigned)c >= (unsigned)n) {
+        c %= n;
+        if (c < 0) c += n;
+    }
     cell = c;
     frac = f;
+}
+
+// floor(x / d) for 0 <= x < 2^32 / d as the high word of x * m, m = ceil(2^32 / d)
+// (Granlund & Montgomery 1994: with m d = 2^32 + e, 0 <= e < d, the error x e / (d 2^32) is
+// below 1/d, less than the distance from x / d to the next integer).
+__device__ __forceinline__ unsigned div_magic(unsigned x, unsigned m) { return __umulhi(x, m); }
+
+inline unsigned magic32(unsigned d) { return (unsigned)((0x100000000ULL + d - 1) / d); }  // d >= 2
+inline unsigned long long magic64(unsigned long long d)                                  // d >= 2
+{
+    return ~0ULL / d + 1ULL;  // ceil(2^64 / d)
 }
 
 // Coordinates of point j.  MODE 0: arrays of the plan's precision; MODE 1: rotation.
@@ -132,7 +148,16 @@ struct QuatSrc {
     const float2 *rot_df;  // FP32 plans: inv_rot and ppr split into double-float pairs
     const float2 *ppr_df;
     float2 scale_df;       // pi / rext as a double-float pair
+    unsigned long long npix_magic;  // ceil(2^64 / n_pix) (n_pix >= 2), else 0
 };
+
+// (image, pixel) of point j < 2^31: j / n_pix as the high word of j * ceil(2^64 / n_pix),
+// exact for all j < 2^64 / n_pix
+__device__ __forceinline__ void img_pix(int64_t j, const QuatSrc &q, unsigned &img, unsigned &pix)
+{
+    img = q.npix_magic ? (unsigned)__umul64hi((unsigned long long)j, q.npix_magic) : (unsigned)j;
+    pix = (unsigned)j - img * (unsigned)q.n_pix;
+}
 
 __global__ void k_split_df(const double *in, int64_t n, float2 *out)
 {
@@ -155,7 +180,8 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
         // the chain below in double-float: H = inv(R) . p, float32(H), * (pi / extent), with
         // the rotations and q-vectors pre-split into (hi, lo) float pairs
         // N < 2^31 (set_pts_impl), so 32-bit index arithmetic
-        const unsigned img = (unsigned)j / (unsigned)q.n_pix, pix = (unsigned)j - img * (unsigned)q.n_pix;
+        unsigned img, pix;
+        img_pix(j, q, img, pix);
         const float2 *R = q.rot_df + 9 * img;
         float2 a0 = q.ppr_df[pix], a1 = q.ppr_df[q.n_pix + pix], a2 = q.ppr_df[2 * q.n_pix + pix];
         DF p0{a0.x, a0.y}, p1{a1.x, a1.y}, p2{a2.x, a2.y};
@@ -175,7 +201,8 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
         // float32(inv(R) . p) / reciprocal_extent * pi, as in align.py:52-57 and
         // autocorrelation.py:27,210 + setup_linops :133-135 (products not fused).
         // N < 2^31 (set_pts_impl), so 32-bit index arithmetic
-        const unsigned img = (unsigned)j / (unsigned)q.n_pix, pix = (unsigned)j - img * (unsigned)q.n_pix;
+        unsigned img, pix;
+        img_pix(j, q, img, pix);
         const double *R = q.inv_rot + 9 * img;
         double p0 = q.ppr[pix], p1 = q.ppr[q.n_pix + pix], p2 = q.ppr[2 * q.n_pix + pix];
         double h = __dadd_rn(__dadd_rn(__dmul_rn(R[0], p0), __dmul_rn(R[1], p1)), __dmul_rn(R[2], p2));
@@ -194,15 +221,22 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
 }
 
 template <typename T>
-__device__ __forceinline__ int bin_of(T px, T py, T pz, T s_hi, T s_lo, int n, int bs, int nb, T &rx, T &ry,
-                                      T &rz)
+__device__ __forceinline__ int bin_of(T px, T py, T pz, T s_hi, T s_lo, int n, int bs, unsigned bs_magic, int nb,
+                                      T &rx, T &ry, T &rz)
 {
     int cx, cy, cz;
     T fx, fy, fz;
     cell_and_frac(px, s_hi, s_lo, n, cx, fx);
     cell_and_frac(py, s_hi, s_lo, n, cy, fy);
     cell_and_frac(pz, s_hi, s_lo, n, cz, fz);
-    int bx = cx / bs, by = cy / bs, bz = cz / bs;
+    int bx, by, bz;
+    if (bs_magic) {
+        bx = (int)div_magic((unsigned)cx, bs_magic);
+        by = (int)div_magic((unsigned)cy, bs_magic);
+        bz = (int)div_magic((unsigned)cz, bs_magic);
+    } else {
+        bx = cx / bs, by = cy / bs, bz = cz / bs;
+    }
     rx = T(cx - bx * bs) + fx;
     ry = T(cy - by * bs) + fy;
     rz = T(cz - bz * bs) + fz;
@@ -248,6 +282,7 @@ __device__ __forceinline__ int64_t point_key(int b, T rx, T ry, T rz, int w, int
 
 struct SortGeom {
     int n, bs, nb, w, fine_sort;
+    unsigned bs_magic;  // ceil(2^32 / bs) for cells below 2^32 / bs, else 0 (plain division)
 };
 
 // A point between the two counting passes: its sort key (-1: out of range) and its
@@ -293,7 +328,7 @@ __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T
             if (bad) {
                 atomicOr(flag, 1);
             } else {
-                int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.bs, sg.nb, rx, ry, rz);
+                int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.bs, sg.bs_magic, sg.nb, rx, ry, rz);
                 key = point_key<T>(b, rx, ry, rz, sg.w, sg.bs, sg.fine_sort);
             }
             PtRec<T> r;
@@ -457,14 +492,13 @@ __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin
     const int p0 = bin_start[b] + off;
     for (int i = threadIdx.x; i < nsk; i += blockDim.x) cnt_s[i] = 0;
     __syncthreads();
-    const int64_t kb = (int64_t)nsk;
     const int lane = threadIdx.x & 31;
     const int cnt_up = (cnt + 31) & ~31;
     for (int i = threadIdx.x; i < cnt_up; i += blockDim.x) {
         int key = -1;
         if (i < cnt) {
             const SortedRec<T> r = in[p0 + i];
-            key = (int)(point_key<T>(0, r.x, r.y, r.z, w, bs, 1) % kb);
+            key = (int)point_key<T>(0, r.x, r.y, r.z, w, bs, 1);  // < nsk: bin 0, clamped origin
             skey[i] = (unsigned short)key;
         }
         const unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -954,7 +988,9 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     CMT_TRY_CUDA(cudaMemsetAsync(p.dflag, 0, sizeof(int) * 4, st));
     double s = p.n / (2.0 * kPi);
     T s_hi = (T)s, s_lo = (T)(s - (double)s_hi);
-    SortGeom sgeo{p.n, p.bs, p.nb, p.w, fine_sort};
+    // cells are below n <= 2^20, so the multiply-high division is exact for bs <= 4096
+    SortGeom sgeo{p.n, p.bs, p.nb, p.w, fine_sort,
+                  p.bs >= 2 && (uint64_t)p.n * p.bs < (1ULL << 32) ? magic32((unsigned)p.bs) : 0u};
     int g = grid_for(N);
     // pass 1: counts per key (into key_next), then key_start = exclusive scan (with the total
     // at key_start[nkeys])
@@ -1422,7 +1458,7 @@ extern "C" int cmt_plan_get_tuning(const cmt_plan *p, int *bin_size, int *maxsub
 extern "C" int cmt_set_pts(cmt_plan *p, int64_t N, const void *x, const void *y, const void *z)
 {
     CMT_CHECK_ARG(p && x && y && z, "null argument");
-    QuatSrc q{nullptr, nullptr, 1, 1.0, nullptr, nullptr, make_float2(0.f, 0.f)};
+    QuatSrc q{nullptr, nullptr, 1, 1.0, nullptr, nullptr, make_float2(0.f, 0.f), 0ULL};
     if (p->prec == 64) return set_pts_impl<double>(*p, 0, N, (const double *)x, (const double *)y, (const double *)z, q);
     return set_pts_impl<float>(*p, 0, N, (const float *)x, (const float *)y, (const float *)z, q);
 }
@@ -1433,7 +1469,8 @@ extern "C" int cmt_set_pts_quat(cmt_plan *p, int64_t n_img, const double *inv_ro
     CMT_CHECK_ARG(p && inv_rot && ppr, "null argument");
     CMT_CHECK_ARG(n_img > 0 && n_pix > 0, "empty image set");
     CMT_CHECK_ARG(rext > 0, "reciprocal_extent must be positive");
-    QuatSrc q{inv_rot, ppr, n_pix, rext, nullptr, nullptr, make_float2(0.f, 0.f)};
+    QuatSrc q{inv_rot, ppr, n_pix, rext, nullptr, nullptr, make_float2(0.f, 0.f),
+              n_pix >= 2 ? magic64((unsigned long long)n_pix) : 0ULL};
     int64_t N = n_img * n_pix;
     if (p->prec == 64) return set_pts_impl<double>(*p, 1, N, nullptr, nullptr, nullptr, q);
     // FP32 plans evaluate the float64 coordinate chain in double-float arithmetic
