@@ -44,3 +44,45 @@ def test_python_signatures_cover_header():
 def test_library_reports_version(lib):
     lib.cmt_version.restype = ctypes.c_char_p
     assert b"sm_103a" in lib.cmt_version()
+
+
+# ---- argument checking: rejected before any CUDA call, so these run without a GPU
+
+def _err(lib):
+    lib.cmt_last_error.restype = ctypes.c_char_p
+    return lib.cmt_last_error().decode()
+
+
+def test_bad_arguments_return_arg_error(lib):
+    vp, out = ctypes.c_void_p, ctypes.c_void_p()
+    lib.cmt_plan_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                    ctypes.c_double, vp, ctypes.POINTER(vp)]
+    assert lib.cmt_plan_create(3, 21, 32, 1e-6, 1, 0.0, None, ctypes.byref(out)) == 1
+    assert "type must be 1 or 2" in _err(lib) and not out.value
+    assert lib.cmt_plan_create(1, 21, 16, 1e-6, 1, 0.0, None, ctypes.byref(out)) == 1
+    assert "prec must be 32 or 64" in _err(lib)
+    lib.cmt_phase_create.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.POINTER(vp)]
+    assert lib.cmt_phase_create(0, 64, None, ctypes.byref(out)) == 1 and "M must be in" in _err(lib)
+    assert lib.cmt_phase_create(21, 16, None, ctypes.byref(out)) == 1 and "prec" in _err(lib)
+    lib.cmt_cg_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.POINTER(vp)]
+    assert lib.cmt_cg_create(1, 32, 0, None, ctypes.byref(out)) == 1 and "M must be in [2, 512]" in _err(lib)
+    lib.cmt_match_create.argtypes = [ctypes.c_int64, ctypes.c_int, vp, ctypes.POINTER(vp)]
+    assert lib.cmt_match_create(16384, 7, None, ctypes.byref(out)) == 1 and "mode must be" in _err(lib)
+
+
+def test_noalloc_filter_rejects_grids_beyond_its_scratch(lib):
+    # the allocation-free support filter checks M against its fixed scratch first
+    vp = ctypes.c_void_p
+    lib.cmt_support_from_estimate_noalloc.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp]
+    dummy = vp(16)  # never dereferenced: the size check fails before any device work
+    assert lib.cmt_support_from_estimate_noalloc(dummy, 129, dummy, 0, None) == 1
+    assert "128" in _err(lib)
+    assert lib.cmt_support_from_estimate_noalloc(None, 21, dummy, 0, None) == 1
+
+
+def test_python_binding_maps_status_codes():
+    from cmtip_gb300 import _lib
+    with pytest.raises(ValueError, match="type must be 1 or 2"):
+        _lib.call("cmt_plan_create", 3, 21, 32, 1e-6, 1, 0.0, None, ctypes.byref(ctypes.c_void_p()))
+    with pytest.raises(ValueError, match="null"):
+        _lib.call("cmt_phase_er", None, None, None, None, None, float("inf"), 1)
