@@ -22,7 +22,7 @@ import torch
 from . import _lib
 from .nufft import DEFAULT_EPS, Plan
 
-BIN_SIZES = (4, 8, 16)
+BIN_SIZES = (4, 5, 8, 16)
 MAXSUBS = (2048, 4096, 8192, 16384)
 
 _mem = {}
