@@ -18,7 +18,7 @@ Inputs are synthetic with the reference's shapes: seeded uniform-random quaterni
 intensities = the type-2 NUFFT of a 150-Gaussian particle's autocorrelation at the rotated
 q-points, that autocorrelation with 5% noise as the estimate.
 --impl reference times the reference's own CPU path for the same step on the host cores
-(bounded sample, scaled; see cpu_reference_step).
+(a bounded sample run step after step; see ReferenceStep).
 """
 from __future__ import annotations
 
@@ -157,67 +157,152 @@ def synthetic_geometry(cfg):
 
 # ------------------------------------------------------------------ CPU reference leg
 
-def cpu_reference_step(cfg, n_sample_img=8, n_iter_sample=2):
-    """The reference's solve_ac on the host cores for this step, from a bounded sample:
-    positions (gen_nonuniform_positions) and both type-1 spreads on n_sample_img images
-    (finufft stand-in: the oracle's FP64 ES-kernel NUFFT at eps 1e-7, all cores), scaled
-    linearly to all images; the two uniform-grid FFT/deconvolution stages once; and
-    n_iter_sample iterations of the reference's Toeplitz W_matvec + CG update (numpy
-    complex128, autocorrelation.py:32-63, 88-110, 150-155) scaled to maxiter.
-    Returns (seconds per CG iteration with setup amortised, details)."""
-    from oracle import nufft as on
-    from oracle import reference_port as rp
-    ppr, rext, quats, ac = synthetic_geometry(cfg)
-    M, maxiter = cfg["M"], cfg["maxiter"]
-    n_pix = ppr.shape[-1]
-    n_full = cfg["n_img"] * n_pix
-    rng = np.random.default_rng(1)
-    t0 = time.perf_counter()
-    H, K, L = rp.gen_nonuniform_positions(quats[:n_sample_img], ppr)
-    t_pos = time.perf_counter() - t0
-    xs = [a.astype(np.float32).ravel() / rext * np.pi for a in (H, K, L)]
-    data = rng.standard_normal(xs[0].size)
-    eps = 1e-7
-    w, beta = on.es_params(eps)
-    spread_t, fixed_t = 0.0, 0.0
-    for m_modes, strengths in ((2 * M, np.ones_like(data)), (M, data)):
-        n = on.fine_size(m_modes, w)
+class ReferenceStep:
+    """The reference's solve_ac (cmtip/autocorrelation/autocorrelation.py:176-248) for this
+    step on the host cores, as a bounded sample that is actually run, step after step.
+
+    Each step() does, on the next block of ``images`` images of the workload (cycling):
+    the positions (gen_nonuniform_positions, :12-29) and both type-1 spreads of setup_linops
+    (ones onto the 2M fine grid, the data onto the M fine grid; :141-147, :162-167) with the
+    finufft stand-in (the oracle's FP64 ES-kernel spreader at the GPU arm's eps, so the same
+    kernel width), the two uniform-grid FFT + deconvolution stages, and ``iters`` iterations
+    of ONE continuing CG trajectory (scipy's cg recurrence, complex128, with the reference's
+    own W_matvec: core_problem_convolution :32-63 + fourier_reg :88-110, :150-155), restarted
+    only after maxiter iterations, so every maxiter / iters steps run a whole solve.
+    Nothing is scaled but the spreads and positions, by points: value = (per-point time x
+    all points + the fixed stages + maxiter x the measured iteration time) / maxiter."""
+
+    def __init__(self, cfg, images=100, iters=10, threads=None):
+        from oracle import nufft as on
+        from oracle import reference_port as rp
+        self.on, self.rp = on, rp
+        self.cfg, self.images, self.iters = cfg, images, iters
+        self.threads = threads or cores()
+        self.ppr, self.rext, self.quats, ac = synthetic_geometry(cfg)
+        M = cfg["M"]
+        self.n_pix = self.ppr.shape[-1]
+        self.n_full = cfg["n_img"] * self.n_pix
+        self.w, self.beta = on.es_params(cfg["eps"])
+        self.block = 0
+        self.rng = np.random.default_rng(1)
+        # the CG operator of the sample: the reference's W on the first block's points
+        s = rp.solve_ac_inputs(self.ppr, np.zeros((images, 1, self.n_pix), np.float32), M,
+                               self.quats[:images], ac.copy())
+        self.support = s["ac_support"]
+        self.anti = rp.gen_F_antisupport(M)
+        self.rlambda = s["rlambda"]
+        self.x0 = s["x0"].astype(np.complex128)
+        self.Fk = None
+        self.d = None
+        self.cg_it = 0
+        self.t_spread, self.t_pos, self.t_fixed, self.t_iter, self.pts = [], [], [], [], 0
+
+    def _spread_block(self, nthreads, n_img=None):
+        on, rp = self.on, self.rp
+        M = self.cfg["M"]
+        n_img = n_img or self.images
+        i0 = (self.block * self.images) % self.cfg["n_img"]
+        q = self.quats[i0:i0 + n_img]
         t0 = time.perf_counter()
-        g = on.spread(*xs, strengths.astype(np.complex128), n, w, beta)
-        spread_t += time.perf_counter() - t0
+        H, K, L = rp.gen_nonuniform_positions(q, self.ppr)
+        xs = [a.astype(np.float32).ravel() / self.rext * np.pi for a in (H, K, L)]
+        t_pos = time.perf_counter() - t0
+        data = self.rng.standard_normal(xs[0].size)
+        t_spread, t_fixed, grids = 0.0, 0.0, {}
+        for m_modes, strengths in ((2 * M, np.ones_like(data)), (M, data)):
+            n = on.fine_size(m_modes, self.w)
+            t0 = time.perf_counter()
+            g = on.spread(*xs, strengths.astype(np.complex128), n, self.w, self.beta, nthreads)
+            t_spread += time.perf_counter() - t0
+            t0 = time.perf_counter()
+            G = np.fft.ifftn(g) * float(n) ** 3
+            idx = on.modes(m_modes) % n
+            p = on._deconv(m_modes, n, self.w, self.beta)
+            f = G[np.ix_(idx, idx, idx)] * (p[:, None, None] * p[None, :, None] * p[None, None, :])
+            f = f.real / m_modes ** 3
+            if m_modes == 2 * M:
+                grids["Fk"] = np.fft.fftn(np.fft.ifftshift(f))
+            else:
+                grids["d"] = (f * self.support).ravel() + self.rlambda * self.x0
+            t_fixed += time.perf_counter() - t0
+            del g, G
+        return xs[0].size, t_pos, t_spread, t_fixed, grids
+
+    def single_thread_sample(self, n_img=4):
+        """Per-point spread time on one host thread (positions and both spreads)."""
+        n, t_pos, t_spread, _, _ = self._spread_block(1, n_img)
+        return (t_pos + t_spread) / n
+
+    def step(self):
+        rp = self.rp
+        M = self.cfg["M"]
+        t_step = time.perf_counter()
+        n, t_pos, t_spread, t_fixed, grids = self._spread_block(self.threads)
+        self.block += 1
+        self.pts += n
+        self.t_pos.append(t_pos)
+        self.t_spread.append(t_spread)
+        self.t_fixed.append(t_fixed)
+        if self.Fk is None or self.cg_it >= self.cfg["maxiter"]:
+            # (re)start a solve: the operator and right-hand side of the current block
+            self.Fk, self.d = grids["Fk"], grids["d"]
+            self.x = self.x0.copy()
+            self.r = self.d - self._matvec(self.x)
+            self.rho_prev, self.p, self.cg_it = None, None, 0
         t0 = time.perf_counter()
-        G = np.fft.ifftn(g) * float(n) ** 3
-        idx = on.modes(m_modes) % n
-        p = on._deconv(m_modes, n, w, beta)
-        f = G[np.ix_(idx, idx, idx)] * (p[:, None, None] * p[None, :, None] * p[None, None, :])
-        if m_modes == 2 * M:
-            np.fft.fftn(np.fft.ifftshift(f.real / m_modes ** 3))
-        fixed_t += time.perf_counter() - t0
-        del g, G
-    scale = n_full / data.size
-    # CG iterations with the reference's operator
-    s = rp.solve_ac_inputs(ppr, np.zeros((n_sample_img, 1, n_pix), np.float32), M, quats[:n_sample_img], ac.copy())
-    Fk = np.fft.fftn(np.fft.ifftshift(rng.standard_normal((2 * M,) * 3)))
-    anti = rp.gen_F_antisupport(M)
-    x = s["x0"].astype(np.complex128)
-    r = rng.standard_normal(M ** 3).astype(np.complex128)
-    pvec = r.copy()
-    t0 = time.perf_counter()
-    for _ in range(n_iter_sample):
-        q = (rp.core_problem_convolution(pvec, M, Fk, 2 * M, s["ac_support"]) + 1e-3 * pvec
-             + 1e3 * rp.fourier_reg(pvec, s["ac_support"], anti, M, True))
-        rho = np.vdot(r, r)
-        alpha = rho / np.vdot(pvec, q)
-        x += alpha * pvec
-        r -= alpha * q
-        beta_ = np.vdot(r, r) / rho
-        pvec = r + beta_ * pvec
-    t_iter = (time.perf_counter() - t0) / n_iter_sample
-    total = t_pos * scale + spread_t * scale + fixed_t + maxiter * t_iter
-    details = dict(sample_images=n_sample_img, sample_points=int(data.size), scale=scale,
-                   spread_s_sample=spread_t, fft_deconv_s=fixed_t, positions_s_sample=t_pos,
-                   cg_iteration_s=t_iter, solve_s_estimate=total, eps=eps, width=w)
-    return total / maxiter, details
+        for _ in range(self.iters):
+            rho = np.vdot(self.r, self.r).real
+            self.p = self.r.copy() if self.p is None else self.r + (rho / self.rho_prev) * self.p
+            q = self._matvec(self.p)
+            alpha = rho / np.vdot(self.p, q).real
+            self.x += alpha * self.p
+            self.r -= alpha * q
+            self.rho_prev = rho
+            self.cg_it += 1
+        self.t_iter.append((time.perf_counter() - t0) / self.iters)
+        return time.perf_counter() - t_step
+
+    def _matvec(self, u):
+        rp, M = self.rp, self.cfg["M"]
+        return (rp.core_problem_convolution(u, M, self.Fk, 2 * M, self.support) + self.rlambda * u
+                + 1e3 * rp.fourier_reg(u, self.support, self.anti, M, True))
+
+    def value(self):
+        """Seconds per CG iteration of the full workload, setup amortised."""
+        per_pt = (sum(self.t_pos) + sum(self.t_spread)) / self.pts
+        fixed = float(np.mean(self.t_fixed))
+        t_it = float(np.mean(self.t_iter))
+        maxiter = self.cfg["maxiter"]
+        return (per_pt * self.n_full + fixed + maxiter * t_it) / maxiter, dict(
+            spread_positions_s_per_point=per_pt, fft_deconv_s=fixed, cg_iteration_s=t_it,
+            solve_s_estimate=per_pt * self.n_full + fixed + maxiter * t_it, sampled_points=self.pts,
+            sampled_point_fraction=self.pts / self.n_full, cg_iterations_run=len(self.t_iter) * self.iters,
+            eps=self.cfg["eps"], width=self.w, threads=self.threads)
+
+    def describe(self):
+        return (f"per step: positions + both type-1 spreads of {self.images} of {self.cfg['n_img']} images "
+                f"(FP64 ES-kernel stand-in for finufft, eps {self.cfg['eps']}, w = {self.w}, {self.threads} threads), "
+                f"both FFT/deconvolution stages, {self.iters} iterations of one continuing complex128 CG with the "
+                f"reference's W_matvec (a whole {self.cfg['maxiter']}-iteration solve every "
+                f"{self.cfg['maxiter'] // self.iters} steps); spreads extrapolated by points, nothing else scaled")
+
+
+def cpu_baseline(cfg, steps=1, single_thread=True):
+    """The cpu_baseline object of the GPU arm's line: ``steps`` reference steps (all host
+    threads) plus the per-point spread time on one thread."""
+    ref = ReferenceStep(cfg)
+    for _ in range(steps):
+        ref.step()
+    v, det = ref.value()
+    out = {"value": v, "unit": "s/CG-iteration", "cores": ref.threads, "kind": "port", "extrapolated": True,
+           "sample": ref.describe(), "details": det}
+    if single_thread:
+        per_pt1 = ref.single_thread_sample()
+        v1 = (per_pt1 * ref.n_full + det["fft_deconv_s"] + cfg["maxiter"] * det["cg_iteration_s"]) / cfg["maxiter"]
+        out["single_thread"] = {"value": v1, "cores": 1, "spread_positions_s_per_point": per_pt1,
+                                "sample": "positions + both spreads of 4 images on one thread; the FFT stages "
+                                          "and CG iterations (numpy, one thread already) as measured above"}
+    return out
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -333,7 +418,8 @@ def gpu_arm(args):
         extras = {"cg_iteration_s": t_cg, "setup_s": t_step - maxiter * t_cg}
         if not args.no_extras:
             extras.update(pair_and_nufft(torch, nf, acm, ws, cfg, dev, N, args))
-            extras.update(fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_step))
+            extras["nufft_parity"] = nufft_parity(torch, nf, cfg, dev, N)
+            extras.update(fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_step, t_cg))
             extras["align"] = align_bench(torch, nf, alm, args)
             extras["prep"] = prep_bench(torch, slices, ppr, cfg)
             extras["tikhonov"] = tikhonov_bench(torch, args)
@@ -411,27 +497,132 @@ def pair_and_nufft(torch, nf, acm, ws, cfg, dev, N, args):
     return res
 
 
-def fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_mixed):
-    """The same solve in the plain-FP64 GPU form (FP64 NUFFT, vectors, FFTs); relative L2 of
-    the mixed-precision result against it after 10 (config 0's count) and 100 iterations."""
+def fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_mixed, t_cg_mixed):
+    """The same solve in the plain-FP64 GPU form (FP64 NUFFT at eps 1e-12, FP64 vectors and
+    FFTs) and in the reference's own precision split (FP32 NUFFT, FP64 CG), each warmed up
+    (plans, sort buffers, cuFFT plans, captured graph) before it is timed by CUDA events;
+    whole-solve and pure CG-iteration times separately.  Errors of the mixed form against
+    the FP64 form after 10, 30, 60 and 100 iterations of the same CG, and the sensitivity of
+    the FP64 form itself: its 100-iteration result when only its Toeplitz kernel is
+    perturbed (recomputed, i.e. another order of its FP64 atomics; or times 1 + 1e-7 N(0,1)),
+    which is the floor any single-precision operator meets."""
     M, maxiter = cfg["M"], cfg["maxiter"]
-    kw = dict(orientations=quats_d, maxiter=maxiter, rtol=0.0, eps=cfg["eps"], verbose=False, return_info=True)
-    ref, info32 = acm.solve_ac(0, ppr_d, rext, slices, M, ac_estimate=est.clone(), prec=32, **kw)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ac64, info64 = acm.solve_ac(0, ppr_d, rext, slices, M, ac_estimate=est.clone(), prec=64, **kw)
-    torch.cuda.synchronize()
-    t64 = time.perf_counter() - t0
-    rel = lambda a, b: float(torch.linalg.norm(a.double() - b.double()) / torch.linalg.norm(b.double()))
-    err100 = rel(ref, ac64)
-    x10_32, _ = info32["solver"].solve(info32["d"], info32["x0"], maxiter=10, rtol=0.0)
-    x10_64, _ = info64["solver"].solve(info64["d"], info64["x0"], maxiter=10, rtol=0.0)
-    err10 = rel(x10_32, x10_64)
-    del info32, info64
+    dev = ppr_d.device
+    kw = dict(orientations=quats_d, rtol=0.0, verbose=False, return_info=True)
+    rel = lambda a, b: float(torch.linalg.norm(a.double().reshape(-1) - b.double().reshape(-1))
+                             / torch.linalg.norm(b.double().reshape(-1)))
+
+    def timed(**kwargs):
+        acm.solve_ac(0, ppr_d, rext, slices, M, ac_estimate=est.clone(), maxiter=2, **kw, **kwargs)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        x, info = acm.solve_ac(0, ppr_d, rext, slices, M, ac_estimate=est.clone(), maxiter=maxiter, **kw, **kwargs)
+        e1.record()
+        torch.cuda.synchronize()
+        return x, info, e0.elapsed_time(e1) / 1e3
+
+    def cg_time(solver, d, x0):
+        solver.solve(d, x0, maxiter=3, rtol=0.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        solver.solve(d, x0, maxiter=maxiter, rtol=0.0)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / maxiter
+
+    x32, i32, _ = timed(prec=32, eps=cfg["eps"])
+    x64, i64, t64 = timed(prec=64, eps=1e-12)
+    ws64 = acm._workspace(M, 64, acm.TOEPLITZ, 1e-12, dev)
+    ws32 = acm._workspace(M, 32, acm.TOEPLITZ, cfg["eps"], dev)
+    t_cg64 = cg_time(ws64.solver, i64["d"], i64["x0"])
+    res = {"fp64_form_solve_s": t64, "fp64_form_cg_iteration_s": t_cg64,
+           "speedup_vs_fp64_form": t64 / t_mixed, "cg_iteration_speedup_vs_fp64_form": t_cg64 / t_cg_mixed,
+           "ac_rel_l2_mixed_vs_fp64_100it": rel(x32, x64)}
+    T64 = acm.toeplitz_kernel(ws64.plan_2M, M).clone()
+    T32 = acm.toeplitz_kernel(ws32.plan_2M, M).clone()
+    res["toeplitz_kernel_rel_l2_vs_fp64"] = rel(T32, T64)
+    res["rhs_rel_l2_vs_fp64"] = rel(i32["d"], i64["d"])
+    curve = {}
+    for its in (10, 30, 60, 100):
+        a, _ = i32["solver"].solve(i32["d"], i32["x0"], maxiter=its, rtol=0.0)
+        b, _ = ws64.solver.solve(i64["d"], i64["x0"], maxiter=its, rtol=0.0)
+        curve[str(its)] = rel(a, b)
+    res["ac_rel_l2_mixed_vs_fp64_by_iterations"] = curve
+    res["ac_rel_l2_mixed_vs_fp64_10it"] = curve["10"]
+    # sensitivity of the FP64 form to perturbations of its Toeplitz kernel alone
+    g = torch.Generator(device=dev).manual_seed(99)
+    sens = {}
+    for tag, T in (("recomputed_kernel", acm.toeplitz_kernel(ws64.plan_2M, M).clone()),
+                   ("kernel_x(1+1e-7N)", T64 * (1 + 1e-7 * torch.randn(T64.shape, generator=g, device=dev,
+                                                                        dtype=torch.float64))),
+                   ("kernel_x(1+1e-9N)", T64 * (1 + 1e-9 * torch.randn(T64.shape, generator=g, device=dev,
+                                                                        dtype=torch.float64)))):
+        ws64.solver.set_kernel(T)
+        xp, _ = ws64.solver.solve(i64["d"], i64["x0"], maxiter=maxiter, rtol=0.0)
+        sens[tag] = rel(xp, x64)
+    ws64.solver.set_kernel(T64)
+    res["fp64_form_100it_rel_l2_under_kernel_perturbation"] = sens
+    del i64, ws64, T64, T32
     acm.clear_workspaces()
     torch.cuda.empty_cache()
-    return {"fp64_form_s_per_iteration": t64 / maxiter, "speedup_vs_fp64_form": t64 / t_mixed,
-            "ac_rel_l2_mixed_vs_fp64_10it": err10, "ac_rel_l2_mixed_vs_fp64_100it": err100}
+    # the reference's precision split: FP32 NUFFT (eps as the step), FP64 CG
+    xs, isp, tsp = timed(prec=32, cg_prec=64, eps=cfg["eps"])
+    res["fp32_nufft_fp64_cg"] = {"solve_s": tsp, "s_per_iteration": tsp / maxiter,
+                                 "cg_iteration_s": cg_time(isp["solver"], isp["d"], isp["x0"]),
+                                 "ac_rel_l2_vs_fp64_100it": rel(xs, x64),
+                                 "speedup_vs_fp64_form": t64 / tsp}
+    del isp, i32
+    acm.clear_workspaces()
+    torch.cuda.empty_cache()
+    return res
+
+
+def nufft_parity(torch, nf, cfg, dev, N, n_img_check=4):
+    """Errors at the production size (config 1's bar, error vs FP64): the type-1 of N(0,1)
+    complex strengths at all 1.31e9 points onto the M^3 modes against an FP64 plan at eps
+    1e-12 (the whole grid), and the type-2 of N(0,1) complex modes at the points of
+    n_img_check seeded images (>= 1e6 points) against the FP64 oracle (the reference's
+    float32 coordinate chain, evaluated on the host)."""
+    from oracle import nufft as on
+    from oracle import reference_port as rp
+    M = cfg["M"]
+    ppr, rext, quats, _ = synthetic_geometry(cfg)
+    n_pix = ppr.shape[-1]
+    inv = nf.inverse_rotations(torch.from_numpy(quats).to(dev))
+    pprd = torch.from_numpy(ppr).to(dev)
+    rel = lambda a, b: float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+    g = torch.Generator(device=dev).manual_seed(21)
+    res = {"points": N, "eps": cfg["eps"]}
+    # type 1, whole grid
+    c = torch.randn(N, device=dev, dtype=torch.complex64, generator=g)
+    p32 = nf.Plan(1, M, eps=cfg["eps"], isign=1).set_pts_quat(inv, pprd, rext)
+    f32 = p32.execute(c)
+    p32.close()
+    p64 = nf.Plan(1, M, eps=1e-12, isign=1, prec=64).set_pts_quat(inv, pprd, rext)
+    f64 = p64.execute(c.to(torch.complex128))
+    p64.close()
+    del c
+    res["type1_rel_l2_vs_fp64_plan"] = rel(f32.to(torch.complex128), f64)
+    del f32, f64
+    torch.cuda.empty_cache()
+    # type 2 at the points of a few seeded images
+    fm = torch.randn((M,) * 3, device=dev, dtype=torch.complex64, generator=g)
+    p2 = nf.Plan(2, M, eps=cfg["eps"], isign=-1).set_pts_quat(inv, pprd, rext)
+    out = p2.execute(fm)
+    p2.close()
+    imgs = np.sort(np.random.default_rng(8).choice(cfg["n_img"], n_img_check, replace=False))
+    H, K, L = rp.gen_nonuniform_positions(quats[imgs], ppr)
+    xs = [a.astype(np.float32).ravel() / rext * np.pi for a in (H, K, L)]
+    ref = on.type2(*xs, fm.cpu().numpy().astype(np.complex128), eps=1e-12, isign=-1)
+    idx = torch.from_numpy((imgs[:, None] * n_pix + np.arange(n_pix)[None, :]).ravel()).to(dev)
+    got = out[idx].cpu().numpy().astype(np.complex128)
+    res["type2_rel_l2_vs_fp64_oracle"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    res["type2_points_checked"] = int(ref.size)
+    del out
+    torch.cuda.empty_cache()
+    return res
 
 
 def align_bench(torch, nf, alm, args):
@@ -885,17 +1076,7 @@ def _run():
     if args.impl == "reference":
         if rank != 0:
             return None
-        v, det = cpu_reference_step(cfg)
-        line = {"impl": "reference", "metric": metric, "value": v, "unit": "s/CG-iteration", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * cfg["maxiter"] * 1e3,
-                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": config,
-                "cpu_baseline": {"value": v, "unit": "s/CG-iteration", "cores": cores(), "kind": "port",
-                                 "sample": f"{det['sample_images']} of {cfg['n_img']} images' spreads scaled x"
-                                           f"{det['scale']:.0f}; 2 CG iterations scaled to {cfg['maxiter']}",
-                                 "details": det},
-                "e2e": {"value": v, "unit": "s/CG-iteration", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        return line
+        return reference_arm(args, cfg, metric, config)
     t_step, cfg_used, out, N = gpu_arm(args)
     if rank != 0:
         return None
@@ -907,12 +1088,64 @@ def _run():
             "config": config}
     line.update(out)
     if not args.no_cpu and world == 1:
-        v, det = cpu_reference_step(cfg)
-        line["cpu_baseline"] = {"value": v, "unit": "s/CG-iteration", "cores": cores(), "kind": "port",
-                                "sample": f"{det['sample_images']} of {cfg['n_img']} images' spreads scaled "
-                                          f"x{det['scale']:.0f}; 2 CG iterations scaled to {cfg['maxiter']}",
-                                "details": det}
+        line["cpu_baseline"] = cpu_baseline(cfg)
+    line["summary"] = summarize(line)
     return line
+
+
+def summarize(line):
+    """The key figures of the line's extras, repeated last on the line (a reader of its tail
+    sees them)."""
+    ex = line.get("extras", {})
+    g = lambda d, *ks: (None if d is None else (d.get(ks[0]) if len(ks) == 1 else g(d.get(ks[0]), *ks[1:])))
+    out = {"s_per_cg_iteration": line.get("value"), "e2e_s_per_cg_iteration": g(line, "e2e", "value"),
+           "pure_cg_iteration_s": ex.get("cg_iteration_s"),
+           "speedup_vs_fp64_form": ex.get("speedup_vs_fp64_form"),
+           "cg_iteration_speedup_vs_fp64_form": ex.get("cg_iteration_speedup_vs_fp64_form"),
+           "ac_rel_l2_mixed_vs_fp64": ex.get("ac_rel_l2_mixed_vs_fp64_by_iterations"),
+           "fp64_form_sensitivity": ex.get("fp64_form_100it_rel_l2_under_kernel_perturbation"),
+           "fp32_nufft_fp64_cg": {k: g(ex, "fp32_nufft_fp64_cg", k) for k in
+                                  ("s_per_iteration", "ac_rel_l2_vs_fp64_100it", "speedup_vs_fp64_form")},
+           "type1_rel_l2_vs_fp64": g(ex, "nufft_parity", "type1_rel_l2_vs_fp64_plan"),
+           "type2_rel_l2_vs_fp64": g(ex, "nufft_parity", "type2_rel_l2_vs_fp64_oracle"),
+           "type1_pts_per_s": ex.get("type1_pts_per_s"), "type2_pts_per_s": ex.get("type2_pts_per_s"),
+           "align_bf16_img_per_s": g(ex, "align", "bf16", "img_per_s"),
+           "align_speedup_vs_fp64_form": g(ex, "align", "speedup_bf16_vs_fp64_form"),
+           "align_disagree_outside_fp32_ties": g(ex, "align", "bf16", "disagree_outside_fp32_ties"),
+           "tikhonov_s": g(ex, "tikhonov", "solve_s"), "tikhonov_rel_l2_vs_fp64": g(ex, "tikhonov", "rel_l2_mixed_vs_fp64"),
+           "cpu_baseline_s_per_cg_iteration": g(line, "cpu_baseline", "value"),
+           "cpu_baseline_single_thread": g(line, "cpu_baseline", "single_thread", "value")}
+    return {k: v for k, v in out.items() if v is not None}
+
+
+def reference_arm(args, cfg, metric, config):
+    """--impl reference: W untimed then K timed steps of the reference's CPU path on all host
+    threads (ReferenceStep); ms_per_step is the measured time of one sampled step, value the
+    workload's s/CG-iteration from the sample (spreads extrapolated by points)."""
+    ref = ReferenceStep(cfg)
+    for _ in range(args.warmup):
+        ref.step()
+    ref.t_spread, ref.t_pos, ref.t_fixed, ref.t_iter, ref.pts = [], [], [], [], 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ref.step()
+    t_step = (time.perf_counter() - t0) / max(args.steps, 1)
+    v, det = ref.value()
+    base = {"value": v, "unit": "s/CG-iteration", "cores": ref.threads, "kind": "port", "extrapolated": True,
+            "sample": ref.describe(), "details": det}
+    per_pt1 = ref.single_thread_sample()
+    base["single_thread"] = {
+        "value": (per_pt1 * ref.n_full + det["fft_deconv_s"] + cfg["maxiter"] * det["cg_iteration_s"]) / cfg["maxiter"],
+        "cores": 1, "spread_positions_s_per_point": per_pt1,
+        "sample": "positions + both spreads of 4 images on one thread (after the timed steps); the FFT stages and "
+                  "CG iterations as measured in the steps"}
+    return {"impl": "reference", "metric": metric, "value": v, "unit": "s/CG-iteration", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config, "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "s/CG-iteration", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "consistency_note": "ms_per_step is one sampled step as run; value extrapolates only the spreads "
+                                "and positions from the sampled points to all points"}
 
 
 if __name__ == "__main__":

@@ -220,11 +220,14 @@ def setup_linops(H, K, L, data, ac_support, weights, x0, M, Mtot, N, reciprocal_
 
 
 class _Workspace:
-    """Plans and solver reused across solve_ac calls with the same (M, prec, operator, eps):
-    the sorted-point buffers, fine grids and cuFFT plans are allocated once."""
+    """Plans and solvers reused across solve_ac calls with the same (M, prec, operator, eps):
+    the sorted-point buffers, fine grids and cuFFT plans are allocated once; one CG solver
+    per CG precision shares the plans."""
 
     def __init__(self, M, prec, op, eps):
-        self.solver = CGSolver(M, prec=prec, op=op)
+        self.M, self.op = int(M), int(op)
+        self.solvers = {int(prec): CGSolver(M, prec=prec, op=op)}
+        self.solver = self.solvers[int(prec)]
         self.plan_M = Plan(1, M, eps=eps, isign=1, prec=prec)
         if op == TOEPLITZ and prec == 32:
             # bins of 5 fine cells and 16384 points per subproblem: the derived 2M plan's bins
@@ -236,6 +239,12 @@ class _Workspace:
 
     def plans(self):
         return [p for p in (self.plan_M, self.plan_2M) if p is not None]
+
+    def cg_solver(self, cg_prec):
+        s = self.solvers.get(int(cg_prec))
+        if s is None:
+            s = self.solvers[int(cg_prec)] = CGSolver(self.M, prec=cg_prec, op=self.op)
+        return s
 
 
 _WORKSPACES = {}
@@ -257,10 +266,17 @@ def clear_workspaces():
 
 def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, M, orientations=None,
              ac_estimate=None, use_gpu=True, use_recip_sym=True, *, maxiter=100, rtol=1e-5, prec=32,
-             operator="toeplitz", eps=DEFAULT_EPS, use_graph=True, return_info=False, rng=None, verbose=True):
+             operator="toeplitz", eps=DEFAULT_EPS, use_graph=True, return_info=False, rng=None, verbose=True,
+             cg_prec=None):
     """autocorrelation.py:176-248 on the GPU.  Returns the float64 (M, M, M) autocorrelation
     (numpy for numpy inputs, a CUDA tensor for tensor inputs); with ``return_info`` also a
-    dict with the iteration count."""
+    dict with the iteration count.
+
+    ``prec`` sets the NUFFT precision and, unless ``cg_prec`` is given, the CG's (32: FP32
+    vectors and FFT convolutions with FP64 dot products, norms and step scalars; 64: all
+    FP64).  ``cg_prec=64`` with ``prec=32`` is the reference's own precision split: FP32
+    NUFFT (finufft single precision, cmtip/nufft/adjoint.py:32-33) and a complex128-accurate
+    CG (scipy's cg on float64 d, :239)."""
     if not use_recip_sym:
         raise NotImplementedError("the GPU solver implements the reference's use_recip_sym=True path")
     numpy_io = not torch.is_tensor(slices_)
@@ -289,8 +305,10 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
         x0 = est.reshape(-1).to(torch.float64)
     alambda, rlambda, flambda = 1.0, Mtot / N / 1000, 1e3
     op = PAIR if operator == "pair" else TOEPLITZ
+    if cg_prec not in (None, prec) and op == PAIR:
+        raise ValueError("the pair operator runs in the NUFFT's precision (cg_prec must equal prec)")
     ws = _workspace(M, prec, op, eps, dev)
-    solver, plan_M, plan_2M = ws.solver, ws.plan_M, ws.plan_2M
+    solver, plan_M, plan_2M = ws.cg_solver(cg_prec or prec), ws.plan_M, ws.plan_2M
     solver.set_operator(sup, alambda, rlambda, flambda)
     # the intensities are first needed by the right-hand side, after the point sort and the
     # Toeplitz kernel: from pinned host memory their copy overlaps that work.  It is issued

@@ -21,16 +21,22 @@ from .nufft import DEFAULT_EPS, Plan, inverse_rotations
 
 class Slice(torch.autograd.Function):
     """c = Re(A f) on the points of ``plan2`` (type 2, isign -1); backward via ``plan1``
-    (type 1, isign +1, same points)."""
+    (type 1, isign +1, same points).  ``plan1`` must keep the forward's points until the
+    backward has run: giving it new points in between raises in the backward instead of
+    returning the gradient on the wrong points."""
 
     @staticmethod
     def forward(ctx, f: torch.Tensor, plan2: Plan, plan1: Plan):
         ctx.plan1 = plan1
+        ctx.points_version = plan1.points_version
         ctx.fshape = f.shape
         return plan2.execute(f.detach().reshape(-1), real_out=True)
 
     @staticmethod
     def backward(ctx, g: torch.Tensor):
+        if ctx.plan1.points_version != ctx.points_version:
+            raise RuntimeError("Slice.backward: the adjoint plan was given new points after the forward; "
+                               "run backward before re-pointing the plans (or use one SlicePlans per graph)")
         grad = ctx.plan1.execute(g.detach().contiguous().reshape(-1), real_out=True)
         return grad.reshape(ctx.fshape).to(g.dtype), None, None
 

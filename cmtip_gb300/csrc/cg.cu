@@ -696,19 +696,12 @@ extern "C" int cmt_support_from_estimate(float *est, int M, float *support, floa
     CMT_CHECK_ARG(est && support && scratch && M > 0, "bad argument");
     cudaStream_t st = (cudaStream_t)stream;
     int64_t m3 = (int64_t)M * M * M;
-    // ndimage _gaussian_kernel1d(sigma=0.5, radius=2)
-    double w[3];
-    double sum = 0.0;
-    for (int k = 0; k <= 2; ++k) {
-        w[k] = exp(-0.5 / (0.5 * 0.5) * k * k);
-        sum += k == 0 ? w[k] : 2 * w[k];
-    }
-    double phi[5];
+    // ndimage _gaussian_kernel1d(sigma=0.5, radius=2): normalised taps exp(-k^2 / (2 sigma^2))
+    double phi[5], w[3];
     for (int k = -2; k <= 2; ++k) phi[k + 2] = exp(-0.5 / (0.5 * 0.5) * k * k);
     double tot = 0.0;
     for (double v : phi) tot += v;
     for (int k = 0; k <= 2; ++k) w[k] = phi[k + 2] / tot;
-    (void)sum;
     float *a = scratch, *b = scratch + m3;
     unsigned gb = (unsigned)ceil_div(m3, 256);
     k_gauss_axis<<<gb, 256, 0, st>>>(est, a, M, 0, w[0], w[1], w[2]);
@@ -722,11 +715,11 @@ extern "C" int cmt_support_from_estimate(float *est, int M, float *support, floa
 // ---------------------------------------------------------------- allocation-free variant
 //
 // Same computation as cmt_support_from_estimate, for callers that cannot allocate device
-// memory: a host program driving this library from inside CUDA graph capture (a plain
-// cudaMalloc is not capturable), or one that hands the GPU's memory to its own pool and
-// forbids any other allocator from taking or returning blocks.  The two M^3 float grids
-// of scratch live in a file-scope device array, so every GPU that loads the library holds
-// CMT_NOALLOC_MAX_M^3 * 2 floats (16 MiB) until the process exits.
+// memory: a host whose own pool has reserved the GPU's memory and forbids any other
+// allocator from taking or returning blocks, or a latency-bound caller that cannot take
+// the device-wide synchronisation a cudaMalloc / cudaFree may cause.  The two M^3 float
+// grids of scratch live in a file-scope device array, so every GPU that loads the library
+// holds CMT_NOALLOC_MAX_M^3 * 2 floats (16 MiB) until the process exits.
 static __device__ __align__(256) float g_support_scratch[2 * CMT_NOALLOC_MAX_M * CMT_NOALLOC_MAX_M *
                                                          CMT_NOALLOC_MAX_M];
 
@@ -738,7 +731,8 @@ float *g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device.  Host code only sees a
 // host-side stand-in under the array's name, so the address is looked up once per
-// device (with that device current) and cached.
+// device (with that device current) and cached by device ordinal; a cudaDeviceReset
+// invalidates the cached address, and callers must not use this entry point after one.
 static int scratch_address(float **out)
 {
     int dev = 0;

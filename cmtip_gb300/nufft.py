@@ -82,6 +82,15 @@ class Plan:
     def N(self):
         return self._src.N if getattr(self, "_src", None) is not None else self._n
 
+    @property
+    def points_version(self) -> int:
+        """Incremented whenever the plan's points (or its source plan's) are replaced."""
+        src = getattr(self, "_src", None)
+        return src.points_version if src is not None else getattr(self, "_pts_version", 0)
+
+    def _bump_points(self):
+        self._pts_version = getattr(self, "_pts_version", 0) + 1
+
     @N.setter
     def N(self, value):
         self._n = value
@@ -126,6 +135,7 @@ class Plan:
     def set_tuning(self, bin_size: int = 0, maxsub: int = 0) -> "Plan":
         _lib.call("cmt_plan_set_tuning", self._h, int(bin_size), int(maxsub))
         self.N = 0
+        self._bump_points()
         return self
 
     def tuning(self) -> dict:
@@ -143,6 +153,7 @@ class Plan:
             _lib.call("cmt_set_pts", self._h, x.numel(), _ptr(x), _ptr(y), _ptr(z))
         self.N = x.numel()
         self._keep = (x, y, z)
+        self._bump_points()
         return self
 
     def set_pts_quat(self, inv_rot: torch.Tensor, ppr: torch.Tensor, reciprocal_extent: float):
@@ -154,6 +165,7 @@ class Plan:
             _lib.call("cmt_set_pts_quat", self._h, n_img, _ptr(inv_rot), n_pix, _ptr(ppr), float(reciprocal_extent))
         self.N = n_img * n_pix
         self._keep = (inv_rot, ppr)
+        self._bump_points()
         return self
 
     # -- execution

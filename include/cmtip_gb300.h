@@ -199,14 +199,16 @@ int cmt_support_from_estimate(float *est, int M, float *support, float *scratch,
 #define CMT_NOALLOC_MAX_M 128
 
 /* cmt_support_from_estimate without the scratch argument and without any allocation, for
- * callers that cannot allocate device memory: code running inside CUDA graph capture, or
- * an application whose own pool owns the GPU's memory.  No counterpart in the reference
- * (cmtip computes the support on the host with scipy).  The scratch is a fixed
- * 2 * 128^3-float (16 MiB) device array that every GPU loading the library keeps until the
- * process exits; M > CMT_NOALLOC_MAX_M returns CMT_ERR_ARG.  The first call on a device
- * looks the array's device address up: make it before any stream capture.  All calls share
- * the array, so calls that overlap on the GPU (other streams, other host threads) race:
- * order them on one stream. */
+ * callers that cannot allocate device memory: a host whose own memory pool has reserved the
+ * whole GPU (a cudaMalloc here would fail or fragment that pool), or a latency-bound caller
+ * that cannot take the device-wide synchronisation a cudaMalloc / cudaFree may cause.  No
+ * counterpart in the reference (cmtip computes the support on the host with scipy).  The
+ * scratch is a fixed 2 * 128^3-float (16 MiB) device array that every GPU loading the
+ * library keeps until the process exits; M > CMT_NOALLOC_MAX_M returns CMT_ERR_ARG.  The
+ * first call on a device looks the array's device address up and caches it for that device
+ * ordinal (the cache does not survive cudaDeviceReset): make that first call before any
+ * stream capture.  All calls share the array, so calls that overlap on the GPU (other
+ * streams, other host threads) race: order them on one stream. */
 int cmt_support_from_estimate_noalloc(float *est, int M, float *support, int est_inplace, void *stream);
 
 /* ---------------------------------------------------------------- orientation matching

@@ -1,7 +1,9 @@
 """Generate the golden fixtures in this folder by running the UNMODIFIED reference.
 
-This script is the only place that imports the reference (cmtip) itself, from the
-read-only checkout at /root/reference; it runs in the development container only.
+This script is the only place that imports the reference (cmtip) itself, from a
+read-only checkout named by ``--reference PATH`` or the ``CMTIP_REFERENCE`` environment
+variable (the directory that holds the ``cmtip`` package); it runs in the development
+container only.
 Third-party modules the reference needs but that are absent here are replaced by
 stubs in ``sys.modules`` before import:
 
@@ -14,7 +16,8 @@ The package ``cmtip`` is registered without executing ``cmtip/__init__.py`` (whi
 pulls in h5py/mrcfile/skopi-GPU drivers); only the hot-path submodules are loaded.
 Outputs: small ``.npz`` files holding inputs and the reference's outputs.
 
-Run:  python tests/golden/make_golden.py  (``--phasing``: only the phasing fixture)
+Run:  python tests/golden/make_golden.py --reference PATH [--only NAME ...]
+      (NAME: core, phasing; default: all)
 """
 from __future__ import annotations
 
@@ -26,7 +29,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = os.environ.get("CMTIP_REFERENCE", "")
 sys.path.insert(0, REPO)
 
 from cmtip_gb300 import geometry  # noqa: E402
@@ -201,7 +204,6 @@ def main():
                         clip_ppr=c_ppr, trim_ppr=t_ppr, trim_img=t_img, index_map_bin2=im2)
     out["prep"] = (b2.shape, c_img.shape, t_img.shape, t_img.dtype)
     print(out)
-    phasing_fixtures()
 
 
 def phasing_fixtures():
@@ -273,8 +275,24 @@ def phasing_fixtures():
     print("phasing", {k: getattr(v, "shape", v) for k, v in res.items() if k.endswith("_ac")})
 
 
+FIXTURES = {"core": lambda: main(), "phasing": lambda: phasing_fixtures()}
+
+
+def _cli():
+    import argparse
+    global REF
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--reference", default=REF,
+                    help="checkout of the reference project (holds cmtip/); default $CMTIP_REFERENCE")
+    ap.add_argument("--only", nargs="*", choices=sorted(FIXTURES), default=None,
+                    help="fixtures to regenerate (default: all)")
+    a = ap.parse_args()
+    if not a.reference or not os.path.isdir(os.path.join(a.reference, "cmtip")):
+        ap.error("give the reference checkout with --reference PATH or CMTIP_REFERENCE")
+    REF = a.reference
+    for name in (a.only or list(FIXTURES)):
+        FIXTURES[name]()
+
+
 if __name__ == "__main__":
-    if "--phasing" in sys.argv:
-        phasing_fixtures()
-    else:
-        main()
+    _cli()

@@ -94,3 +94,16 @@ def test_chunked_least_squares_recomputes_slices(ag):
     r = plans(f) - data.reshape(-1).cuda()
     (0.5 * torch.dot(r, r)).backward()
     assert rel_l2(f.grad.cpu().numpy(), out[0][1]) < 1e-10
+
+
+def test_backward_refuses_repointed_plans(ag):
+    # the adjoint plan given new points between forward and backward: the gradient would be
+    # taken on the wrong points, so the backward raises instead
+    rng = np.random.default_rng(33)
+    M, N = 15, 300
+    plans = ag.SlicePlans(M, prec=64, eps=1e-9).set_pts(*_points(rng, N))
+    f = torch.from_numpy(rng.standard_normal((M,) * 3)).cuda().requires_grad_(True)
+    loss = plans(f).sum()
+    plans.set_pts(*_points(rng, N))
+    with pytest.raises(RuntimeError, match="new points"):
+        loss.backward()

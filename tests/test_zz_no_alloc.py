@@ -1,10 +1,11 @@
 """The allocation-free support filter (cmt_support_from_estimate_noalloc) against the
 allocating entry point, called through the C ABI.
 
-Callers that cannot allocate device memory (graph-captured pipelines, applications whose
-memory pool owns the GPU) use the allocation-free variant; it must give the same mask and
-the same masked estimate as cmt_support_from_estimate with caller scratch, call after
-call, since every call reuses one fixed device array.  This file is collected last.
+Callers that cannot allocate device memory (a host whose own memory pool has reserved the
+GPU, or a latency-bound caller that cannot take a cudaMalloc's synchronisation) use the
+allocation-free variant; it must give the same mask and the same masked estimate as
+cmt_support_from_estimate with caller scratch, call after call, since every call reuses
+one fixed device array.  This file is collected last.
 """
 import ctypes
 
