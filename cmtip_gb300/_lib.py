@@ -60,6 +60,7 @@ SIGNATURES = {
     "cmt_cg_set_pair_plan": [_vp, _vp],
     "cmt_cg_matvec": [_vp, _vp, _vp],
     "cmt_cg_solve": [_vp, _vp, _vp, _i32, _f64, _f64, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_f64)],
+    "cmt_cg_solve_many": [_i32, _vp, _vp, _vp, _i32, _f64, _f64, _vp, _vp],
     "cmt_cg_destroy": [_vp],
     "cmt_support_from_estimate": [_vp, _i32, _vp, _vp, _i32, _vp],
     "cmt_support_from_estimate_noalloc": [_vp, _i32, _vp, _i32, _vp],

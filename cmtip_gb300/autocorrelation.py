@@ -240,6 +240,14 @@ class _Workspace:
     def plans(self):
         return [p for p in (self.plan_M, self.plan_2M) if p is not None]
 
+    def sweep_solvers(self, cg_prec, n):
+        key = ("sweep", int(cg_prec))
+        lst = self.solvers.get(key, [])
+        while len(lst) < n:
+            lst.append(CGSolver(self.M, prec=cg_prec, op=self.op))
+        self.solvers[key] = lst
+        return lst[:n]
+
     def cg_solver(self, cg_prec):
         s = self.solvers.get(int(cg_prec))
         if s is None:
@@ -262,6 +270,44 @@ def _workspace(M, prec, op, eps, dev) -> _Workspace:
 
 def clear_workspaces():
     _WORKSPACES.clear()
+
+
+def _support_and_x0(ac_estimate, Mtot, dev):
+    """autocorrelation.py:213-220: the support (all ones without an estimate, else
+    gaussian_filter(est, 0.5) > 1e-12) and x0 = the estimate masked by it (zeros without
+    one); a float32 numpy estimate is masked in place, as the reference does."""
+    if ac_estimate is None:
+        return (torch.ones(Mtot, dtype=torch.float32, device=dev),
+                torch.zeros(Mtot, dtype=torch.float64, device=dev))
+    if torch.is_tensor(ac_estimate):
+        est = ac_estimate.to(dev, torch.float32).contiguous()
+    else:
+        est = torch.from_numpy(np.ascontiguousarray(ac_estimate, dtype=np.float32)).to(dev)
+    sup = support_from_estimate(est, inplace=True).reshape(-1)
+    if isinstance(ac_estimate, np.ndarray) and ac_estimate.dtype == np.float32:
+        ac_estimate *= sup.reshape(ac_estimate.shape).cpu().numpy()  # the reference masks in place
+    return sup, est.reshape(-1).to(torch.float64)
+
+
+def sweep_lambdas(Mtot, N, n):
+    """(rlambda, flambda) of ranks 0 .. n-1 of the reference's lambda scan on n MPI ranks
+    (cmtip/autocorrelation/autocorrelation_mpi.py:139-141): rlambda = Mtot / N * 2^(r - n/2),
+    flambda = 1e5 * 10^(r - n//2), with N the number of data points one rank holds."""
+    rl = [float(Mtot / np.int64(N) * 2 ** (r - n / 2)) for r in range(n)]
+    fl = [1e5 * pow(10, r - n // 2) for r in range(n)]
+    return np.array(rl), np.array(fl, dtype=np.float64)
+
+
+def sweep_select(generation, rlambdas, v1s, v2s):
+    """Index of the kept solution (autocorrelation_mpi.py:157-178): in generation 0 the
+    largest rlambda among the solutions with ||x|| >= mean ||x||, later the corner of the
+    L-curve, argmin(||x|| + ||W x - d||)."""
+    rlambdas, v1s, v2s = (np.asarray(a, dtype=np.float64) for a in (rlambdas, v1s, v2s))
+    if generation == 0:
+        idx = v1s >= np.mean(v1s)
+        imax = np.argmax(rlambdas[idx])
+        return int(np.arange(len(v1s), dtype=int)[idx][imax])
+    return int(np.argmin(v1s + v2s))
 
 
 def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, M, orientations=None,
@@ -291,18 +337,7 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
     ppr = _as_device(pixel_position_reciprocal, torch.float64).reshape(3, -1)
     quats = orientations if torch.is_tensor(orientations) else np.asarray(orientations, dtype=np.float32)
     inv_rot = inverse_rotations(quats, device=dev)
-    if ac_estimate is None:
-        sup = torch.ones(Mtot, dtype=torch.float32, device=dev)
-        x0 = torch.zeros(Mtot, dtype=torch.float64, device=dev)
-    else:
-        if torch.is_tensor(ac_estimate):
-            est = ac_estimate.to(dev, torch.float32).contiguous()
-        else:
-            est = torch.from_numpy(np.ascontiguousarray(ac_estimate, dtype=np.float32)).to(dev)
-        sup = support_from_estimate(est, inplace=True).reshape(-1)
-        if isinstance(ac_estimate, np.ndarray) and ac_estimate.dtype == np.float32:
-            ac_estimate *= sup.reshape(ac_estimate.shape).cpu().numpy()  # the reference masks in place
-        x0 = est.reshape(-1).to(torch.float64)
+    sup, x0 = _support_and_x0(ac_estimate, Mtot, dev)
     alambda, rlambda, flambda = 1.0, Mtot / N / 1000, 1e3
     op = PAIR if operator == "pair" else TOEPLITZ
     if cg_prec not in (None, prec) and op == PAIR:
@@ -334,6 +369,81 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
     if return_info:
         return out, {"iterations": iters, "d": d, "x0": x0, "solver": solver}
     return out
+
+
+def solve_ac_sweep(generation, pixel_position_reciprocal, reciprocal_extent, slices_, M, orientations=None,
+                   ac_estimate=None, use_gpu=True, use_recip_sym=True, *, n_lambdas=8, maxiter=100, rtol=1e-5,
+                   prec=32, cg_prec=None, eps=DEFAULT_EPS, return_info=False, rng=None, verbose=True):
+    """The lambda scan of cmtip/autocorrelation/autocorrelation_mpi.py:99-190 (solve_ac_mpi)
+    on one GPU: the n_lambdas ranks' solves share the points, the Toeplitz kernel and the
+    type-1 of the data, and differ in (rlambda, flambda) (sweep_lambdas) and thus in
+    d = A^H b + rlambda x0; their CG iterations run together as independent branches of one
+    captured graph (cmt_cg_solve_many), each with scipy's stopping rule (rtol 1e-5,
+    maxiter 100, autocorrelation_mpi.py:142,153).  The kept solution follows the
+    reference's rule (sweep_select) on v1 = ||x||, v2 = ||W x - d||.  Every rank here holds
+    the whole image set (N = all data points, as one rank of the reference holding all
+    images).  Returns the kept float64 (M, M, M) autocorrelation; with ``return_info`` also
+    the lambdas, v1, v2, iteration counts, all solutions and the kept index."""
+    if not use_recip_sym:
+        raise NotImplementedError("the GPU solver implements the reference's use_recip_sym=True path")
+    numpy_io = not torch.is_tensor(slices_)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    Mtot = M ** 3
+    N = int(np.prod(slices_.shape))
+    if orientations is None:
+        from .geometry import random_quaternions
+        orientations = random_quaternions(slices_.shape[0], rng or np.random.default_rng())
+    rt = torch.float64 if prec == 64 else torch.float32
+    ppr = _as_device(pixel_position_reciprocal, torch.float64).reshape(3, -1)
+    quats = orientations if torch.is_tensor(orientations) else np.asarray(orientations, dtype=np.float32)
+    inv_rot = inverse_rotations(quats, device=dev)
+    sup, x0 = _support_and_x0(ac_estimate, Mtot, dev)
+    rls, fls = sweep_lambdas(Mtot, N, n_lambdas)
+    ws = _workspace(M, prec, TOEPLITZ, eps, dev)
+    solvers = ws.sweep_solvers(cg_prec or prec, n_lambdas)
+    data, data_ready = _as_device_async(slices_, torch.float32)
+    ws.plan_M.set_pts_quat(inv_rot, ppr, float(reciprocal_extent))
+    kern = toeplitz_kernel(ws.plan_2M, M)
+    if data_ready is not None:
+        torch.cuda.current_stream().wait_event(data_ready)
+    data = data.reshape(-1)
+    adb = ws.plan_M.execute(data if data.dtype == rt else data.to(rt), support=sup, scale=1.0 / float(M) ** 3,
+                            real_out=True).reshape(-1).to(torch.float64)
+    ds, xs = [], []
+    for s, rl, fl in zip(solvers, rls, fls):
+        s.set_operator(sup, 1.0, rl, fl)
+        s.set_kernel(kern)
+        ds.append((adb + rl * x0).to(s.dtype).contiguous())
+        xs.append(x0.to(s.dtype).clone())
+    its = solve_many(solvers, ds, xs, maxiter=maxiter, rtol=rtol)
+    v1 = np.array([float(torch.linalg.norm(x.double())) for x in xs])
+    v2 = np.array([float(torch.linalg.norm(s.matvec(x).double() - d.double())) for s, x, d in zip(solvers, xs, ds)])
+    keep = sweep_select(generation, rls, v1, v2)
+    ac = xs[keep].to(torch.float64).reshape((M,) * 3)
+    if verbose:
+        for r, it in enumerate(its):
+            print(f"Rank {r} got AC in {it} iterations.", flush=True)
+        print(f"Keeping result from rank {keep}.", flush=True)
+    out = ac.cpu().numpy() if numpy_io else ac
+    if return_info:
+        return out, {"rlambdas": rls, "flambdas": fls, "v1": v1, "v2": v2, "iterations": its, "keep": keep,
+                     "solutions": [x.to(torch.float64).reshape((M,) * 3) for x in xs]}
+    return out
+
+
+def solve_many(solvers, ds, xs, maxiter=100, rtol=1e-5, atol=0.0):
+    """Run several CGSolvers' solves together (cmt_cg_solve_many): xs (x0 in, solutions out)
+    and ds are device vectors of each solver's precision.  Returns the iteration counts."""
+    n = len(solvers)
+    arr = lambda objs: (ctypes.c_void_p * n)(*[o for o in objs])
+    hs = arr([s._h.value for s in solvers])
+    dp = arr([d.data_ptr() for d in ds])
+    xp = arr([x.data_ptr() for x in xs])
+    its = (ctypes.c_int * n)()
+    rho = (ctypes.c_double * n)()
+    with torch.cuda.device(solvers[0].device):
+        _lib.call("cmt_cg_solve_many", n, hs, dp, xp, int(maxiter), float(rtol), float(atol), its, rho)
+    return [int(v) for v in its]
 
 
 def solve_tikhonov(pixel_position_reciprocal, reciprocal_extent, slices_, M, orientations, weights=None, lam=1e-3,

@@ -421,13 +421,13 @@ static int route_to(Cg &c, cudaStream_t s)
 // captured) and instantiate it; the graph is then launched on the caller's stream.
 template <typename T> static int iteration(Cg &c);
 
+// Capture one iteration on the private stream (legacy-default-stream callers cannot be
+// captured) into *out (not instantiated); the solver's launches are routed back to its
+// stream afterwards.
 template <typename T>
-static int capture_iteration(Cg &c)
+static int capture_graph(Cg &c, cudaGraph_t *out)
 {
-    if (c.graph) {
-        cudaGraphExecDestroy(c.graph);
-        c.graph = nullptr;
-    }
+    *out = nullptr;
     if (!c.cap_stream) CMT_TRY_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
     cudaStream_t user = c.stream;
     CMT_TRY(route_to(c, c.cap_stream));
@@ -441,18 +441,96 @@ static int capture_iteration(Cg &c)
         if (graph) cudaGraphDestroy(graph);
         return CMT_ERR_CUDA;
     }
-    if (rc != CMT_OK) {
+    if (rc != CMT_OK || rc2 != CMT_OK) {
         cudaGraphDestroy(graph);
-        return rc;
+        return rc != CMT_OK ? rc : rc2;
     }
-    if (rc2 != CMT_OK) {
-        cudaGraphDestroy(graph);
-        return rc2;
+    *out = graph;
+    return CMT_OK;
+}
+
+// Capture one iteration and instantiate it; the graph is then launched on the caller's stream.
+template <typename T>
+static int capture_iteration(Cg &c)
+{
+    if (c.graph) {
+        cudaGraphExecDestroy(c.graph);
+        c.graph = nullptr;
     }
-    e = cudaGraphInstantiate(&c.graph, graph, 0);
+    cudaGraph_t graph = nullptr;
+    CMT_TRY(capture_graph<T>(c, &graph));
+    cudaError_t e = cudaGraphInstantiate(&c.graph, graph, 0);
     cudaGraphDestroy(graph);
     CMT_TRY_CUDA(e);
     c.ready = true;
+    return CMT_OK;
+}
+
+// Start of a solve (scipy's cg before its loop): b = d, x = x0, ||b||, r0 = b - W x0 when x0
+// has a nonzero entry (else r0 = b), rho = r0.r0, stopping threshold max(atol, rtol ||b||).
+// *trivial: ||b|| = 0, where scipy returns b itself (already copied into x).
+template <typename T>
+static int solve_begin(Cg &c, const T *d, T *x, double rtol, double atol, bool *trivial)
+{
+    cudaStream_t st = c.stream;
+    size_t bytes = sizeof(T) * c.m3;
+    int g = grid_elems(c.m3);
+    *trivial = false;
+    CMT_TRY_CUDA(cudaMemsetAsync(c.sc, 0, sizeof(CgScalars), st));
+    CMT_TRY_CUDA(cudaMemcpyAsync(c.b, d, bytes, cudaMemcpyDeviceToDevice, st));
+    CMT_TRY_CUDA(cudaMemcpyAsync(c.x, x, bytes, cudaMemcpyDeviceToDevice, st));
+    CgScalars *sc = c.sc;
+    k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.b, (const T *)c.b, c.m3, c.partial, &sc->ticket[2],
+                                                 &sc->bnorm);
+    CMT_LAUNCH_CHECK();
+    k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.x, (const T *)c.x, c.m3, c.partial, &sc->ticket[3],
+                                                 &sc->pq);
+    CMT_LAUNCH_CHECK();
+    CgScalars h;
+    CMT_TRY_CUDA(cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st));
+    CMT_TRY_CUDA(cudaStreamSynchronize(st));
+    const double xx_host = h.pq;
+    const double bnorm = sqrt(h.bnorm);
+    if (bnorm == 0.0) {  // scipy returns b itself
+        CMT_TRY_CUDA(cudaMemcpyAsync(x, c.b, bytes, cudaMemcpyDeviceToDevice, st));
+        *trivial = true;
+        return CMT_OK;
+    }
+    CgScalars init = h;
+    init.bnorm = bnorm;
+    init.atol = std::max(atol, rtol * bnorm);
+    init.it = 0;
+    init.done = 0;
+    init.pq = 0.0;
+    memset(init.ticket, 0, sizeof init.ticket);
+    CMT_TRY_CUDA(cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st));
+    CMT_TRY_CUDA(cudaStreamSynchronize(st));
+    if (xx_host != 0.0) {
+        CMT_TRY(matvec_impl<T>(c, (const T *)c.x, (T *)c.q, false));
+        k_residual<T><<<g, 256, 0, st>>>((const T *)c.b, (const T *)c.q, (T *)c.r, c.m3);
+        CMT_LAUNCH_CHECK();
+    } else {
+        CMT_TRY_CUDA(cudaMemcpyAsync(c.r, c.b, bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.r, (const T *)c.r, c.m3, c.partial, &sc->ticket[2],
+                                                 &sc->rho);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+// End of a solve: x out, iteration count and r.r (host, optional; synchronises).
+template <typename T>
+static int solve_end(Cg &c, T *x, bool trivial, int *iters, double *final_rho)
+{
+    cudaStream_t st = c.stream;
+    if (!trivial) CMT_TRY_CUDA(cudaMemcpyAsync(x, c.x, sizeof(T) * c.m3, cudaMemcpyDeviceToDevice, st));
+    if (iters || final_rho) {
+        CgScalars h;
+        CMT_TRY_CUDA(cudaMemcpyAsync(&h, c.sc, sizeof h, cudaMemcpyDeviceToHost, st));
+        CMT_TRY_CUDA(cudaStreamSynchronize(st));
+        if (iters) *iters = trivial ? 0 : h.it;
+        if (final_rho) *final_rho = trivial ? 0.0 : h.rho;
+    }
     return CMT_OK;
 }
 
@@ -603,67 +681,86 @@ template <typename T>
 static int solve_impl(Cg &c, const T *d, T *x, int maxiter, double rtol, double atol, int use_graph, int *iters,
                       double *final_rho)
 {
-    cudaStream_t st = c.stream;
-    size_t bytes = sizeof(T) * c.m3;
-    int g = grid_elems(c.m3);
-    CMT_TRY_CUDA(cudaMemsetAsync(c.sc, 0, sizeof(CgScalars), st));
-    CMT_TRY_CUDA(cudaMemcpyAsync(c.b, d, bytes, cudaMemcpyDeviceToDevice, st));
-    CMT_TRY_CUDA(cudaMemcpyAsync(c.x, x, bytes, cudaMemcpyDeviceToDevice, st));
-    // ||b||, x0.any()
-    CgScalars *sc = c.sc;
-    k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.b, (const T *)c.b, c.m3, c.partial, &sc->ticket[2],
-                                                 &sc->bnorm);
-    CMT_LAUNCH_CHECK();
-    double xx_host = 0.0;
-    {
-        k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.x, (const T *)c.x, c.m3, c.partial,
-                                                     &sc->ticket[3], &sc->pq);
-        CMT_LAUNCH_CHECK();
-        CgScalars h;
-        CMT_TRY_CUDA(cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st));
-        CMT_TRY_CUDA(cudaStreamSynchronize(st));
-        xx_host = h.pq;
-        double bnorm = sqrt(h.bnorm);
-        if (bnorm == 0.0) {  // scipy returns b itself
-            CMT_TRY_CUDA(cudaMemcpyAsync(x, c.b, bytes, cudaMemcpyDeviceToDevice, st));
-            if (iters) *iters = 0;
-            if (final_rho) *final_rho = 0.0;
-            return CMT_OK;
+    bool trivial = false;
+    CMT_TRY(solve_begin<T>(c, d, x, rtol, atol, &trivial));
+    if (!trivial) {
+        if (use_graph) {
+            if (!c.ready) CMT_TRY(capture_iteration<T>(c));
+            for (int it = 0; it < maxiter; ++it) CMT_TRY_CUDA(cudaGraphLaunch(c.graph, c.stream));
+        } else {
+            for (int it = 0; it < maxiter; ++it) CMT_TRY(iteration<T>(c));
         }
-        CgScalars init = h;
-        init.bnorm = bnorm;
-        init.atol = std::max(atol, rtol * bnorm);
-        init.it = 0;
-        init.done = 0;
-        init.pq = 0.0;
-        memset(init.ticket, 0, sizeof init.ticket);
-        CMT_TRY_CUDA(cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st));
-        CMT_TRY_CUDA(cudaStreamSynchronize(st));
     }
-    if (xx_host != 0.0) {
-        CMT_TRY(matvec_impl<T>(c, (const T *)c.x, (T *)c.q, false));
-        k_residual<T><<<g, 256, 0, st>>>((const T *)c.b, (const T *)c.q, (T *)c.r, c.m3);
-    } else {
-        CMT_TRY_CUDA(cudaMemcpyAsync(c.r, c.b, bytes, cudaMemcpyDeviceToDevice, st));
+    return solve_end<T>(c, x, trivial, iters, final_rho);
+}
+
+// Several solvers at once: each one's iteration is captured as a child graph of one parent
+// graph with no edges between the children, so one launch of the parent runs one iteration
+// of every solve and the independent branches overlap on the GPU.  Every solver keeps its own
+// operator, scalars and stopping test; all run on the stream of the first.
+template <typename T>
+static int solve_many_impl(int n, cmt_cg *const *cgs, const void *const *d, void *const *x, int maxiter, double rtol,
+                           double atol, int *iters, double *final_rho)
+{
+    cudaStream_t st = cgs[0]->stream;
+    std::vector<cudaStream_t> own(n);
+    std::vector<char> trivial(n, 0);
+    for (int i = 0; i < n; ++i) {
+        own[i] = cgs[i]->stream;
+        CMT_TRY(route_to(*cgs[i], st));
     }
-    k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.r, (const T *)c.r, c.m3, c.partial, &sc->ticket[2],
-                                                 &sc->rho);
-    CMT_LAUNCH_CHECK();
-    if (use_graph) {
-        if (!c.ready) CMT_TRY(capture_iteration<T>(c));
-        for (int it = 0; it < maxiter; ++it) CMT_TRY_CUDA(cudaGraphLaunch(c.graph, st));
-    } else {
-        for (int it = 0; it < maxiter; ++it) CMT_TRY(iteration<T>(c));
+    auto restore = [&]() {
+        for (int i = 0; i < n; ++i) route_to(*cgs[i], own[i]);
+    };
+    int rc = CMT_OK;
+    for (int i = 0; i < n && rc == CMT_OK; ++i) {
+        bool t = false;
+        rc = solve_begin<T>(*cgs[i], (const T *)d[i], (T *)x[i], rtol, atol, &t);
+        trivial[i] = t;
     }
-    CMT_TRY_CUDA(cudaMemcpyAsync(x, c.x, bytes, cudaMemcpyDeviceToDevice, st));
-    if (iters || final_rho) {
-        CgScalars h;
-        CMT_TRY_CUDA(cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st));
-        CMT_TRY_CUDA(cudaStreamSynchronize(st));
-        if (iters) *iters = h.it;
-        if (final_rho) *final_rho = h.rho;
+    cudaGraph_t parent = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (rc == CMT_OK) {
+        cudaError_t e = cudaGraphCreate(&parent, 0);
+        if (e != cudaSuccess) {
+            set_error("cudaGraphCreate: %s", cudaGetErrorString(e));
+            rc = CMT_ERR_CUDA;
+        }
     }
-    return CMT_OK;
+    for (int i = 0; i < n && rc == CMT_OK; ++i) {
+        if (trivial[i]) continue;
+        cudaGraph_t child = nullptr;
+        rc = capture_graph<T>(*cgs[i], &child);
+        if (rc != CMT_OK) break;
+        cudaGraphNode_t node;
+        cudaError_t e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, child);
+        cudaGraphDestroy(child);  // the parent holds a copy
+        if (e != cudaSuccess) {
+            set_error("cudaGraphAddChildGraphNode: %s", cudaGetErrorString(e));
+            rc = CMT_ERR_CUDA;
+        }
+    }
+    if (rc == CMT_OK) {
+        cudaError_t e = cudaGraphInstantiate(&exec, parent, 0);
+        if (e != cudaSuccess) {
+            set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+            rc = CMT_ERR_CUDA;
+        }
+    }
+    for (int it = 0; it < maxiter && rc == CMT_OK; ++it) {
+        cudaError_t e = cudaGraphLaunch(exec, st);
+        if (e != cudaSuccess) {
+            set_error("cudaGraphLaunch: %s", cudaGetErrorString(e));
+            rc = CMT_ERR_CUDA;
+        }
+    }
+    for (int i = 0; i < n && rc == CMT_OK; ++i)
+        rc = solve_end<T>(*cgs[i], (T *)x[i], trivial[i], iters ? iters + i : nullptr,
+                          final_rho ? final_rho + i : nullptr);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (parent) cudaGraphDestroy(parent);
+    restore();
+    return rc;
 }
 
 // Solve W x = d from x (in: x0, out: solution) with at most maxiter iterations,
@@ -678,6 +775,30 @@ extern "C" int cmt_cg_solve(cmt_cg *c, const void *d, void *x, int maxiter, doub
     if (c->prec == 64)
         return solve_impl<double>(*c, (const double *)d, (double *)x, maxiter, rtol, atol, use_graph, iters, final_rho);
     return solve_impl<float>(*c, (const float *)d, (float *)x, maxiter, rtol, atol, use_graph, iters, final_rho);
+}
+
+// Run the solves of n solvers (same precision and device) together: d[i], x[i] as for
+// cmt_cg_solve on cgs[i]; iters[i] / final_rho[i] optional (host arrays of n).  Used for the
+// lambda sweep of cmtip/autocorrelation/autocorrelation_mpi.py:139-186, whose ranks solve
+// the same data with different lambdas.
+extern "C" int cmt_cg_solve_many(int n, cmt_cg *const *cgs, const void *const *d, void *const *x, int maxiter,
+                                 double rtol, double atol, int *iters, double *final_rho)
+{
+    CMT_CHECK_ARG(n >= 1 && n <= 64 && cgs && d && x, "need 1..64 solvers and their d / x arrays");
+    CMT_CHECK_ARG(maxiter >= 0, "maxiter must be >= 0");
+    for (int i = 0; i < n; ++i) {
+        CMT_CHECK_ARG(cgs[i] && d[i] && x[i], "null solver, d or x at %d", i);
+        CMT_CHECK_ARG(cgs[i]->prec == cgs[0]->prec, "solvers of one call share a precision");
+        CMT_CHECK_ARG(cgs[i]->op == 0 || cgs[i]->pair_plan, "pair operator without a plan at %d", i);
+        for (int j = 0; j < i; ++j) {
+            CMT_CHECK_ARG(cgs[j] != cgs[i], "solver %d given twice", i);
+            CMT_CHECK_ARG(!cgs[i]->pair_plan || cgs[j]->pair_plan != cgs[i]->pair_plan,
+                          "solvers %d and %d share a pair plan (its grids would race)", j, i);
+        }
+    }
+    if (cgs[0]->prec == 64)
+        return solve_many_impl<double>(n, cgs, d, x, maxiter, rtol, atol, iters, final_rho);
+    return solve_many_impl<float>(n, cgs, d, x, maxiter, rtol, atol, iters, final_rho);
 }
 
 extern "C" int cmt_cg_destroy(cmt_cg *c)

@@ -188,6 +188,16 @@ int cmt_cg_matvec(cmt_cg *cg, const void *x, void *y);
 int cmt_cg_solve(cmt_cg *cg, const void *d, void *x, int maxiter, double rtol, double atol,
                  int use_graph, int *iters, double *final_rho);
 
+/* The solves of n solvers (1..64, one precision, one device) at once: cgs[i] solves
+ * W_i x_i = d_i from x_i as cmt_cg_solve does (d[i], x[i] device vectors of its precision),
+ * each with its own operator, lambdas and stopping test.  One iteration of every solver is
+ * captured as an independent branch of one CUDA graph, so the branches overlap on the GPU;
+ * all run on the stream of cgs[0].  iters / final_rho: optional host arrays of n.  Replaces
+ * the rank-parallel lambda scan of cmtip/autocorrelation/autocorrelation_mpi.py:139-155
+ * (one scipy cg per MPI rank, each rank with its own rlambda / flambda). */
+int cmt_cg_solve_many(int n, cmt_cg *const *cgs, const void *const *d, void *const *x, int maxiter, double rtol,
+                      double atol, int *iters, double *final_rho);
+
 int cmt_cg_destroy(cmt_cg *cg);
 
 /* support = gaussian_filter(est, 0.5) > 1e-12 as 0/1 floats, and est *= support when

@@ -275,7 +275,135 @@ def phasing_fixtures():
     print("phasing", {k: getattr(v, "shape", v) for k, v in res.items() if k.endswith("_ac")})
 
 
-FIXTURES = {"core": lambda: main(), "phasing": lambda: phasing_fixtures()}
+class _RankComm:
+    """Rank ``rank`` of a ``size``-rank communicator in which every rank holds the whole data
+    set, for running the reference's MPI lambda scan (autocorrelation_mpi.py:99-190) one rank
+    after another in one process: Reduce keeps the rank's own grid (the data are that rank's),
+    the broadcasts of reduced grids are no-ops, and rank 0 -- run last -- gathers the
+    summaries the other ranks recorded and receives the kept rank's solution by Bcast."""
+
+    def __init__(self, rank, size, book):
+        self.rank, self.size, self.book = rank, size, book
+
+    def Reduce(self, send, recv, op=None, root=0):
+        recv[...] = send
+
+    def Bcast(self, buf, root=0):
+        if self.rank == 0 and root != 0:
+            buf[...] = self.book["ac"][root]
+
+    def bcast(self, obj, root=0):
+        return obj if self.rank == root else -1
+
+    def gather(self, obj, root=0):
+        self.book["summary"][self.rank] = obj
+        if self.rank != root:
+            return None
+        return [self.book["summary"][r] for r in range(self.size)]
+
+
+def sweep_fixture():
+    """7. the lambda scan of autocorrelation_mpi.py:99-190 on n ranks, generations 0 and 1."""
+    import contextlib
+    import importlib
+    import io
+    import re
+    _install_stubs()
+    mpi = types.ModuleType("mpi4py")
+    mpi.MPI = types.SimpleNamespace(SUM="sum")
+    sys.modules["mpi4py"] = mpi
+    acm = importlib.import_module("cmtip.autocorrelation.autocorrelation_mpi")
+    solved = []
+    scipy_cg = acm.cg
+
+    def recording_cg(*args, **kwargs):  # scipy's cg unchanged; keeps each rank's own solution
+        ret = scipy_cg(*args, **kwargs)
+        solved.append(np.ascontiguousarray(ret[0].real))
+        return ret
+
+    acm.cg = recording_cg
+    case = synthetic_case(M=21, n_img=12, P=8, n_atoms=20, radius=4.0, seed=71)
+    rng = np.random.default_rng(72)
+    est = (case["ac"] * (1.0 + 0.05 * rng.standard_normal(case["ac"].shape))).astype(np.float32)
+    size, M = 6, 21
+    out = dict(quats=case["quats"], ppr=case["ppr"], rext=case["rext"], slices=case["slices"], estimate=est,
+               M=M, size=size)
+    for gen in (0, 1):
+        book = {"summary": {}, "ac": {}}
+        its, own = {}, {}
+        for rank in list(range(1, size)) + [0]:
+            buf = io.StringIO()
+            with contextlib.redirect_stdout(buf):
+                ac = acm.solve_ac_mpi(_RankComm(rank, size, book), gen, case["ppr"], case["rext"],
+                                      case["slices"], M, orientations=case["quats"],
+                                      ac_estimate=None if gen == 0 else est.copy(), use_gpu=False)
+            its[rank] = int(re.search(r"got AC in (\d+) iterations", buf.getvalue()).group(1))
+            own[rank] = solved[-1].reshape((M,) * 3)
+            if rank != 0:
+                book["ac"][rank] = ac.copy()
+            else:
+                kept = re.search(r"Keeping result from rank (\d+)", buf.getvalue())
+                out[f"g{gen}_keep"] = int(kept.group(1))
+                out[f"g{gen}_ac"] = ac
+        ranks, lambdas, v1s, v2s = [np.array(el) for el in zip(*[book["summary"][r] for r in range(size)])]
+        out.update({f"g{gen}_rlambdas": lambdas, f"g{gen}_v1": v1s, f"g{gen}_v2": v2s,
+                    f"g{gen}_iterations": np.array([its[r] for r in range(size)]),
+                    f"g{gen}_solutions": np.stack([own[r] for r in range(size)])})
+    acm.cg = scipy_cg
+    np.savez_compressed(os.path.join(HERE, "lambda_sweep.npz"), **out)
+    print("lambda_sweep", {k: out[k] for k in ("g0_keep", "g1_keep")}, out["g0_iterations"], out["g1_iterations"])
+    for gen in (0, 1):
+        print(gen, out[f"g{gen}_v1"], out[f"g{gen}_v2"], np.mean(out[f"g{gen}_v1"]))
+
+
+LOOP = dict(M=21, n_img=30, P=8, n_atoms=20, radius=4.0, seed=81, generations=3, np_seed=17,
+            phase=dict(n_iterations=1, nER=5, nHIO=5))
+
+
+def loop_fixture():
+    """8. the MTIP generation loop (reconstruct.py:29-96, run_mtip) on a small case, not
+    aligned: random generation-0 orientations (the skopi stub's seeded generator), then
+    matching against the reference's hard-coded 5000 references at its 9 A resolution limit.
+    Two stand-ins: save_checkpoint (h5py / mrcfile) records each generation's checkpoint in
+    memory, and phase() runs a short schedule (LOOP['phase']) -- ER / HIO from a random start
+    are chaotic over the default 1300 iterations, so only short schedules can be compared."""
+    import functools
+    import importlib
+    _install_stubs()
+    sys.modules["h5py"] = types.ModuleType("h5py")
+    pk = types.ModuleType("cmtip.phasing")
+    pk.__path__ = [os.path.join(REF, "cmtip", "phasing")]  # skip __init__ (maps.py needs mrcfile)
+    sys.modules["cmtip.phasing"] = pk
+    ph = importlib.import_module("cmtip.phasing.phase")
+    pk.phase = functools.partial(ph.phase, **LOOP["phase"])
+    rec = importlib.import_module("cmtip.reconstruct")
+    saved = {}
+
+    def record(generation, output, checkpoint):
+        saved[generation] = {k: (np.array(v, copy=True) if isinstance(v, np.ndarray) else v)
+                             for k, v in checkpoint.items()}
+
+    rec.save_checkpoint = record
+    case = synthetic_case(M=LOOP["M"], n_img=LOOP["n_img"], P=LOOP["P"], n_atoms=LOOP["n_atoms"],
+                          radius=LOOP["radius"], seed=LOOP["seed"])
+    data = {"pixel_position_reciprocal": case["ppr"], "reciprocal_extent": case["rext"],
+            "intensities": case["slices"], "orientations": case["quats"]}
+    np.random.seed(LOOP["np_seed"])
+    rec.run_mtip(data, LOOP["M"], "unused", aligned=False, n_iterations=LOOP["generations"], use_gpu=False,
+                 checkpoint=rec.load_checkpoint())
+    out = dict(ppr=case["ppr"], rext=case["rext"], slices=case["slices"], quats_true=case["quats"],
+               ac_true=case["ac"], M=LOOP["M"], np_seed=LOOP["np_seed"], stub_seed=1234,
+               generations=LOOP["generations"], **{"phase_" + k: v for k, v in LOOP["phase"].items()})
+    for g, ck in saved.items():
+        for k in ("orientations", "ac", "ac_phased", "support_", "rho_"):
+            if ck.get(k) is not None:
+                out[f"g{g}_{k}"] = ck[k]
+    np.savez_compressed(os.path.join(HERE, "mtip_loop.npz"), **out)
+    print("mtip_loop", sorted(k for k in out if k.startswith("g")))
+
+
+FIXTURES = {"core": lambda: main(), "phasing": lambda: phasing_fixtures(), "sweep": lambda: sweep_fixture(),
+            "loop": lambda: loop_fixture()}
 
 
 def _cli():
