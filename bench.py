@@ -425,6 +425,7 @@ def gpu_arm(args):
             extras["tikhonov"] = tikhonov_bench(torch, args)
             extras["batch"] = batch_bench(torch, args)
             extras["phase"] = phase_bench(torch, args)
+            extras["loop"] = loop_bench(torch, args)
         out["extras"] = extras
 
         # ---------------- end to end through the public API with host buffers
@@ -688,6 +689,113 @@ def align_bench(torch, nf, alm, args):
                                       "assigned_to_true_volume": float(np.mean(conf == 0)),
                                       "argmin_equal_to_single_volume_bf16": int(np.sum(info["index"] == idx["bf16"]["index"])),
                                       "volume_ties": info["volume_ties"]}
+    return res
+
+
+# ------------------------------------------------------------------ config 0: the MTIP loop and the lambda scan
+
+LOOP_CFG = dict(n_img=1000, P=128, M=81, n_ref=2000, cg_iterations=10, phase_rounds=10, generations=3, seed=7,
+                n_atoms=150, radius=12.0, n_lambdas=8)
+
+
+def loop_bench(torch, args):
+    """Config 0 through run_mtip (cmtip/reconstruct.py:29-96): 1000 images x 4 x 128^2 pixels
+    (6.6e7 points) of the 150-Gaussian particle, M = 81, not aligned (random generation-0
+    orientations), 2000 references at the 9 A limit, 10 CG iterations and 10 ER/HIO/shrink-
+    wrap rounds per generation, 3 generations.  Per-generation stage times (CUDA events), the
+    orientation error against the truth and the phased autocorrelation's error against the
+    true one.  Then the lambda scan (autocorrelation_mpi.py:99-190) of generation 1 with 8
+    lambdas: the 8 CG solves as branches of one graph against 8 single solves in a row."""
+    import cmtip_gb300.autocorrelation as acm
+    from cmtip_gb300 import alignment, geometry, phasing, reconstruct
+    cfg = dict(LOOP_CFG)
+    if args.small:
+        cfg.update(n_img=100, P=64, n_ref=500)
+    rng = np.random.default_rng(cfg["seed"])
+    M = cfg["M"]
+    rho = geometry.gaussian_particle(M, cfg["n_atoms"], cfg["radius"], rng)
+    ac_true = geometry.autocorrelation_of(rho)
+    ppr, rext = geometry.ewald_detector(cfg["P"])
+    rext /= 0.9
+    quats = geometry.random_quaternions(cfg["n_img"], rng).astype(np.float32)
+    intens = alignment.compute_slices(torch.from_numpy(quats), ppr, rext,
+                                      torch.from_numpy(ac_true.astype(np.float32)).cuda(), eps=1e-7)
+    intens = intens.reshape(cfg["n_img"], 1, -1)
+    data = {"pixel_position_reciprocal": ppr, "reciprocal_extent": rext, "intensities": intens,
+            "orientations": quats}
+    marks = []
+
+    def mark(g, ck):
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record()
+        marks.append((g, ev, {k: (ck[k].detach().cpu().numpy() if torch.is_tensor(ck[k]) else np.array(ck[k]))
+                              for k in ("orientations", "ac_phased") if ck.get(k) is not None}))
+
+    kw = dict(aligned=False, n_iterations=cfg["generations"], n_ref=cfg["n_ref"], cg_maxiter=cfg["cg_iterations"],
+              cg_rtol=0.0, phase_iterations=cfg["phase_rounds"], rng=np.random.default_rng(1), verbose=False)
+    np.random.seed(2)
+    reconstruct.run_mtip(data, M, **dict(kw, n_iterations=2))  # warm-up: plans, matchers, graphs
+    marks.clear()
+    torch.cuda.synchronize()
+    np.random.seed(2)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    t0 = time.perf_counter()
+    reconstruct.run_mtip(data, M, on_generation=mark, **kw)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    res = {"images": cfg["n_img"], "pixels_per_image": 4 * cfg["P"] ** 2, "M": M, "n_ref": cfg["n_ref"],
+           "cg_iterations": cfg["cg_iterations"], "phase_rounds": cfg["phase_rounds"], "generations": cfg["generations"],
+           "total_s": e0.elapsed_time(marks[-1][1]) / 1e3, "wall_s": wall, "per_generation": [],
+           "note": "three generations from random orientations: a timing of the loop's hand-offs, not a converged "
+                   "reconstruction (MTIP needs more generations to align)"}
+    prev = e0
+    cc = lambda a, b: float(np.corrcoef(np.ravel(a), np.ravel(b))[0, 1])  # the scale is not determined
+    for g, ev, ck in marks:
+        row = {"generation": g, "s": prev.elapsed_time(ev) / 1e3,
+               "ac_phased_cc_vs_true_ac": cc(ck["ac_phased"], ac_true)}
+        if g > 0:
+            # angle between matched and true orientations (q and -q are one rotation)
+            dots = np.abs(np.sum(ck["orientations"].astype(np.float64) * quats, axis=1)).clip(0, 1)
+            row["median_orientation_error_deg"] = float(np.degrees(2 * np.arccos(np.median(dots))))
+        res["per_generation"].append(row)
+        prev = ev
+    # the lambda scan of generation 1 (estimate = the phased autocorrelation of generation 0)
+    est = marks[0][2]["ac_phased"].astype(np.float32)
+    sweep_kw = dict(orientations=quats, n_lambdas=cfg["n_lambdas"], maxiter=100, rtol=1e-5, verbose=False,
+                    return_info=True)
+    acm.solve_ac_sweep(1, ppr, rext, intens, M, ac_estimate=est.copy(), **sweep_kw)  # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    _, info = acm.solve_ac_sweep(1, ppr, rext, intens, M, ac_estimate=est.copy(), **sweep_kw)
+    e1.record()
+    torch.cuda.synchronize()
+    t_sweep = e0.elapsed_time(e1) / 1e3
+    ws = acm._workspace(M, 32, acm.TOEPLITZ, acm.DEFAULT_EPS, torch.device("cuda", torch.cuda.current_device()))
+    solvers = ws.sweep_solvers(64, cfg["n_lambdas"])
+    x0 = torch.zeros(M ** 3, dtype=torch.float64, device="cuda")
+    ds = [s.matvec(torch.ones(M ** 3, dtype=torch.float64, device="cuda")) for s in solvers]
+    fixed = dict(maxiter=100, rtol=0.0)
+    acm.solve_many(solvers, ds, [x0.clone() for _ in solvers], **fixed)
+    torch.cuda.synchronize()
+    e0.record()
+    acm.solve_many(solvers, ds, [x0.clone() for _ in solvers], **fixed)
+    e1.record()
+    torch.cuda.synchronize()
+    t_graph = e0.elapsed_time(e1) / 1e3
+    e0.record()
+    for s, d in zip(solvers, ds):
+        s.solve(d, x0, **fixed)
+    e1.record()
+    torch.cuda.synchronize()
+    t_seq = e0.elapsed_time(e1) / 1e3
+    res["lambda_scan"] = {"n_lambdas": cfg["n_lambdas"], "s": t_sweep, "kept_rank": info["keep"],
+                          "iterations": info["iterations"], "cg": "FP64 (the reference's cg precision)",
+                          "solves_100it_one_graph_s": t_graph, "solves_100it_in_a_row_s": t_seq,
+                          "graph_speedup": t_seq / t_graph}
+    acm.clear_workspaces()
+    torch.cuda.empty_cache()
     return res
 
 
@@ -1050,6 +1158,7 @@ def _run():
     ap.add_argument("--batch", action="store_true", help="run only the batched-reconstructions leg and exit")
     ap.add_argument("--tikhonov", action="store_true", help="run only the weighted Tikhonov solve leg and exit")
     ap.add_argument("--phase", action="store_true", help="run only the phasing leg and exit")
+    ap.add_argument("--loop", action="store_true", help="run only the MTIP loop / lambda scan leg and exit")
     ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full"],
                     help="run one case of each hot kernel (for ncu captures) and exit")
     args = ap.parse_args()
@@ -1059,6 +1168,9 @@ def _run():
     if args.phase:
         import torch
         return {"phase": phase_bench(torch, args)}
+    if args.loop:
+        import torch
+        return {"loop": loop_bench(torch, args)}
     if args.tikhonov:
         import torch
         return {"tikhonov": tikhonov_bench(torch, args)}
@@ -1121,6 +1233,7 @@ def summarize(line):
            "align_bf16_img_per_s": g(ex, "align", "bf16", "img_per_s"),
            "align_speedup_vs_fp64_form": g(ex, "align", "speedup_bf16_vs_fp64_form"),
            "align_disagree_outside_fp32_ties": g(ex, "align", "bf16", "disagree_outside_fp32_ties"),
+           "loop_config0_s": g(ex, "loop", "total_s"), "lambda_scan_s": g(ex, "loop", "lambda_scan", "s"),
            "tikhonov_s": g(ex, "tikhonov", "solve_s"), "tikhonov_rel_l2_vs_fp64": g(ex, "tikhonov", "rel_l2_mixed_vs_fp64"),
            "cpu_baseline_s_per_cg_iteration": g(line, "cpu_baseline", "value"),
            "cpu_baseline_single_thread": g(line, "cpu_baseline", "single_thread", "value")}

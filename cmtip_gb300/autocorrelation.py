@@ -373,7 +373,7 @@ def solve_ac(generation, pixel_position_reciprocal, reciprocal_extent, slices_, 
 
 def solve_ac_sweep(generation, pixel_position_reciprocal, reciprocal_extent, slices_, M, orientations=None,
                    ac_estimate=None, use_gpu=True, use_recip_sym=True, *, n_lambdas=8, maxiter=100, rtol=1e-5,
-                   prec=32, cg_prec=None, eps=DEFAULT_EPS, return_info=False, rng=None, verbose=True):
+                   prec=32, cg_prec=64, eps=DEFAULT_EPS, return_info=False, rng=None, verbose=True):
     """The lambda scan of cmtip/autocorrelation/autocorrelation_mpi.py:99-190 (solve_ac_mpi)
     on one GPU: the n_lambdas ranks' solves share the points, the Toeplitz kernel and the
     type-1 of the data, and differ in (rlambda, flambda) (sweep_lambdas) and thus in
@@ -382,8 +382,12 @@ def solve_ac_sweep(generation, pixel_position_reciprocal, reciprocal_extent, sli
     maxiter 100, autocorrelation_mpi.py:142,153).  The kept solution follows the
     reference's rule (sweep_select) on v1 = ||x||, v2 = ||W x - d||.  Every rank here holds
     the whole image set (N = all data points, as one rank of the reference holding all
-    images).  Returns the kept float64 (M, M, M) autocorrelation; with ``return_info`` also
-    the lambdas, v1, v2, iteration counts, all solutions and the kept index."""
+    images).  The CG runs in double precision by default (``cg_prec=64``, the reference's
+    complex128 cg): the scan's largest flambda, 1e5 * 10^(n/2), puts W's condition beyond
+    what single-precision CG vectors resolve, and the L-curve pick then follows rounding
+    (``cg_prec=32`` is available for the small-flambda ranks' speed).  Returns the kept
+    float64 (M, M, M) autocorrelation; with ``return_info`` also the lambdas, v1, v2,
+    iteration counts, all solutions and the kept index."""
     if not use_recip_sym:
         raise NotImplementedError("the GPU solver implements the reference's use_recip_sym=True path")
     numpy_io = not torch.is_tensor(slices_)
@@ -417,7 +421,15 @@ def solve_ac_sweep(generation, pixel_position_reciprocal, reciprocal_extent, sli
         xs.append(x0.to(s.dtype).clone())
     its = solve_many(solvers, ds, xs, maxiter=maxiter, rtol=rtol)
     v1 = np.array([float(torch.linalg.norm(x.double())) for x in xs])
-    v2 = np.array([float(torch.linalg.norm(s.matvec(x).double() - d.double())) for s, x, d in zip(solvers, xs, ds)])
+    # v2 = ||W x - d|| in double precision, as the reference's complex128 W * ret - d: with
+    # flambda up to 1e5 * 10^(n/2) a single-precision matvec's rounding would swamp the residual
+    check = ws.cg_solver(64)
+    check.set_kernel(kern)
+    v2 = []
+    for x, rl, fl in zip(xs, rls, fls):
+        check.set_operator(sup, 1.0, rl, fl)
+        v2.append(float(torch.linalg.norm(check.matvec(x.double()) - (adb + rl * x0))))
+    v2 = np.array(v2)
     keep = sweep_select(generation, rls, v1, v2)
     ac = xs[keep].to(torch.float64).reshape((M,) * 3)
     if verbose:

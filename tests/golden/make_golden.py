@@ -17,7 +17,7 @@ pulls in h5py/mrcfile/skopi-GPU drivers); only the hot-path submodules are loade
 Outputs: small ``.npz`` files holding inputs and the reference's outputs.
 
 Run:  python tests/golden/make_golden.py --reference PATH [--only NAME ...]
-      (NAME: core, phasing; default: all)
+      (NAME: core, phasing, sweep, loop; default: all)
 """
 from __future__ import annotations
 
@@ -361,9 +361,15 @@ LOOP = dict(M=21, n_img=30, P=8, n_atoms=20, radius=4.0, seed=81, generations=3,
 
 
 def loop_fixture():
+    _loop_fixture(aligned=False, name="mtip_loop")
+    _loop_fixture(aligned=True, name="mtip_loop_aligned")
+
+
+def _loop_fixture(aligned, name):
     """8. the MTIP generation loop (reconstruct.py:29-96, run_mtip) on a small case, not
-    aligned: random generation-0 orientations (the skopi stub's seeded generator), then
-    matching against the reference's hard-coded 5000 references at its 9 A resolution limit.
+    aligned (random generation-0 orientations from the skopi stub's seeded generator, then
+    matching against the reference's hard-coded 5000 references at its 9 A resolution
+    limit) and aligned (the true orientations throughout).
     Two stand-ins: save_checkpoint (h5py / mrcfile) records each generation's checkpoint in
     memory, and phase() runs a short schedule (LOOP['phase']) -- ER / HIO from a random start
     are chaotic over the default 1300 iterations, so only short schedules can be compared."""
@@ -384,22 +390,34 @@ def loop_fixture():
                              for k, v in checkpoint.items()}
 
     rec.save_checkpoint = record
+    solves = []
+    ref_solve = rec.autocorrelation.solve_ac
+
+    def recording_solve(*args, **kwargs):  # the reference's solve_ac, unchanged; keeps its output
+        ac = ref_solve(*args, **kwargs)
+        solves.append(np.array(ac, copy=True))
+        return ac
+
+    rec.autocorrelation.solve_ac = recording_solve
     case = synthetic_case(M=LOOP["M"], n_img=LOOP["n_img"], P=LOOP["P"], n_atoms=LOOP["n_atoms"],
                           radius=LOOP["radius"], seed=LOOP["seed"])
     data = {"pixel_position_reciprocal": case["ppr"], "reciprocal_extent": case["rext"],
             "intensities": case["slices"], "orientations": case["quats"]}
     np.random.seed(LOOP["np_seed"])
-    rec.run_mtip(data, LOOP["M"], "unused", aligned=False, n_iterations=LOOP["generations"], use_gpu=False,
+    rec.run_mtip(data, LOOP["M"], "unused", aligned=aligned, n_iterations=LOOP["generations"], use_gpu=False,
                  checkpoint=rec.load_checkpoint())
     out = dict(ppr=case["ppr"], rext=case["rext"], slices=case["slices"], quats_true=case["quats"],
                ac_true=case["ac"], M=LOOP["M"], np_seed=LOOP["np_seed"], stub_seed=1234,
                generations=LOOP["generations"], **{"phase_" + k: v for k, v in LOOP["phase"].items()})
+    rec.autocorrelation.solve_ac = ref_solve
+    out["g0_ac"] = solves[0]
+    out["aligned"] = aligned
     for g, ck in saved.items():
         for k in ("orientations", "ac", "ac_phased", "support_", "rho_"):
             if ck.get(k) is not None:
                 out[f"g{g}_{k}"] = ck[k]
-    np.savez_compressed(os.path.join(HERE, "mtip_loop.npz"), **out)
-    print("mtip_loop", sorted(k for k in out if k.startswith("g")))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, sorted(k for k in out if k.startswith("g")))
 
 
 FIXTURES = {"core": lambda: main(), "phasing": lambda: phasing_fixtures(), "sweep": lambda: sweep_fixture(),

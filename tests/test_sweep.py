@@ -56,24 +56,28 @@ def test_sweep_fp64_matches_reference(sweep, gen):
                                   verbose=False)
     assert info["keep"] == int(sweep[f"g{gen}_keep"])
     assert np.array_equal(info["rlambdas"], sweep[f"g{gen}_rlambdas"])
-    # scipy's stopping test on each rank's own system: the same iteration counts (one apart
-    # at most where a rank's residual crosses rtol ||b|| within rounding)
-    assert np.max(np.abs(np.array(info["iterations"]) - sweep[f"g{gen}_iterations"])) <= 1
-    for r in range(size):
-        assert rel_l2(info["solutions"][r].cpu().numpy(), sweep[f"g{gen}_solutions"][r]) < 1e-4, r
+    # scipy's stopping test on each rank's own system: where the residual flattens near
+    # rtol ||b|| (generation 1, ~80 iterations) the reference's single-precision rounding of
+    # its type-1 outputs moves the stopping iteration by a few
+    its, ref_its = np.array(info["iterations"]), sweep[f"g{gen}_iterations"]
+    assert np.all(np.abs(its - ref_its) <= np.maximum(1, 0.05 * ref_its)), (its, ref_its)
+    errs = [rel_l2(info["solutions"][r].cpu().numpy(), sweep[f"g{gen}_solutions"][r]) for r in range(size)]
+    assert max(errs) < 1e-4, errs
     assert rel_l2(info["v1"], sweep[f"g{gen}_v1"]) < 1e-5
     assert ac.dtype == np.float64 and rel_l2(ac, sweep[f"g{gen}_ac"]) < 1e-4
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("gen", [0, 1])
-def test_sweep_mixed_keeps_reference_rank(sweep, gen):
+@pytest.mark.parametrize("gen,cg_prec", [(0, 64), (1, 64), (0, 32)])
+def test_sweep_fp32_nufft_keeps_reference_rank(sweep, gen, cg_prec):
+    # FP32 NUFFT with the default FP64 CG (and, in generation 0, whose flambdas stay small
+    # enough for it, FP32 CG vectors)
     import cmtip_gb300.autocorrelation as acm
     M, size = int(sweep["M"]), int(sweep["size"])
     est = None if gen == 0 else sweep["estimate"].copy()
     ac, info = acm.solve_ac_sweep(gen, sweep["ppr"], sweep["rext"], sweep["slices"], M, orientations=sweep["quats"],
-                                  ac_estimate=est, n_lambdas=size, prec=32, eps=1e-6, return_info=True,
-                                  verbose=False)
+                                  ac_estimate=est, n_lambdas=size, prec=32, cg_prec=cg_prec, eps=1e-6,
+                                  return_info=True, verbose=False)
     assert info["keep"] == int(sweep[f"g{gen}_keep"])
     assert rel_l2(ac, sweep[f"g{gen}_ac"]) < 2e-4
 
