@@ -1006,6 +1006,11 @@ def batch_bench(torch, args):
     tot_s = st["slices_s"] + st["match_slices_s"] + st["match_gemm_s"] + st["solve_s"]
     res["aggregate_pts_per_s"] = tot_pts / tot_s
     res["total_s"] = tot_s
+    res["alone"] = batch_alone(torch, inst, acs_d, cfg)
+    res["alone"]["batch_speedup"] = {k: res["alone"][k + "_s"] / v for k, v in
+                                     (("slices", st["slices_s"]), ("match", st["match_slices_s"] + st["match_gemm_s"]),
+                                      ("solve", st["solve_s"]))}
+    res["alone"]["batch_speedup"]["total"] = res["alone"]["total_s"] / tot_s
     # errors against the FP64 forms
     errs = []
     order = np.argsort([x.orientations.shape[0] * x.n_pix for x in inst])
@@ -1071,6 +1076,47 @@ def batch_bench(torch, args):
     acm.clear_workspaces()
     torch.cuda.empty_cache()
     return res
+
+
+def batch_alone(torch, inst, acs_d, cfg):
+    """The batch's three stages with each instance run alone through the single-instance API
+    (compute_slices, match_orientations, solve_ac with the same iteration count), after one
+    untimed pass over all instances; CUDA-event time summed over the instances."""
+    import cmtip_gb300.alignment as alm
+    import cmtip_gb300.autocorrelation as acm
+
+    def stage(fn):
+        fn()  # warm-up pass
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    def slices():
+        for x, ac in zip(inst, acs_d):
+            alm.compute_slices(x.orientations, x.ppr.numpy(), x.rext, ac, eps=cfg["eps"])
+
+    def match():
+        for x, ac in zip(inst, acs_d):
+            alm.match_orientations(0, x.ppr.numpy().reshape(3, 1, -1), x.rext, x.images.reshape(-1, 1, x.n_pix), ac,
+                                   cfg["n_ref"], mode="bf16", eps=cfg["eps"])
+
+    def solve():
+        for x in inst:
+            acm.solve_ac(0, x.ppr.numpy().reshape(3, 1, -1), x.rext, x.images.reshape(-1, 1, x.n_pix), x.M,
+                         orientations=x.orientations, maxiter=cfg["cg_iterations"], rtol=0.0, eps=cfg["eps"],
+                         verbose=False)
+
+    out = {"slices_s": stage(slices), "match_s": stage(match), "solve_s": stage(solve)}
+    out["total_s"] = out["slices_s"] + out["match_s"] + out["solve_s"]
+    out["note"] = ("each instance through the single-instance API after a warm-up pass (solve_ac keeps 4 workspaces, "
+                   "so instances of other M re-create theirs)")
+    acm.clear_workspaces()
+    torch.cuda.empty_cache()
+    return out
 
 
 # ------------------------------------------------------------------ small kernel cases (profiling)
@@ -1233,6 +1279,8 @@ def summarize(line):
            "align_bf16_img_per_s": g(ex, "align", "bf16", "img_per_s"),
            "align_speedup_vs_fp64_form": g(ex, "align", "speedup_bf16_vs_fp64_form"),
            "align_disagree_outside_fp32_ties": g(ex, "align", "bf16", "disagree_outside_fp32_ties"),
+           "batch_total_s": g(ex, "batch", "total_s"),
+           "batch_speedup_vs_alone": g(ex, "batch", "alone", "batch_speedup"),
            "loop_config0_s": g(ex, "loop", "total_s"), "lambda_scan_s": g(ex, "loop", "lambda_scan", "s"),
            "tikhonov_s": g(ex, "tikhonov", "solve_s"), "tikhonov_rel_l2_vs_fp64": g(ex, "tikhonov", "rel_l2_mixed_vs_fp64"),
            "cpu_baseline_s_per_cg_iteration": g(line, "cpu_baseline", "value"),

@@ -92,6 +92,24 @@ class Matcher:
         _lib.call("cmt_match_run", self._h, _ptr(idx), _ptr(d1), _ptr(d2), _ptr(tie), ctypes.byref(nn))
         return idx, d1, d2, tie, nn.value
 
+    @staticmethod
+    def run_many(matchers):
+        """The tensor-core runs of several matchers (one instance each, modes bf16 / bf16x3) as
+        one persistent launch (``cmt_match_run_many``) and one host synchronisation: a list of
+        (best index, best distance, second distance, near-tie flags, near-tie count)."""
+        n = len(matchers)
+        outs = []
+        for m in matchers:
+            k = m.n_img
+            outs.append((torch.empty(k, dtype=torch.int32, device="cuda"), torch.empty(k, dtype=torch.float64, device="cuda"),
+                         torch.empty(k, dtype=torch.float64, device="cuda"), torch.empty(k, dtype=torch.int32, device="cuda")))
+        arr = lambda xs: (ctypes.c_void_p * n)(*xs)
+        nn = (ctypes.c_int * n)()
+        _lib.call("cmt_match_run_many", n, arr([m._h.value for m in matchers]), arr([o[0].data_ptr() for o in outs]),
+                  arr([o[1].data_ptr() for o in outs]), arr([o[2].data_ptr() for o in outs]),
+                  arr([o[3].data_ptr() for o in outs]), nn)
+        return [o + (int(nn[i]),) for i, o in enumerate(outs)]
+
     def stats(self):
         out = (ctypes.c_double * (self.nbatches + 1))()
         _lib.call("cmt_match_stats", self._h, out)

@@ -139,12 +139,14 @@ class BatchedReconstruction:
       orientations (align.py:39-65), one batched type-2 launch;
     * ``match(acs, n_ref)``: orientation matching of every instance's images against n_ref
       reference orientations (align.py:68-132): the references' slices of a group of
-      instances in one batched launch (groups bounded by ``max_points``), then each
-      instance's tensor-core distance GEMM and exact re-scoring;
+      instances in one batched launch (groups bounded by ``max_points``), then one
+      persistent tensor-core distance launch over the group's instances and each
+      instance's exact re-scoring;
     * ``solve(maxiter, estimates)``: every instance's autocorrelation solve
       (autocorrelation.py:176-248 with a fixed iteration count): the Toeplitz kernels (unit
       strengths onto 2M modes) in one batched launch, the right-hand sides (data onto M
-      modes) in another, then each instance's graph-captured CG.
+      modes) in another, then every instance's CG iterations as the branches of one
+      captured graph (``solve_many``).
 
     ``tuning``: None (defaults), "auto" (``tune.autotune`` per instance and transform), or a
     list of dicts (bin_size, maxsub) per instance.
@@ -157,10 +159,16 @@ class BatchedReconstruction:
         self.max_points = int(max_points)
         self.stream = stream
         self.stats = {}
+        self._matchers = {}  # (instance, mode) -> Matcher, operand buffers kept across calls
+        self._weights = {}
 
     # ---------------------------------------------------------------- helpers
     def _tuned(self, plan, i, kind, set_points, data):
         if self.tuning is None:
+            if kind == "solve" and self.prec == 32:
+                # solve_ac's Toeplitz workspace tuning: bins of 5 fine cells, 16384 points per
+                # subproblem (the derived 2M plan then fits four CTAs per SM)
+                return plan.set_tuning(5, 16384)
             return plan
         if self.tuning == "auto":
             from . import tune
@@ -215,10 +223,22 @@ class BatchedReconstruction:
         quats = orientations if orientations is not None else [x.orientations for x in self.inst]
         return self._slice_group(list(range(len(self.inst))), acs, quats, "slices_s")
 
+    def _matcher(self, i, mode):
+        from .alignment import Matcher, generate_weights
+        key = (i, mode)
+        if key not in self._matchers:
+            x = self.inst[i]
+            self._matchers[key] = Matcher(x.n_pix, mode)
+            self._weights[i] = generate_weights(x.ppr.cpu().numpy().reshape(3, 1, -1), order=0)
+        return self._matchers[key]
+
     def match(self, acs, n_ref, mode="bf16", ref_orientations=None):
         """Best reference orientation of every image of every instance: list of
-        (quaternions (n_img, 4) float32 numpy, info dict)."""
-        from .alignment import Matcher, generate_weights, reference_orientations
+        (quaternions (n_img, 4) float32 numpy, info dict).  Per group of instances: the
+        references' slices in one batched interpolation launch, every instance's operands,
+        then (tensor-core forms) ONE persistent distance launch over all the group's
+        instances and one host synchronisation."""
+        from .alignment import Matcher, reference_orientations
         refs = reference_orientations(n_ref, ref_orientations=ref_orientations)  # float32, as match_orientations
         results = [None] * len(self.inst)
         groups, cur, pts = [], [], 0
@@ -231,29 +251,32 @@ class BatchedReconstruction:
             pts += n
         if cur:
             groups.append(cur)
+        grouped = mode in ("bf16", "bf16x3")
         for g in groups:
+            matchers = [self._matcher(i, mode) for i in g]
             models = self._slice_group(g, [acs[i] for i in g], [refs] * len(g), "match_slices_s")
 
-            def run(models=models, g=g):
+            def run(models=models, g=g, matchers=matchers):
                 for k, i in enumerate(g):
                     x = self.inst[i]
-                    mt = Matcher(x.n_pix, mode)
-                    w = generate_weights(x.ppr.cpu().numpy().reshape(3, 1, -1), order=0)
-                    mt.set_data(torch.as_tensor(x.images).cuda().reshape(-1, x.n_pix), w)
-                    mt.set_refs(models[k].reshape(len(refs), x.n_pix))
-                    idx, d1, d2, tie, n_near = mt.run()
-                    index = idx.cpu().numpy().astype(np.int64)
-                    results[i] = (refs[index], dict(index=index, best=d1.cpu().numpy(), second=d2.cpu().numpy(),
-                                                    near_ties=int(n_near), refs=refs))
-                    mt.close()
-            self._timed("match_gemm_s", run)
+                    matchers[k].set_data(torch.as_tensor(x.images).cuda().reshape(-1, x.n_pix), self._weights[i])
+                    matchers[k].set_refs(models[k].reshape(len(refs), x.n_pix))
+                if grouped:
+                    return Matcher.run_many(matchers)
+                return [mt.run() for mt in matchers]
+            outs = self._timed("match_gemm_s", run)
+            for k, i in enumerate(g):
+                idx, d1, d2, tie, n_near = outs[k]
+                index = idx.cpu().numpy().astype(np.int64)
+                results[i] = (refs[index], dict(index=index, best=d1.cpu().numpy(), second=d2.cpu().numpy(),
+                                                near_ties=int(n_near), refs=refs))
             del models
         return results
 
     def solve(self, maxiter=20, estimates=None, rtol=0.0, data=None, orientations=None):
         """Every instance's autocorrelation solve (solve_ac with a fixed iteration count and
         the instances' known orientations); list of float64 (M, M, M) tensors."""
-        from .autocorrelation import TOEPLITZ, CGSolver, support_from_estimate, toeplitz_kernel
+        from .autocorrelation import TOEPLITZ, CGSolver, solve_many, support_from_estimate
         from .nufft import inverse_rotations
         K = len(self.inst)
         rt = torch.float64 if self.prec == 64 else torch.float32
@@ -290,16 +313,17 @@ class BatchedReconstruction:
                                  scale=[1.0 / float(2 * x.M) ** 3 for x in self.inst])
             bM = Batch(plans_M, stream=self.stream)
             adbs = bM.execute(datas, real_out=True, support=sups, scale=[1.0 / float(x.M) ** 3 for x in self.inst])
-            outs = []
+            ds, xs = [], []
             for i in range(K):
                 solvers[i].set_operator(sups[i], 1.0, rl[i], 1e3)
                 solvers[i].set_kernel(kernels[i])
-                d = adbs[i].reshape(-1).to(torch.float64) + rl[i] * x0s[i]
-                xsol, _ = solvers[i].solve(d, x0s[i], maxiter=maxiter, rtol=rtol)
-                outs.append(xsol.to(torch.float64).reshape((self.inst[i].M,) * 3))
+                ds.append((adbs[i].reshape(-1).to(torch.float64) + rl[i] * x0s[i]).to(solvers[i].dtype).contiguous())
+                xs.append(x0s[i].to(solvers[i].dtype).clone())
+            # every instance's CG iterations as branches of one captured graph
+            solve_many(solvers, ds, xs, maxiter=maxiter, rtol=rtol)
             b2.close()
             bM.close()
-            return outs
+            return [x.to(torch.float64).reshape((inst.M,) * 3) for x, inst in zip(xs, self.inst)]
         out = self._timed("solve_s", run)
         self.stats["solve_points"] = 2 * sum(p.N for p in plans_M)
         for s in solvers:

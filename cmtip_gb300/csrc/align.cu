@@ -407,19 +407,40 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32])
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-struct TcWork {
-    int n_img, n_ref, Kp;
-    int n_itiles, n_rtiles;
-    long long units;
-    int maxseg;
+// One distance problem of a launch: its image-major (image tile, reference tile) units are
+// [ustart, ustart + n_itiles * n_rtiles) of the launch's unit list.
+struct TcProblem {
+    long long ustart;
+    int n_rtiles;
+    int KB;      // K blocks of TC_BK per unit (padded pixels x terms / TC_BK)
+    int maxseg;  // most image tiles of this problem one CTA touches (output segments per CTA)
+    const float *ca, *cb;
+    float *pscore;  // [cta][segment][row][TOPK]
+    int *pidx;
 };
 
-// Persistent: CTA c owns the units [c U / G, (c+1) U / G) of the image-major (image tile,
-// reference tile) list, keeps each image's running top-k across the reference tiles in the
-// epilogue threads' registers and writes it once per image tile it touched.
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    k_dist_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcWork wk,
-              const float *ca, const float *cb, float *pscore, int *pidx, int *err)
+constexpr int TC_MAXP = 16;  // problems per launch
+
+struct TcGroup {
+    CUtensorMap tmA[TC_MAXP], tmB[TC_MAXP];
+    TcProblem p[TC_MAXP];
+    int np;
+    const long long *cta_u;  // CTA c owns units [cta_u[c], cta_u[c + 1])
+};
+
+// advance p to the problem holding unit u (units are visited in increasing order)
+__device__ __forceinline__ int problem_of(const TcGroup &g, long long u, int p)
+{
+    while (p + 1 < g.np && u >= g.p[p + 1].ustart) ++p;
+    return p;
+}
+
+// Persistent over the units of one or more problems (an instance each: its own images,
+// references, pixel count, score coefficients and outputs): CTA c owns a contiguous range
+// of the concatenated unit list, balanced by cost on the host, keeps each image's running
+// top-k across the reference tiles in the epilogue threads' registers and writes it once
+// per image tile it touched.
+__global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant__ TcGroup g, int *err)
 {
     extern __shared__ unsigned char smem_raw[];
     uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -436,10 +457,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long U = wk.units;
-    const long long G = gridDim.x;
-    const long long u0 = (long long)blockIdx.x * U / G, u1 = (long long)(blockIdx.x + 1) * U / G;
-    const int KB = wk.Kp / TC_BK;
+    const long long u0 = g.cta_u[blockIdx.x], u1 = g.cta_u[blockIdx.x + 1];
     if (u0 >= u1) return;
 
     if (threadIdx.x == 0) {
@@ -470,16 +488,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             int s = 0;
             uint32_t ph = 0;
             bool ok = true;
+            int p = 0;
             for (long long u = u0; u < u1 && ok; ++u) {
-                int m = (int)(u / wk.n_rtiles), t = (int)(u % wk.n_rtiles);
+                p = problem_of(g, u, p);
+                const long long lu = u - g.p[p].ustart;
+                const int m = (int)(lu / g.p[p].n_rtiles), t = (int)(lu % g.p[p].n_rtiles);
+                const int KB = g.p[p].KB;
                 for (int kb = 0; kb < KB; ++kb) {
                     if (!mbar_wait(empty_b(s), ph ^ 1, abort_flag)) {
                         ok = false;
                         break;
                     }
                     mbar_expect_tx(full_b(s), TC_STAGE_BYTES);
-                    tma_load_2d(sA0 + s * TC_A_BYTES, &tmA, full_b(s), kb * TC_BK, m * TC_BM);
-                    tma_load_2d(sB0 + s * TC_B_BYTES, &tmB, full_b(s), kb * TC_BK, t * TC_BN);
+                    tma_load_2d(sA0 + s * TC_A_BYTES, &g.tmA[p], full_b(s), kb * TC_BK, m * TC_BM);
+                    tma_load_2d(sB0 + s * TC_B_BYTES, &g.tmB[p], full_b(s), kb * TC_BK, t * TC_BN);
                     if (++s == TC_STAGES) {
                         s = 0;
                         ph ^= 1;
@@ -494,8 +516,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             int s = 0;
             uint32_t ph = 0;
             bool ok = true;
-            int lt = 0;
+            int lt = 0, p = 0;
             for (long long u = u0; u < u1 && ok; ++u, ++lt) {
+                p = problem_of(g, u, p);
+                const int KB = g.p[p].KB;
                 int b = lt & 1;
                 if (!mbar_wait(acce_b(b), ((lt >> 1) & 1) ^ 1, abort_flag)) {
                     ok = false;
@@ -535,25 +559,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             id[k] = -1;
         }
         int lt = 0;
-        int cur_m = (int)(u0 / wk.n_rtiles);
-        const int m_first = cur_m;
+        int cur_p = problem_of(g, u0, 0);
+        // the first image tile of problem p this CTA touches
+        auto first_tile = [&](int p) {
+            const long long ub = u0 > g.p[p].ustart ? u0 : g.p[p].ustart;
+            return (int)((ub - g.p[p].ustart) / g.p[p].n_rtiles);
+        };
+        int cur_m = first_tile(cur_p), m_first = cur_m;
         bool ok = true;
-        auto flush = [&](int m) {
-            long long o = (((long long)blockIdx.x * wk.maxseg + (m - m_first)) * TC_BM + row) * TOPK;
+        auto flush = [&](int p, int m) {
+            const TcProblem &pr = g.p[p];
+            long long o = (((long long)blockIdx.x * pr.maxseg + (m - m_first)) * TC_BM + row) * TOPK;
 #pragma unroll
             for (int k = 0; k < TOPK; ++k) {
-                pscore[o + k] = s[k];
-                pidx[o + k] = id[k];
+                pr.pscore[o + k] = s[k];
+                pr.pidx[o + k] = id[k];
                 s[k] = SCORE_INF;
                 id[k] = -1;
             }
         };
         for (long long u = u0; u < u1; ++u, ++lt) {
-            int m = (int)(u / wk.n_rtiles), t = (int)(u % wk.n_rtiles);
-            if (m != cur_m) {
-                flush(cur_m);
+            const int p = problem_of(g, u, cur_p);
+            const long long lu = u - g.p[p].ustart;
+            const int m = (int)(lu / g.p[p].n_rtiles), t = (int)(lu % g.p[p].n_rtiles);
+            if (p != cur_p || m != cur_m) {
+                flush(cur_p, cur_m);
+                if (p != cur_p) m_first = first_tile(p);
+                cur_p = p;
                 cur_m = m;
             }
+            const float *ca = g.p[p].ca, *cb = g.p[p].cb;
             int b = lt & 1;
             if (!mbar_wait(accf_b(b), (lt >> 1) & 1, abort_flag)) {
                 ok = false;
@@ -577,7 +612,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(acce_b(b));
         }
-        if (ok) flush(cur_m);
+        if (ok) flush(cur_p, cur_m);
         else if (lane == 0) atomicOr(err, 1);
     }
     tc_fence_before();
@@ -600,8 +635,9 @@ struct SegInfo {
     int mode;       // 0: SIMT layout [ref tile][image]; 1: tcgen05 layout [cta][seg][row]
     int nseg;       // mode 0: reference tiles
     int nimg_pad;   // mode 0
-    long long units, G;
+    long long ustart, G;          // mode 1: the problem's first unit, CTAs of the launch
     int n_rtiles, maxseg;
+    const long long *cta_u;       // mode 1: CTA c owned units [cta_u[c], cta_u[c + 1])
 };
 
 // One warp per image.  T: type of the raw model / data values (float or double).
@@ -631,11 +667,11 @@ __global__ void k_merge_rescore(SegInfo si, const float *pscore, const int *pidx
         for (int t = lane; t < si.nseg; t += 32) take(((long long)t * si.nimg_pad + i) * TOPK);
     } else {
         int m = i / TC_BM, row = i % TC_BM;
-        long long ub = (long long)m * si.n_rtiles, ue = ub + si.n_rtiles;
+        long long ub = si.ustart + (long long)m * si.n_rtiles, ue = ub + si.n_rtiles;
         for (long long c = lane; c < si.G; c += 32) {
-            long long c0 = c * si.units / si.G, c1 = (c + 1) * si.units / si.G;
+            long long c0 = si.cta_u[c], c1 = si.cta_u[c + 1];
             if (c0 >= c1 || c1 <= ub || c0 >= ue) continue;
-            int seg = m - (int)(c0 / si.n_rtiles);
+            int seg = m - (int)(((c0 > si.ustart ? c0 : si.ustart) - si.ustart) / si.n_rtiles);
             take(((c * si.maxseg + seg) * TC_BM + row) * TOPK);
         }
     }
@@ -758,6 +794,9 @@ struct Match {
     int *err = nullptr;
     int *near = nullptr;
     double *scratch_d = nullptr;
+    long long *cta_u = nullptr;  // CTA unit ranges of the last tensor-core launch (num_sms + 1)
+    int64_t cap_img = 0;         // bytes of dsum / dsq
+    int64_t cap_ref = 0;         // references of msum .. cb
 };
 
 }  // namespace cmt
@@ -842,6 +881,111 @@ static void row_stats(const Match &m, const void *v, int64_t rows, double *rsum,
         k_row_stats<float><<<(unsigned)rows, 256, 0, m.stream>>>((const float *)v, m.n_pix, rsum, rsq);
 }
 
+// One tensor-core launch over the matchers ms[0 .. n) (modes 0 / 3, n <= TC_MAXP), on the
+// stream st: each matcher's (image tile, reference tile) units are concatenated and split
+// over min(units, SMs) persistent CTAs in contiguous ranges of about equal cost (a unit
+// costs its K blocks plus a constant for the epilogue), so instances of very different
+// size share the GPU in one launch.  si[i] receives matcher i's segment layout for
+// k_merge_rescore; the CTA ranges live in ms[0]->cta_u until its next launch.
+static int tc_launch(int n, cmt_match *const *ms, cudaStream_t st, SegInfo *si)
+{
+    std::vector<long long> ustart(n + 1, 0), unit_cost(n);
+    std::vector<int> n_rt(n), n_it(n), KB(n);
+    long long cost_total = 0;
+    for (int i = 0; i < n; ++i) {
+        const Match &m = *ms[i];
+        n_it[i] = (int)((m.n_img + TC_BM - 1) / TC_BM);
+        n_rt[i] = (int)(m.n_ref_pad / TC_BN);
+        KB[i] = (int)((int64_t)m.Kp * m.terms / TC_BK);
+        unit_cost[i] = KB[i] + 16;
+        const long long U = (long long)n_it[i] * n_rt[i];
+        ustart[i + 1] = ustart[i] + U;
+        cost_total += U * unit_cost[i];
+    }
+    const long long U = ustart[n];
+    const long long G = std::min<long long>(U, ms[0]->num_sms);
+    // CTA c starts at the first unit whose preceding cost reaches c * cost_total / G
+    std::vector<long long> cta(G + 1);
+    {
+        int i = 0;
+        long long cum = 0;  // cost of the units of the problems before i
+        for (long long c = 0; c < G; ++c) {
+            const long long target = (long long)((__int128)c * cost_total / G);
+            while (i < n - 1 && cum + (ustart[i + 1] - ustart[i]) * unit_cost[i] <= target) {
+                cum += (ustart[i + 1] - ustart[i]) * unit_cost[i];
+                ++i;
+            }
+            long long u = ustart[i] + (target - cum + unit_cost[i] - 1) / unit_cost[i];
+            u = std::min(u, ustart[i + 1]);
+            cta[c] = std::max(u, c ? cta[c - 1] : 0LL);
+        }
+        cta[G] = U;
+    }
+    int64_t cap = 0;
+    if (!ms[0]->cta_u) {
+        CMT_TRY_CUDA(cudaMalloc(&ms[0]->cta_u, sizeof(long long) * (ms[0]->num_sms + 1)));
+    }
+    CMT_TRY_CUDA(cudaMemcpyAsync(ms[0]->cta_u, cta.data(), sizeof(long long) * (G + 1), cudaMemcpyHostToDevice, st));
+    TcGroup g;  // the parameter block (copied at launch)
+    memset(&g, 0, sizeof g);
+    g.np = n;
+    g.cta_u = ms[0]->cta_u;
+    for (int i = 0; i < n; ++i) {
+        Match &m = *ms[i];
+        int maxseg = 1;
+        for (long long c = 0; c < G; ++c) {
+            const long long a = std::max(cta[c], ustart[i]), b = std::min(cta[c + 1], ustart[i + 1]);
+            if (a < b) maxseg = std::max<int>(maxseg, (int)((b - 1 - ustart[i]) / n_rt[i] - (a - ustart[i]) / n_rt[i] + 1));
+        }
+        const int64_t need = G * maxseg * TC_BM * TOPK;
+        cap = m.cap_part;
+        CMT_TRY(ensure((void **)&m.pscore, cap, need * 4));
+        int64_t cap2 = m.cap_part;
+        CMT_TRY(ensure((void **)&m.pidx, cap2, need * 4));
+        m.cap_part = std::min(cap, cap2);
+        const int64_t kld = (int64_t)m.Kp * m.terms;
+        CMT_TRY(make_map(&g.tmA[i], m.opA, m.n_img, kld, TC_BM));
+        CMT_TRY(make_map(&g.tmB[i], m.opB, m.n_ref, kld, TC_BN));
+        g.p[i] = TcProblem{ustart[i], n_rt[i], KB[i], maxseg, m.ca, m.cb, m.pscore, m.pidx};
+        si[i] = SegInfo{};
+        si[i].mode = 1;
+        si[i].ustart = ustart[i];
+        si[i].G = G;
+        si[i].n_rtiles = n_rt[i];
+        si[i].maxseg = maxseg;
+        si[i].cta_u = ms[0]->cta_u;
+    }
+    CMT_TRY_CUDA(cudaFuncSetAttribute(k_dist_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    CMT_TRY_CUDA(cudaMemsetAsync(ms[0]->err, 0, sizeof(int), st));
+    k_dist_tc<<<(unsigned)G, TC_THREADS, TC_SMEM, st>>>(g, ms[0]->err);
+    CMT_LAUNCH_CHECK();
+    return CMT_OK;
+}
+
+static void merge(const Match &m, const SegInfo &si, cudaStream_t st, int *best_idx, double *best_d, double *second_d,
+                  int *near_tie)
+{
+    unsigned blocks = (unsigned)((m.n_img * 32 + 255) / 256);
+    if (m.mode == 2)
+        k_merge_rescore<double><<<blocks, 256, 0, st>>>(si, m.pscore, m.pidx, (int)m.n_img, (const double *)m.model,
+                                                        (const double *)m.data, m.w, m.wdf, m.sref, m.n_pix, best_idx,
+                                                        best_d, second_d, near_tie);
+    else
+        k_merge_rescore<float><<<blocks, 256, 0, st>>>(si, m.pscore, m.pidx, (int)m.n_img, (const float *)m.model,
+                                                       (const float *)m.data, m.w, m.wdf, m.sref, m.n_pix, best_idx,
+                                                       best_d, second_d, near_tie);
+}
+
+static int count_near(const Match &m, const int *near_tie, int *n_near)
+{
+    std::vector<int> h(m.n_img);
+    CMT_TRY_CUDA(cudaMemcpy(h.data(), near_tie, sizeof(int) * m.n_img, cudaMemcpyDeviceToHost));
+    int c = 0;
+    for (int v : h) c += v;
+    *n_near = c;
+    return CMT_OK;
+}
+
 }  // namespace cmt
 
 using namespace cmt;
@@ -885,10 +1029,11 @@ extern "C" int cmt_match_set_data(cmt_match *m, int64_t n_img, const void *data,
     int64_t cap = m->capA;
     CMT_TRY(ensure(&m->opA, cap, (int64_t)op_size(m->mode) * n_img * m->Kp * m->terms));
     m->capA = cap;
-    cudaFree(m->dsum);
-    cudaFree(m->dsq);
-    CMT_TRY_CUDA(cudaMalloc(&m->dsum, sizeof(double) * n_img));
-    CMT_TRY_CUDA(cudaMalloc(&m->dsq, sizeof(double) * n_img));
+    // per-image buffers are kept while large enough (a cudaFree would synchronise the device)
+    int64_t capd = m->cap_img, capq = m->cap_img;
+    CMT_TRY(ensure((void **)&m->dsum, capd, (int64_t)sizeof(double) * n_img));
+    CMT_TRY(ensure((void **)&m->dsq, capq, (int64_t)sizeof(double) * n_img));
+    m->cap_img = std::min(capd, capq);
     unsigned gp = (unsigned)ceil_div(m->n_pix, 256);
     if (m->mode == 2)
         k_col_mean<double><<<gp, 256, 0, m->stream>>>((const double *)data, m->w, n_img, m->n_pix, m->cen);
@@ -916,14 +1061,21 @@ extern "C" int cmt_match_set_refs(cmt_match *m, int64_t n_ref, const void *model
     int64_t cap = m->capB;
     CMT_TRY(ensure(&m->opB, cap, (int64_t)op_size(m->mode) * n_ref * m->Kp * m->terms));
     m->capB = cap;
-    void *bufs[] = {m->msum, m->msq, m->mnorm, m->sref, m->ca, m->cb};
-    for (void *b : bufs) cudaFree(b);
-    CMT_TRY_CUDA(cudaMalloc(&m->msum, sizeof(double) * n_ref));
-    CMT_TRY_CUDA(cudaMalloc(&m->msq, sizeof(double) * n_ref));
-    CMT_TRY_CUDA(cudaMalloc(&m->mnorm, sizeof(double) * n_ref));
-    CMT_TRY_CUDA(cudaMalloc(&m->sref, sizeof(double) * n_ref));
-    CMT_TRY_CUDA(cudaMalloc(&m->ca, sizeof(float) * m->n_ref_pad));
-    CMT_TRY_CUDA(cudaMalloc(&m->cb, sizeof(float) * m->n_ref_pad));
+    // per-reference buffers are kept while large enough (a cudaFree would synchronise the device)
+    if (m->n_ref_pad > m->cap_ref) {
+        void *bufs[] = {m->msum, m->msq, m->mnorm, m->sref, m->ca, m->cb};
+        for (void *b : bufs) cudaFree(b);
+        m->msum = m->msq = m->mnorm = m->sref = nullptr;
+        m->ca = m->cb = nullptr;
+        m->cap_ref = 0;
+        CMT_TRY_CUDA(cudaMalloc(&m->msum, sizeof(double) * m->n_ref_pad));
+        CMT_TRY_CUDA(cudaMalloc(&m->msq, sizeof(double) * m->n_ref_pad));
+        CMT_TRY_CUDA(cudaMalloc(&m->mnorm, sizeof(double) * m->n_ref_pad));
+        CMT_TRY_CUDA(cudaMalloc(&m->sref, sizeof(double) * m->n_ref_pad));
+        CMT_TRY_CUDA(cudaMalloc(&m->ca, sizeof(float) * m->n_ref_pad));
+        CMT_TRY_CUDA(cudaMalloc(&m->cb, sizeof(float) * m->n_ref_pad));
+        m->cap_ref = m->n_ref_pad;
+    }
     row_stats(*m, model, n_ref, m->msum, m->msq);
     k_batch_scales<<<1, 1024, 0, m->stream>>>(m->dsum, m->dsq, m->n_img, m->msum, m->msq, n_ref, nbatches, m->n_pix,
                                               m->sref, m->stats);
@@ -942,40 +1094,13 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
     CMT_CHECK_ARG(m->n_img > 0 && m->n_ref > 0, "set_data and set_refs first");
     cudaStream_t st = m->stream;
     SegInfo si{};
-    int64_t need;
     if (m->mode == 0 || m->mode == 3) {
-        int n_it = (int)((m->n_img + TC_BM - 1) / TC_BM), n_rt = (int)(m->n_ref_pad / TC_BN);
-        long long U = (long long)n_it * n_rt;
-        long long G = std::min<long long>(U, m->num_sms);
-        int maxseg = 1;
-        for (long long c = 0; c < G; ++c) {
-            long long c0 = c * U / G, c1 = (c + 1) * U / G;
-            if (c1 > c0) maxseg = std::max<int>(maxseg, (int)((c1 - 1) / n_rt - c0 / n_rt + 1));
-        }
-        need = G * maxseg * TC_BM * TOPK;
-        si.mode = 1;
-        si.units = U;
-        si.G = G;
-        si.n_rtiles = n_rt;
-        si.maxseg = maxseg;
-        int64_t cap = m->cap_part;
-        CMT_TRY(ensure((void **)&m->pscore, cap, need * 4));
-        int64_t cap2 = m->cap_part;
-        CMT_TRY(ensure((void **)&m->pidx, cap2, need * 4));
-        m->cap_part = std::min(cap, cap2);
-        CUtensorMap ta, tb;
-        int64_t kld = (int64_t)m->Kp * m->terms;
-        CMT_TRY(make_map(&ta, m->opA, m->n_img, kld, TC_BM));
-        CMT_TRY(make_map(&tb, m->opB, m->n_ref, kld, TC_BN));
-        TcWork wk{(int)m->n_img, (int)m->n_ref, (int)kld, n_it, n_rt, U, maxseg};
-        CMT_TRY_CUDA(cudaFuncSetAttribute(k_dist_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-        CMT_TRY_CUDA(cudaMemsetAsync(m->err, 0, sizeof(int), st));
-        k_dist_tc<<<(unsigned)G, TC_THREADS, TC_SMEM, st>>>(ta, tb, wk, m->ca, m->cb, m->pscore, m->pidx, m->err);
-        CMT_LAUNCH_CHECK();
+        cmt_match *one[1] = {m};
+        CMT_TRY(tc_launch(1, one, st, &si));
     } else {
         int n_it = (int)((m->n_img + 63) / 64), n_rt = (int)(m->n_ref_pad / 64);
         int nimg_pad = n_it * 64;
-        need = (int64_t)n_rt * nimg_pad * TOPK;
+        int64_t need = (int64_t)n_rt * nimg_pad * TOPK;
         si.mode = 0;
         si.nseg = n_rt;
         si.nimg_pad = nimg_pad;
@@ -994,15 +1119,7 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
                                                       nimg_pad);
         CMT_LAUNCH_CHECK();
     }
-    unsigned blocks = (unsigned)((m->n_img * 32 + 255) / 256);
-    if (m->mode == 2)
-        k_merge_rescore<double><<<blocks, 256, 0, st>>>(si, m->pscore, m->pidx, (int)m->n_img, (const double *)m->model,
-                                                        (const double *)m->data, m->w, m->wdf, m->sref, m->n_pix, best_idx,
-                                                        best_d, second_d, near_tie);
-    else
-        k_merge_rescore<float><<<blocks, 256, 0, st>>>(si, m->pscore, m->pidx, (int)m->n_img, (const float *)m->model,
-                                                       (const float *)m->data, m->w, m->wdf, m->sref, m->n_pix, best_idx,
-                                                       best_d, second_d, near_tie);
+    merge(*m, si, st, best_idx, best_d, second_d, near_tie);
     CMT_LAUNCH_CHECK();
     if (m->mode == 0 || m->mode == 3 || n_near_host) {
         int herr = 0;
@@ -1012,14 +1129,46 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
             set_error("tensor-core distance kernel: a bounded pipeline wait timed out");
             return CMT_ERR_TIMEOUT;
         }
-        if (n_near_host) {
-            std::vector<int> h(m->n_img);
-            CMT_TRY_CUDA(cudaMemcpy(h.data(), near_tie, sizeof(int) * m->n_img, cudaMemcpyDeviceToHost));
-            int c = 0;
-            for (int v : h) c += v;
-            *n_near_host = c;
-        }
+        if (n_near_host) CMT_TRY(count_near(*m, near_tie, n_near_host));
     }
+    return CMT_OK;
+}
+
+// The tensor-core runs of n matchers (modes 0 / 3, any sizes) in one launch per TC_MAXP
+// matchers, then each one's re-scoring, with one host synchronisation at the end; outputs
+// as for cmt_match_run, per matcher.  Runs on the stream of ms[0].
+extern "C" int cmt_match_run_many(int n, cmt_match *const *ms, int *const *best_idx, double *const *best_d,
+                                  double *const *second_d, int *const *near_tie, int *n_near_host)
+{
+    CMT_CHECK_ARG(n >= 1 && ms && best_idx && best_d && second_d && near_tie, "bad argument");
+    for (int i = 0; i < n; ++i) {
+        CMT_CHECK_ARG(ms[i] && best_idx[i] && best_d[i] && second_d[i] && near_tie[i], "null argument at %d", i);
+        CMT_CHECK_ARG(ms[i]->mode == 0 || ms[i]->mode == 3, "matcher %d is not a tensor-core form (mode 0 or 3)", i);
+        CMT_CHECK_ARG(ms[i]->n_img > 0 && ms[i]->n_ref > 0, "matcher %d: set_data and set_refs first", i);
+        for (int j = 0; j < i; ++j) CMT_CHECK_ARG(ms[j] != ms[i], "matcher %d given twice", i);
+    }
+    cudaStream_t st = ms[0]->stream;
+    std::vector<SegInfo> si(n);
+    std::vector<int> err_at;
+    for (int b = 0; b < n; b += TC_MAXP) {
+        const int k = std::min(TC_MAXP, n - b);
+        CMT_TRY(tc_launch(k, ms + b, st, si.data() + b));
+        // the CTA ranges in ms[b]->cta_u are read by these merges before the next launch
+        for (int i = b; i < b + k; ++i) merge(*ms[i], si[i], st, best_idx[i], best_d[i], second_d[i], near_tie[i]);
+        CMT_LAUNCH_CHECK();
+        err_at.push_back(b);
+    }
+    std::vector<int> herr(err_at.size(), 0);
+    for (size_t j = 0; j < err_at.size(); ++j)
+        CMT_TRY_CUDA(cudaMemcpyAsync(&herr[j], ms[err_at[j]]->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CMT_TRY_CUDA(cudaStreamSynchronize(st));
+    for (int e : herr)
+        if (e) {
+            set_error("tensor-core distance kernel: a bounded pipeline wait timed out");
+            return CMT_ERR_TIMEOUT;
+        }
+    if (n_near_host)
+        for (int i = 0; i < n; ++i) CMT_TRY(count_near(*ms[i], near_tie[i], n_near_host + i));
     return CMT_OK;
 }
 
@@ -1037,7 +1186,7 @@ extern "C" int cmt_match_destroy(cmt_match *m)
 {
     if (!m) return CMT_OK;
     void *bufs[] = {m->w, m->wdf, m->cen, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
-                    m->ca, m->cb, m->stats, m->pscore, m->pidx, m->err, m->near, m->scratch_d};
+                    m->ca, m->cb, m->stats, m->pscore, m->pidx, m->err, m->near, m->scratch_d, m->cta_u};
     for (void *b : bufs) cudaFree(b);
     delete m;
     return CMT_OK;

@@ -50,6 +50,7 @@ struct Cg {
     float *support = nullptr;  // M^3
     double *partial = nullptr;
     CgScalars *sc = nullptr;
+    CgScalars *host_sc = nullptr;  // pinned host copy of sc, read after a solve
     cufftHandle r2c_big = 0, c2r_big = 0, r2c_small = 0, c2r_small = 0;
     bool have_big = false, have_small = false;
     cmt_plan *pair_plan = nullptr;
@@ -237,6 +238,28 @@ __global__ void __launch_bounds__(RED_THREADS) k_update(CgScalars *sc, T *x, T *
     }
 }
 
+// Scalars at the start of a solve, on the device (no host round trip): ||b|| from the
+// b.b that k_dot left in sc->bnorm, the stopping threshold max(atol, rtol ||b||), and
+// done = 1 when ||b|| = 0 (scipy then returns b itself).
+__global__ void k_begin_scalars(CgScalars *sc, double rtol, double atol)
+{
+    const double bnorm = sqrt(sc->bnorm);
+    sc->bnorm = bnorm;
+    sc->atol = fmax(atol, rtol * bnorm);
+    sc->it = 0;
+    sc->done = bnorm == 0.0 ? 1 : 0;
+    sc->pq = 0.0;
+}
+
+// x = b where the solve is trivial (||b|| = 0)
+template <typename T>
+__global__ void k_copy_if_done(const CgScalars *sc, const T *b, T *x, int64_t n)
+{
+    if (!sc->done) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = b[i];
+}
+
 // r = b - q  (q = W x0)
 template <typename T>
 __global__ void k_residual(const T *b, const T *q, T *r, int64_t n)
@@ -389,6 +412,7 @@ static void cg_destroy(Cg *c)
     void *bufs[] = {c->x, c->r, c->p, c->q, c->b, c->sx, c->pad, c->conv, c->spec, c->spec2, c->reg,
                     c->kern_hat, c->mask_hat, c->support, c->partial, c->sc};
     for (void *b : bufs) cudaFree(b);
+    if (c->host_sc) cudaFreeHost(c->host_sc);
     if (c->have_big) {
         cufftDestroy(c->r2c_big);
         cufftDestroy(c->c2r_big);
@@ -466,16 +490,16 @@ static int capture_iteration(Cg &c)
     return CMT_OK;
 }
 
-// Start of a solve (scipy's cg before its loop): b = d, x = x0, ||b||, r0 = b - W x0 when x0
-// has a nonzero entry (else r0 = b), rho = r0.r0, stopping threshold max(atol, rtol ||b||).
-// *trivial: ||b|| = 0, where scipy returns b itself (already copied into x).
+// Start of a solve (scipy's cg before its loop), stream-ordered with no host round trip:
+// b = d, x = x0, ||b||, threshold max(atol, rtol ||b||), r0 = b - W x0, rho = r0.r0.  scipy
+// skips the matvec when x0 is all zeros; W 0 is exactly 0, so r0 = b either way.  When
+// ||b|| = 0 the done flag is set and x = b (scipy returns b itself).
 template <typename T>
-static int solve_begin(Cg &c, const T *d, T *x, double rtol, double atol, bool *trivial)
+static int solve_begin(Cg &c, const T *d, T *x, double rtol, double atol)
 {
     cudaStream_t st = c.stream;
     size_t bytes = sizeof(T) * c.m3;
     int g = grid_elems(c.m3);
-    *trivial = false;
     CMT_TRY_CUDA(cudaMemsetAsync(c.sc, 0, sizeof(CgScalars), st));
     CMT_TRY_CUDA(cudaMemcpyAsync(c.b, d, bytes, cudaMemcpyDeviceToDevice, st));
     CMT_TRY_CUDA(cudaMemcpyAsync(c.x, x, bytes, cudaMemcpyDeviceToDevice, st));
@@ -483,55 +507,33 @@ static int solve_begin(Cg &c, const T *d, T *x, double rtol, double atol, bool *
     k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.b, (const T *)c.b, c.m3, c.partial, &sc->ticket[2],
                                                  &sc->bnorm);
     CMT_LAUNCH_CHECK();
-    k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.x, (const T *)c.x, c.m3, c.partial, &sc->ticket[3],
-                                                 &sc->pq);
+    k_begin_scalars<<<1, 1, 0, st>>>(sc, rtol, atol);
     CMT_LAUNCH_CHECK();
-    CgScalars h;
-    CMT_TRY_CUDA(cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st));
-    CMT_TRY_CUDA(cudaStreamSynchronize(st));
-    const double xx_host = h.pq;
-    const double bnorm = sqrt(h.bnorm);
-    if (bnorm == 0.0) {  // scipy returns b itself
-        CMT_TRY_CUDA(cudaMemcpyAsync(x, c.b, bytes, cudaMemcpyDeviceToDevice, st));
-        *trivial = true;
-        return CMT_OK;
-    }
-    CgScalars init = h;
-    init.bnorm = bnorm;
-    init.atol = std::max(atol, rtol * bnorm);
-    init.it = 0;
-    init.done = 0;
-    init.pq = 0.0;
-    memset(init.ticket, 0, sizeof init.ticket);
-    CMT_TRY_CUDA(cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st));
-    CMT_TRY_CUDA(cudaStreamSynchronize(st));
-    if (xx_host != 0.0) {
-        CMT_TRY(matvec_impl<T>(c, (const T *)c.x, (T *)c.q, false));
-        k_residual<T><<<g, 256, 0, st>>>((const T *)c.b, (const T *)c.q, (T *)c.r, c.m3);
-        CMT_LAUNCH_CHECK();
-    } else {
-        CMT_TRY_CUDA(cudaMemcpyAsync(c.r, c.b, bytes, cudaMemcpyDeviceToDevice, st));
-    }
+    CMT_TRY(matvec_impl<T>(c, (const T *)c.x, (T *)c.q, false));
+    k_residual<T><<<g, 256, 0, st>>>((const T *)c.b, (const T *)c.q, (T *)c.r, c.m3);
+    CMT_LAUNCH_CHECK();
     k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.r, (const T *)c.r, c.m3, c.partial, &sc->ticket[2],
                                                  &sc->rho);
+    CMT_LAUNCH_CHECK();
+    k_copy_if_done<T><<<g, 256, 0, st>>>(sc, (const T *)c.b, (T *)c.x, c.m3);
     CMT_LAUNCH_CHECK();
     return CMT_OK;
 }
 
-// End of a solve: x out, iteration count and r.r (host, optional; synchronises).
+// End of a solve, stream-ordered: x out, and the scalars into the solver's pinned host copy
+// (read by solve_result once the stream has passed this point).
 template <typename T>
-static int solve_end(Cg &c, T *x, bool trivial, int *iters, double *final_rho)
+static int solve_end(Cg &c, T *x)
 {
-    cudaStream_t st = c.stream;
-    if (!trivial) CMT_TRY_CUDA(cudaMemcpyAsync(x, c.x, sizeof(T) * c.m3, cudaMemcpyDeviceToDevice, st));
-    if (iters || final_rho) {
-        CgScalars h;
-        CMT_TRY_CUDA(cudaMemcpyAsync(&h, c.sc, sizeof h, cudaMemcpyDeviceToHost, st));
-        CMT_TRY_CUDA(cudaStreamSynchronize(st));
-        if (iters) *iters = trivial ? 0 : h.it;
-        if (final_rho) *final_rho = trivial ? 0.0 : h.rho;
-    }
+    CMT_TRY_CUDA(cudaMemcpyAsync(x, c.x, sizeof(T) * c.m3, cudaMemcpyDeviceToDevice, c.stream));
+    CMT_TRY_CUDA(cudaMemcpyAsync(c.host_sc, c.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, c.stream));
     return CMT_OK;
+}
+
+static void solve_result(const Cg &c, int *iters, double *final_rho)
+{
+    if (iters) *iters = c.host_sc->it;
+    if (final_rho) *final_rho = c.host_sc->rho;
 }
 
 }  // namespace cmt
@@ -574,6 +576,14 @@ extern "C" int cmt_cg_create(int M, int prec, int op, void *stream, cmt_cg **out
             set_error("cg allocation of %zu bytes: %s", a.n, cudaGetErrorString(err));
             return fail(CMT_ERR_OOM);
         }
+    }
+    {
+        cudaError_t err = cudaMallocHost((void **)&c->host_sc, sizeof(CgScalars));
+        if (err != cudaSuccess) {
+            set_error("cg pinned scalars: %s", cudaGetErrorString(err));
+            return fail(CMT_ERR_OOM);
+        }
+        memset(c->host_sc, 0, sizeof(CgScalars));
     }
     if (op == 0) {
         struct A big[] = {{&c->pad, e * c->m2}, {&c->conv, e * c->m2}, {&c->spec, 2 * e * hbig}, {&c->kern_hat, 2 * e * hbig}};
@@ -681,17 +691,19 @@ template <typename T>
 static int solve_impl(Cg &c, const T *d, T *x, int maxiter, double rtol, double atol, int use_graph, int *iters,
                       double *final_rho)
 {
-    bool trivial = false;
-    CMT_TRY(solve_begin<T>(c, d, x, rtol, atol, &trivial));
-    if (!trivial) {
-        if (use_graph) {
-            if (!c.ready) CMT_TRY(capture_iteration<T>(c));
-            for (int it = 0; it < maxiter; ++it) CMT_TRY_CUDA(cudaGraphLaunch(c.graph, c.stream));
-        } else {
-            for (int it = 0; it < maxiter; ++it) CMT_TRY(iteration<T>(c));
-        }
+    CMT_TRY(solve_begin<T>(c, d, x, rtol, atol));
+    if (use_graph) {
+        if (!c.ready) CMT_TRY(capture_iteration<T>(c));
+        for (int it = 0; it < maxiter; ++it) CMT_TRY_CUDA(cudaGraphLaunch(c.graph, c.stream));
+    } else {
+        for (int it = 0; it < maxiter; ++it) CMT_TRY(iteration<T>(c));
     }
-    return solve_end<T>(c, x, trivial, iters, final_rho);
+    CMT_TRY(solve_end<T>(c, x));
+    if (iters || final_rho) {
+        CMT_TRY_CUDA(cudaStreamSynchronize(c.stream));
+        solve_result(c, iters, final_rho);
+    }
+    return CMT_OK;
 }
 
 // Several solvers at once: each one's iteration is captured as a child graph of one parent
@@ -704,7 +716,6 @@ static int solve_many_impl(int n, cmt_cg *const *cgs, const void *const *d, void
 {
     cudaStream_t st = cgs[0]->stream;
     std::vector<cudaStream_t> own(n);
-    std::vector<char> trivial(n, 0);
     for (int i = 0; i < n; ++i) {
         own[i] = cgs[i]->stream;
         CMT_TRY(route_to(*cgs[i], st));
@@ -713,11 +724,7 @@ static int solve_many_impl(int n, cmt_cg *const *cgs, const void *const *d, void
         for (int i = 0; i < n; ++i) route_to(*cgs[i], own[i]);
     };
     int rc = CMT_OK;
-    for (int i = 0; i < n && rc == CMT_OK; ++i) {
-        bool t = false;
-        rc = solve_begin<T>(*cgs[i], (const T *)d[i], (T *)x[i], rtol, atol, &t);
-        trivial[i] = t;
-    }
+    for (int i = 0; i < n && rc == CMT_OK; ++i) rc = solve_begin<T>(*cgs[i], (const T *)d[i], (T *)x[i], rtol, atol);
     cudaGraph_t parent = nullptr;
     cudaGraphExec_t exec = nullptr;
     if (rc == CMT_OK) {
@@ -728,7 +735,6 @@ static int solve_many_impl(int n, cmt_cg *const *cgs, const void *const *d, void
         }
     }
     for (int i = 0; i < n && rc == CMT_OK; ++i) {
-        if (trivial[i]) continue;
         cudaGraph_t child = nullptr;
         rc = capture_graph<T>(*cgs[i], &child);
         if (rc != CMT_OK) break;
@@ -754,9 +760,16 @@ static int solve_many_impl(int n, cmt_cg *const *cgs, const void *const *d, void
             rc = CMT_ERR_CUDA;
         }
     }
-    for (int i = 0; i < n && rc == CMT_OK; ++i)
-        rc = solve_end<T>(*cgs[i], (T *)x[i], trivial[i], iters ? iters + i : nullptr,
-                          final_rho ? final_rho + i : nullptr);
+    for (int i = 0; i < n && rc == CMT_OK; ++i) rc = solve_end<T>(*cgs[i], (T *)x[i]);
+    if (rc == CMT_OK && (iters || final_rho)) {
+        cudaError_t e = cudaStreamSynchronize(st);  // one host synchronisation for all solves
+        if (e != cudaSuccess) {
+            set_error("cudaStreamSynchronize: %s", cudaGetErrorString(e));
+            rc = CMT_ERR_CUDA;
+        }
+        for (int i = 0; i < n && rc == CMT_OK; ++i)
+            solve_result(*cgs[i], iters ? iters + i : nullptr, final_rho ? final_rho + i : nullptr);
+    }
     if (exec) cudaGraphExecDestroy(exec);
     if (parent) cudaGraphDestroy(parent);
     restore();

@@ -1698,8 +1698,11 @@ static int batch_execute(Batch &b, void *const *c, void *const *f, const float *
         CMT_TRY_CUDA(cudaMemsetAsync(b.next, 0, sizeof(int), b.stream));
         if (b.timed) CMT_TRY_CUDA(cudaEventRecord(b.ev0, b.stream));
         if (b.nwork > 0) {
+            // derived plans keep their extended register window when the whole batch is derived
+            bool ext = t1 && !cplx && p0.w <= 7;
+            for (int i = 0; i < K; ++i) ext = ext && b.plans[i]->spread_ext && b.plans[i]->spread_tab;
             if (t1)
-                CMT_TRY(launch_spread_batch(p0.prec, cplx, p0.w, b.work, b.nwork, b.inst, p0.beta, b.next, smem,
+                CMT_TRY(launch_spread_batch(p0.prec, cplx, ext, p0.w, b.work, b.nwork, b.inst, p0.beta, b.next, smem,
                                             b.stream));
             else
                 CMT_TRY(launch_interp_batch(p0.prec, cplx ? 0 : 2, p0.w, b.work, b.nwork, b.inst, p0.beta, b.next,

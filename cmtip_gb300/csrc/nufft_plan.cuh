@@ -121,8 +121,9 @@ struct InstDesc {
 
 // One persistent launch over the work list of a batch (all plans of one precision and
 // kernel width 2..8); smem = the largest plan's shared-memory need (batch_smem).
-int launch_spread_batch(int prec, bool cplx, int w, const WorkItem *work, int nwork, const void *inst, double beta,
-                        int *next, size_t smem, cudaStream_t st);
+// ext: every plan of the batch is derived and spreads through the extended register window.
+int launch_spread_batch(int prec, bool cplx, bool ext, int w, const WorkItem *work, int nwork, const void *inst,
+                        double beta, int *next, size_t smem, cudaStream_t st);
 int launch_interp_batch(int prec, int out_mode, int w, const WorkItem *work, int nwork, const void *inst,
                         double beta, int *next, size_t smem, cudaStream_t st);
 size_t batch_smem(const Plan &p, bool spread, bool cplx);

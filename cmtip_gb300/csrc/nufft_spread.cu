@@ -80,27 +80,28 @@ int dispatch(Plan &p, const void *c, bool cplx, int rs)
 template <typename T, bool CPLX>
 using BatchFn = void (*)(const WorkItem *, int, const InstDesc<T> *, T, int *);
 
-template <typename T, bool CPLX>
+template <typename T, bool CPLX, bool EXT>
 BatchFn<T, CPLX> pick_batch(int w)
 {
     switch (w) {
-    case 2: return k_spread_tab_batch<T, CPLX, 2>;
-    case 3: return k_spread_tab_batch<T, CPLX, 3>;
-    case 4: return k_spread_tab_batch<T, CPLX, 4>;
-    case 5: return k_spread_tab_batch<T, CPLX, 5>;
-    case 6: return k_spread_tab_batch<T, CPLX, 6>;
-    case 7: return k_spread_tab_batch<T, CPLX, 7>;
-    case 8: return k_spread_tab_batch<T, CPLX, 8>;
+    case 2: return k_spread_tab_batch<T, CPLX, 2, EXT>;
+    case 3: return k_spread_tab_batch<T, CPLX, 3, EXT>;
+    case 4: return k_spread_tab_batch<T, CPLX, 4, EXT>;
+    case 5: return k_spread_tab_batch<T, CPLX, 5, EXT>;
+    case 6: return k_spread_tab_batch<T, CPLX, 6, EXT>;
+    case 7: return k_spread_tab_batch<T, CPLX, 7, EXT>;
+    case 8: if constexpr (!EXT) return k_spread_tab_batch<T, CPLX, 8, false>;
+    [[fallthrough]];
     default: return nullptr;
     }
 }
 
-template <typename T, bool CPLX>
+template <typename T, bool CPLX, bool EXT>
 int run_batch(int w, const WorkItem *work, int nwork, const void *inst, double beta, int *next, size_t smem,
               cudaStream_t st)
 {
-    BatchFn<T, CPLX> k = pick_batch<T, CPLX>(w);
-    CMT_CHECK_ARG(k, "batched spreading needs a kernel width in 2..8 (got %d)", w);
+    BatchFn<T, CPLX> k = pick_batch<T, CPLX, EXT>(w);
+    CMT_CHECK_ARG(k, "batched spreading needs a kernel width in 2..8 (2..7 on derived plans; got %d)", w);
     CMT_TRY(prep_smem(k, (int)smem));
     int per_sm = 0, dev = 0, sms = 0;
     CMT_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem));
@@ -115,14 +116,17 @@ int run_batch(int w, const WorkItem *work, int nwork, const void *inst, double b
 
 }  // namespace
 
-int launch_spread_batch(int prec, bool cplx, int w, const WorkItem *work, int nwork, const void *inst, double beta,
-                        int *next, size_t smem, cudaStream_t st)
+int launch_spread_batch(int prec, bool cplx, bool ext, int w, const WorkItem *work, int nwork, const void *inst,
+                        double beta, int *next, size_t smem, cudaStream_t st)
 {
-    if (prec == 64)
-        return cplx ? run_batch<double, true>(w, work, nwork, inst, beta, next, smem, st)
-                    : run_batch<double, false>(w, work, nwork, inst, beta, next, smem, st);
-    return cplx ? run_batch<float, true>(w, work, nwork, inst, beta, next, smem, st)
-                : run_batch<float, false>(w, work, nwork, inst, beta, next, smem, st);
+    if (prec == 64) {
+        if (cplx) return run_batch<double, true, false>(w, work, nwork, inst, beta, next, smem, st);
+        return ext ? run_batch<double, false, true>(w, work, nwork, inst, beta, next, smem, st)
+                   : run_batch<double, false, false>(w, work, nwork, inst, beta, next, smem, st);
+    }
+    if (cplx) return run_batch<float, true, false>(w, work, nwork, inst, beta, next, smem, st);
+    return ext ? run_batch<float, false, true>(w, work, nwork, inst, beta, next, smem, st)
+               : run_batch<float, false, false>(w, work, nwork, inst, beta, next, smem, st);
 }
 
 // Shared memory of the batched kernels for plan p (the batch takes the largest).

@@ -555,8 +555,9 @@ __device__ __forceinline__ int next_item(int *next)
 }
 
 // Spreading over the subproblems of all plans of a batch (same precision, strength type and
-// kernel width; bin size, grid size and points per plan), one persistent launch.
-template <typename T, bool CPLX, int W>
+// kernel width; bin size, grid size and points per plan), one persistent launch.  EXT: every
+// plan is derived (a twice finer grid) and spreads through the extended register window.
+template <typename T, bool CPLX, int W, bool EXT>
 __global__ void __launch_bounds__(256) k_spread_tab_batch(const WorkItem *work, int nwork, const InstDesc<T> *inst,
                                                           T beta, int *next)
 {
@@ -565,7 +566,7 @@ __global__ void __launch_bounds__(256) k_spread_tab_batch(const WorkItem *work, 
         if (it >= nwork) return;
         const WorkItem wk = work[it];
         const InstDesc<T> d = inst[wk.inst];
-        spread_tab_sub<T, CPLX, W, false>(wk.bin, wk.off, d.bin_count, d.bin_start, d.perm, (const T *)d.ux,
+        spread_tab_sub<T, CPLX, W, EXT>(wk.bin, wk.off, d.bin_count, d.bin_start, d.perm, (const T *)d.ux,
                                           (const T *)d.uy, (const T *)d.uz, (const T *)d.in, d.gm, beta,
                                           (T *)d.out);
     }

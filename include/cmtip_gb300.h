@@ -146,9 +146,10 @@ int cmt_bin_clip(int prec, const void *in, int64_t n_img, int n_panels, int px, 
  * of all plans, then every plan's FFT and deconvolution; c[i], f[i], support[i], scale[i]
  * mean what they mean for cmt_execute on plan i (support, scale may be NULL).  Plans are
  * borrowed (they must outlive the batch); a plan given new points or tuning is picked up
- * by the next execute.  Derived plans (cmt_plan_create_derived) may be batched: they
- * spread through the batch kernel without their extended register window.  Stream-ordered on the batch's stream.  No counterpart in the
- * reference, which reconstructs one particle per process. */
+ * by the next execute.  Derived plans (cmt_plan_create_derived) may be batched; a batch of
+ * derived plans only spreads through their extended register window, as a single derived
+ * plan does.  Stream-ordered on the batch's stream.  No counterpart in the reference, which
+ * reconstructs one particle per process. */
 typedef struct cmt_batch cmt_batch;
 int cmt_batch_create(int n_plans, cmt_plan *const *plans, void *stream, cmt_batch **batch);
 int cmt_batch_execute(cmt_batch *batch, void *const *c, void *const *f, const float *const *support,
@@ -244,6 +245,16 @@ int cmt_match_set_refs(cmt_match *match, int64_t n_ref, const void *model, int n
  * near_tie (int32: best two within one FP32 rounding); n_near (host, optional) = count. */
 int cmt_match_run(cmt_match *match, int *best_idx, double *best_d, double *second_d, int *near_tie,
                   int *n_near);
+
+/* The tensor-core runs (modes 0 and 3) of n matchers -- one instance each, any image,
+ * reference and pixel counts -- as one persistent launch per 16 matchers: their (image tile,
+ * reference tile) units are concatenated and split over the SMs by cost, so small instances
+ * do not leave the GPU idle; then each matcher's exact re-scoring, and one host
+ * synchronisation.  Outputs per matcher as for cmt_match_run (arrays of n device pointers;
+ * n_near: optional host array of n counts).  Runs on the stream of ms[0].  Replaces one
+ * match_orientations call (cmtip/alignment/align.py:68-132) per reconstruction. */
+int cmt_match_run_many(int n, cmt_match *const *ms, int *const *best_idx, double *const *best_d,
+                       double *const *second_d, int *const *near_tie, int *n_near);
 
 /* host: the nbatches scale factors followed by std(data). */
 int cmt_match_stats(cmt_match *match, double *host_out);

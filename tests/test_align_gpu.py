@@ -134,3 +134,26 @@ def test_multi_conformation_matches_reference(al, golden, mode):
                                          ref_orientations=geometry.uniform_quaternions(60), mode=mode)
     assert np.array_equal(conf, g["conformations"])
     assert np.array_equal(q, g["matched"])
+
+
+@pytest.mark.parametrize("mode", ["bf16", "bf16x3"])
+def test_grouped_launch_equals_single_runs(al, mode):
+    # one persistent tensor-core launch over matchers of different image, reference and
+    # pixel counts gives each matcher exactly its own run's candidates and re-scored result
+    g = torch.Generator(device="cuda").manual_seed(9)
+    matchers, singles = [], []
+    for n_img, n_ref, n_pix in ((300, 700, 1024), (37, 2000, 4096), (1000, 256, 640), (129, 513, 2048)):
+        x = torch.rand(n_img, n_pix, device="cuda", generator=g)
+        m = torch.rand(n_ref, n_pix, device="cuda", generator=g)
+        w = np.random.default_rng(n_pix).uniform(0.5, 1.5, n_pix)
+        w /= w.sum()
+        mt = al.Matcher(n_pix, mode)
+        mt.set_data(x, w)
+        mt.set_refs(m, nbatches=1)
+        singles.append([t.clone() if torch.is_tensor(t) else t for t in mt.run()])
+        matchers.append(mt)
+    grouped = al.Matcher.run_many(matchers)
+    for one, many in zip(singles, grouped):
+        for a, b in zip(one[:4], many[:4]):
+            assert torch.equal(a, b)
+        assert one[4] == many[4]

@@ -147,3 +147,20 @@ def test_batched_reconstruction_equals_per_instance_stages(nf):
                                        x.images.reshape(-1, 1, x.n_pix), x.M, orientations=x.orientations,
                                        maxiter=10, rtol=0.0, verbose=False)
         assert rel_l2(s.cpu().numpy(), ref.cpu().numpy() if torch.is_tensor(ref) else ref) < 1e-4
+
+
+def test_batched_derived_plans_keep_the_extended_window(nf):
+    # a batch of derived (2M) plans spreads through the extended register window like a
+    # single derived plan; results equal each plan's own execute
+    from cmtip_gb300.batch import Batch
+    rng = np.random.default_rng(45)
+    srcs, ders = [], []
+    for M, N in ((17, 30000), (24, 12000), (31, 20000)):
+        p = nf.Plan(1, M, eps=1e-6, isign=1).set_tuning(5, 4096)
+        p.set_pts(*(torch.from_numpy(rng.uniform(-np.pi, np.pi, N).astype(np.float32)) for _ in range(3)))
+        srcs.append(p)
+        ders.append(p.derive(1, 2 * M, isign=1))
+    outs = Batch(ders).execute(None, real_out=True, fft_order=True, scale=[1.0, 2.0, 0.5])
+    for d, o, k in zip(ders, outs, [1.0, 2.0, 0.5]):
+        single = d.execute(None, real_out=True, fft_order=True, scale=k)
+        assert rel_l2(o.cpu().numpy(), single.cpu().numpy()) < 1e-6
