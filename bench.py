@@ -986,8 +986,13 @@ def batch_bench(torch, args):
     acs_d = [torch.from_numpy(a).cuda() for a in acs]
     br = BatchedReconstruction(inst, eps=cfg["eps"])
     res = {"instances": [dict(M=x.M, n_img=int(x.orientations.shape[0]), n_pix=x.n_pix) for x in inst]}
-    # warm-up of the kernels on the smallest instance
-    BatchedReconstruction(inst[:1], eps=cfg["eps"]).slices(acs_d[:1])
+    # one untimed pass of every stage over all instances (pool growth, plans, matchers,
+    # solvers), as the instances run alone get below
+    sl = br.slices(acs_d)
+    for x, s_ in zip(inst, sl):
+        x.images = s_.reshape(-1, x.n_pix)
+    br.match(acs_d, cfg["n_ref"])
+    br.solve(maxiter=cfg["cg_iterations"])
     br.stats.clear()
     sl = br.slices(acs_d)
     for x, s in zip(inst, sl):

@@ -46,6 +46,22 @@ def gen_nonuniform_positions(orientations, pixel_position_reciprocal, device="cu
     return hkl[0], hkl[1], hkl[2]
 
 
+_MASKS = {}
+
+
+def default_mask_fft(M, device):
+    """ifftshift(gen_F_antisupport(M)) as float32 on the device, built once per (M, device):
+    it depends on M only and takes tens of milliseconds of host work at M ~ 100."""
+    key = (int(M), str(torch.device(device)))
+    mask = _MASKS.get(key)
+    if mask is None:
+        if len(_MASKS) >= 32:
+            _MASKS.pop(next(iter(_MASKS)))
+        m = np.asarray(np.fft.ifftshift(gen_F_antisupport(int(M))), dtype=np.float32)
+        mask = _MASKS[key] = torch.from_numpy(m).to(device).contiguous()
+    return mask
+
+
 class CGSolver:
     """Device CG solver of the reference's normal equations (``cmt_cg``)."""
 
@@ -69,12 +85,7 @@ class CGSolver:
     def set_operator(self, support, alambda, rlambda, flambda, mask_fft=None):
         sup = torch.as_tensor(support, device=self.device).to(torch.float32).contiguous()
         if mask_fft is None:
-            # the antisupport depends on M only: built on the host (~10 ms at M = 81) and
-            # uploaded once per solver
-            mask = self._keep.get("default_mask")
-            if mask is None:
-                m = np.asarray(np.fft.ifftshift(gen_F_antisupport(self.M)), dtype=np.float32)
-                mask = self._keep["default_mask"] = torch.from_numpy(m).to(self.device).contiguous()
+            mask = default_mask_fft(self.M, self.device)
         else:
             mask = torch.as_tensor(np.asarray(mask_fft, dtype=np.float32), device=self.device).contiguous()
         with torch.cuda.device(self.device):

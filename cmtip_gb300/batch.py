@@ -159,7 +159,7 @@ class BatchedReconstruction:
         self.max_points = int(max_points)
         self.stream = stream
         self.stats = {}
-        self._matchers = {}  # (instance, mode) -> Matcher, operand buffers kept across calls
+        self._matchers = {}  # per instance: Matchers (per mode) and CG solvers, buffers kept across calls
         self._weights = {}
 
     # ---------------------------------------------------------------- helpers
@@ -293,8 +293,10 @@ class BatchedReconstruction:
                         img.to(rt))
             plans_M.append(p)
             plans_2M.append(p.derive(1, 2 * M, isign=1))
-            s = CGSolver(M, prec=self.prec, op=TOEPLITZ)
-            solvers.append(s)
+            key = ("solver", i, self.prec)  # kept across calls: buffers and cuFFT plans
+            if key not in self._matchers:
+                self._matchers[key] = CGSolver(M, prec=self.prec, op=TOEPLITZ)
+            solvers.append(self._matchers[key])
             if estimates is None or estimates[i] is None:
                 sups.append(torch.ones(Mtot, dtype=torch.float32, device="cuda"))
                 x0s.append(torch.zeros(Mtot, dtype=torch.float64, device="cuda"))
@@ -326,8 +328,6 @@ class BatchedReconstruction:
             return [x.to(torch.float64).reshape((inst.M,) * 3) for x, inst in zip(xs, self.inst)]
         out = self._timed("solve_s", run)
         self.stats["solve_points"] = 2 * sum(p.N for p in plans_M)
-        for s in solvers:
-            s.close()
         for p in plans_2M + plans_M:
             p.close()
         return out
