@@ -674,6 +674,7 @@ def align_bench(torch, nf, alm, args):
         res[mode]["argmin_disagree_vs_fp64"] = int(diff.sum())
         res[mode]["disagree_outside_fp32_ties"] = int((diff & ~tie).sum())
     res["speedup_bf16_vs_fp64_form"] = res["fp64"]["s"] / res["bf16"]["s"]
+    res["split"] = align_split(torch, nf, alm, ppr, rext, img, acd, refs, n_pix)
     # multi-conformation matching (align.py:135-213): the same images against two volumes
     # (the particle and a second one), the references sorted once
     rho2 = geometry.gaussian_particle(cfg["M"], CFG["n_atoms"], CFG["radius"], np.random.default_rng(cfg["seed"] + 1))
@@ -797,6 +798,45 @@ def loop_bench(torch, args):
     acm.clear_workspaces()
     torch.cuda.empty_cache()
     return res
+
+
+def align_split(torch, nf, alm, ppr, rext, img, acd, refs, n_pix):
+    """CUDA-event split of one BF16 (and one BF16x3) match at the align leg's size: the
+    references' slices (type-2 interpolation), the image and reference operands, the
+    tcgen05 distance kernel and the exact re-scoring; the distance kernel's tensor rate
+    against the measured sustained BF16 peak (algorithmic flops 2 n_img n_ref n_pix per
+    operand term)."""
+    peaks = measured_peaks()
+    out = {}
+    plan = nf.get_plan(2, acd.shape[0], eps=nf.DEFAULT_EPS, isign=-1, prec=32)
+    n_img, n_ref = img.shape[0], len(refs)
+    w = alm.generate_weights(ppr, order=0)
+    for mode, terms in (("bf16", 1), ("bf16x3", 3)):
+        mt = alm.Matcher(n_pix, mode)
+        mt.profile(True)
+        reps = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            model = alm.compute_slices(refs, ppr, rext, acd, plan=plan)
+            e1.record()
+            mt.set_data(img.reshape(n_img, n_pix), w)
+            mt.set_refs(model.reshape(n_ref, n_pix))
+            mt.run()
+            torch.cuda.synchronize()
+            t = mt.last_ms()
+            t["slices"] = e0.elapsed_time(e1)
+            reps.append(t)
+            del model
+        t = {k: float(np.median([r[k] for r in reps])) for k in reps[0]}
+        flops = 2.0 * n_img * n_ref * n_pix * terms
+        tf = flops / (t["distance"] / 1e3) / 1e12
+        out[mode] = {"ms": t, "distance_tflops": tf, "tensor_flops_per_launch": flops,
+                     "frac_of_sustained_bf16": tf / peaks["bf16_tflops_sustained"] if peaks["bf16_tflops_sustained"]
+                     else None, "peak_source": peaks["source"]}
+        mt.close()
+    torch.cuda.empty_cache()
+    return out
 
 
 # ------------------------------------------------------------------ data preparation
@@ -1138,7 +1178,24 @@ def kernel_cases(size="small"):
             points per bin and the same runs of shared windows), about 3 GB on the device.
     full:   the full workload's 5000 images x 4 x 256^2 pixels (1.31e9 points; about 30 GB),
             spreads and interpolation only -- for one-pass metrics, never a full capture.
+    align:  the orientation-matching size only: 5000 images x 16384 pixels against 20000
+            references (BF16 operands, one tcgen05 distance launch and its re-scoring;
+            about 2.5 GB on the device).
     """
+    if size == "align":
+        import torch
+        import cmtip_gb300.alignment as alm
+        n_img, n_ref, n_pix = ALIGN_CFG["n_img"], ALIGN_CFG["n_ref"], 4 * ALIGN_CFG["P"] ** 2
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.rand(n_img, n_pix, device="cuda", generator=g)
+        m = torch.rand(n_ref, n_pix, device="cuda", generator=g)
+        mt = alm.Matcher(n_pix, mode="bf16")
+        mt.set_data(x, np.full(n_pix, 1.0 / n_pix))
+        mt.set_refs(m)
+        mt.run()
+        torch.cuda.synchronize()
+        print(f"kernel case align ({n_img} x {n_ref} x {n_pix}) done", flush=True)
+        return
     import torch
     import cmtip_gb300.nufft as nf
     import cmtip_gb300.alignment as alm
@@ -1210,7 +1267,7 @@ def _run():
     ap.add_argument("--tikhonov", action="store_true", help="run only the weighted Tikhonov solve leg and exit")
     ap.add_argument("--phase", action="store_true", help="run only the phasing leg and exit")
     ap.add_argument("--loop", action="store_true", help="run only the MTIP loop / lambda scan leg and exit")
-    ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full"],
+    ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full", "align"],
                     help="run one case of each hot kernel (for ncu captures) and exit")
     args = ap.parse_args()
     if args.kernels:
@@ -1284,6 +1341,8 @@ def summarize(line):
            "align_bf16_img_per_s": g(ex, "align", "bf16", "img_per_s"),
            "align_speedup_vs_fp64_form": g(ex, "align", "speedup_bf16_vs_fp64_form"),
            "align_disagree_outside_fp32_ties": g(ex, "align", "bf16", "disagree_outside_fp32_ties"),
+           "align_distance_kernel_tflops": g(ex, "align", "split", "bf16", "distance_tflops"),
+           "align_distance_kernel_frac_of_sustained_bf16": g(ex, "align", "split", "bf16", "frac_of_sustained_bf16"),
            "batch_total_s": g(ex, "batch", "total_s"),
            "batch_speedup_vs_alone": g(ex, "batch", "alone", "batch_speedup"),
            "loop_config0_s": g(ex, "loop", "total_s"), "lambda_scan_s": g(ex, "loop", "lambda_scan", "s"),

@@ -110,6 +110,15 @@ class Matcher:
                   arr([o[3].data_ptr() for o in outs]), nn)
         return [o + (int(nn[i]),) for i, o in enumerate(outs)]
 
+    def profile(self, enable=True):
+        _lib.call("cmt_match_profile", self._h, int(bool(enable)))
+
+    def last_ms(self):
+        """{set_data, set_refs, distance, rescore}: ms of the last calls (profile() on)."""
+        ms = (ctypes.c_float * 4)()
+        _lib.call("cmt_match_last_ms", self._h, ms)
+        return dict(zip(("set_data", "set_refs", "distance", "rescore"), (float(v) for v in ms)))
+
     def stats(self):
         out = (ctypes.c_double * (self.nbatches + 1))()
         _lib.call("cmt_match_stats", self._h, out)

@@ -797,7 +797,16 @@ struct Match {
     long long *cta_u = nullptr;  // CTA unit ranges of the last tensor-core launch (num_sms + 1)
     int64_t cap_img = 0;         // bytes of dsum / dsq
     int64_t cap_ref = 0;         // references of msum .. cb
+    // optional CUDA-event timing of the stages (cmt_match_profile): set_data, set_refs,
+    // the distance kernel and the re-scoring of the last calls
+    bool timed = false;
+    cudaEvent_t ev[7] = {};
 };
+
+static void mark(const Match &m, int k)
+{
+    if (m.timed) cudaEventRecord(m.ev[k], m.stream);
+}
 
 }  // namespace cmt
 
@@ -1022,6 +1031,7 @@ extern "C" int cmt_match_create(int64_t n_pix, int mode, void *stream, cmt_match
 extern "C" int cmt_match_set_data(cmt_match *m, int64_t n_img, const void *data, const double *weights)
 {
     CMT_CHECK_ARG(m && data && weights && n_img > 0, "bad argument");
+    mark(*m, 0);
     m->n_img = n_img;
     m->data = data;
     CMT_TRY_CUDA(cudaMemcpyAsync(m->w, weights, sizeof(double) * m->n_pix, cudaMemcpyDeviceToDevice, m->stream));
@@ -1042,6 +1052,7 @@ extern "C" int cmt_match_set_data(cmt_match *m, int64_t n_img, const void *data,
     row_stats(*m, data, n_img, m->dsum, m->dsq);
     build_op(*m, data, n_img, nullptr, 0, m->opA, nullptr);
     CMT_LAUNCH_CHECK();
+    mark(*m, 1);
     return CMT_OK;
 }
 
@@ -1053,6 +1064,7 @@ extern "C" int cmt_match_set_refs(cmt_match *m, int64_t n_ref, const void *model
     CMT_CHECK_ARG(nbatches >= 1 && nbatches <= 1024 && n_ref % nbatches == 0,
                   "n_ref must be a positive multiple of nbatches (<= 1024)");
     CMT_CHECK_ARG(m->n_img > 0, "set_data before set_refs");
+    mark(*m, 2);
     m->n_ref = n_ref;
     m->model = model;
     m->nbatches = nbatches;
@@ -1082,6 +1094,7 @@ extern "C" int cmt_match_set_refs(cmt_match *m, int64_t n_ref, const void *model
     build_op(*m, model, n_ref, m->sref, 1, m->opB, m->mnorm);
     k_score_coeffs<<<ceil_div(m->n_ref_pad, 256), 256, 0, m->stream>>>(m->mnorm, n_ref, m->n_ref_pad, m->ca, m->cb);
     CMT_LAUNCH_CHECK();
+    mark(*m, 3);
     return CMT_OK;
 }
 
@@ -1094,6 +1107,7 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
     CMT_CHECK_ARG(m->n_img > 0 && m->n_ref > 0, "set_data and set_refs first");
     cudaStream_t st = m->stream;
     SegInfo si{};
+    mark(*m, 4);
     if (m->mode == 0 || m->mode == 3) {
         cmt_match *one[1] = {m};
         CMT_TRY(tc_launch(1, one, st, &si));
@@ -1119,8 +1133,10 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
                                                       nimg_pad);
         CMT_LAUNCH_CHECK();
     }
+    mark(*m, 5);
     merge(*m, si, st, best_idx, best_d, second_d, near_tie);
     CMT_LAUNCH_CHECK();
+    mark(*m, 6);
     if (m->mode == 0 || m->mode == 3 || n_near_host) {
         int herr = 0;
         if (m->mode == 0 || m->mode == 3) CMT_TRY_CUDA(cudaMemcpyAsync(&herr, m->err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1182,9 +1198,33 @@ extern "C" int cmt_match_stats(cmt_match *m, double *host_out)
     return CMT_OK;
 }
 
+// CUDA-event timing of the matcher's stages (enable 0/1); cmt_match_last_ms then gives, in
+// ms, the last set_data (image operands), set_refs (reference statistics and operands),
+// distance kernel and re-scoring.  Used by benchmarks.
+extern "C" int cmt_match_profile(cmt_match *m, int enable)
+{
+    CMT_CHECK_ARG(m, "null matcher");
+    if (enable && !m->ev[0])
+        for (auto &e : m->ev) CMT_TRY_CUDA(cudaEventCreate(&e));
+    m->timed = enable != 0;
+    return CMT_OK;
+}
+
+extern "C" int cmt_match_last_ms(cmt_match *m, float *ms)
+{
+    CMT_CHECK_ARG(m && ms, "null argument");
+    CMT_CHECK_ARG(m->timed, "profiling is off (cmt_match_profile)");
+    CMT_TRY_CUDA(cudaEventSynchronize(m->ev[6]));
+    const int pairs[4][2] = {{0, 1}, {2, 3}, {4, 5}, {5, 6}};
+    for (int k = 0; k < 4; ++k) CMT_TRY_CUDA(cudaEventElapsedTime(&ms[k], m->ev[pairs[k][0]], m->ev[pairs[k][1]]));
+    return CMT_OK;
+}
+
 extern "C" int cmt_match_destroy(cmt_match *m)
 {
     if (!m) return CMT_OK;
+    for (auto e : m->ev)
+        if (e) cudaEventDestroy(e);
     void *bufs[] = {m->w, m->wdf, m->cen, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
                     m->ca, m->cb, m->stats, m->pscore, m->pidx, m->err, m->near, m->scratch_d, m->cta_u};
     for (void *b : bufs) cudaFree(b);

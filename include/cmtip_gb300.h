@@ -256,6 +256,12 @@ int cmt_match_run(cmt_match *match, int *best_idx, double *best_d, double *secon
 int cmt_match_run_many(int n, cmt_match *const *ms, int *const *best_idx, double *const *best_d,
                        double *const *second_d, int *const *near_tie, int *n_near);
 
+/* CUDA-event timing of a matcher's stages (enable 0/1), and read-back (ms, 4 values) of the
+ * last set_data (image operands), set_refs (reference statistics and operands), distance
+ * kernel and exact re-scoring.  Used by benchmarks; no counterpart in the reference. */
+int cmt_match_profile(cmt_match *match, int enable);
+int cmt_match_last_ms(cmt_match *match, float *ms);
+
 /* host: the nbatches scale factors followed by std(data). */
 int cmt_match_stats(cmt_match *match, double *host_out);
 

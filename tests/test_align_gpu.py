@@ -157,3 +157,16 @@ def test_grouped_launch_equals_single_runs(al, mode):
         for a, b in zip(one[:4], many[:4]):
             assert torch.equal(a, b)
         assert one[4] == many[4]
+
+
+def test_matcher_stage_timing(al):
+    # the stage timers report the last set_data / set_refs / distance / re-scoring
+    g = torch.Generator(device="cuda").manual_seed(3)
+    mt = al.Matcher(1024, "bf16")
+    mt.profile(True)
+    mt.set_data(torch.rand(200, 1024, device="cuda", generator=g), np.full(1024, 1.0 / 1024))
+    mt.set_refs(torch.rand(600, 1024, device="cuda", generator=g))
+    mt.run()
+    t = mt.last_ms()
+    assert set(t) == {"set_data", "set_refs", "distance", "rescore"}
+    assert all(v > 0 for v in t.values())
