@@ -82,6 +82,8 @@ SIGNATURES = {
     "cmt_match_run": [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_i32)],
     "cmt_match_run_many": [_i32, _vp, _vp, _vp, _vp, _vp, _vp],
     "cmt_match_profile": [_vp, _i32],
+    "cmt_match_set_wait_limit": [_vp, _f64],
+    "cmt_match_stall_loads": [_vp, _i32],
     "cmt_match_last_ms": [_vp, ctypes.POINTER(ctypes.c_float)],
     "cmt_match_stats": [_vp, ctypes.POINTER(_f64)],
     "cmt_match_destroy": [_vp],

@@ -110,6 +110,11 @@ class Matcher:
                   arr([o[3].data_ptr() for o in outs]), nn)
         return [o + (int(nn[i]),) for i, o in enumerate(outs)]
 
+    def set_wait_limit(self, seconds):
+        """Limit of the tensor-core pipeline's bounded waits (a run that exceeds it raises
+        CmtError with code CMT_ERR_TIMEOUT; the matcher and the context stay usable)."""
+        _lib.call("cmt_match_set_wait_limit", self._h, float(seconds))
+
     def profile(self, enable=True):
         _lib.call("cmt_match_profile", self._h, int(bool(enable)))
 

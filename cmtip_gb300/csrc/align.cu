@@ -324,9 +324,11 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Bounded wait on an mbarrier phase: gives up after ~2 s (or when another role has
-// already given up) and reports false; the caller records the timeout and unwinds.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag)
+// Bounded wait on an mbarrier phase: gives up after limit_ns of %globaltimer (or, with an
+// abort flag, as soon as another role has given up) and reports false; the caller records
+// the timeout and unwinds.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                          uint64_t limit_ns)
 {
     uint64_t t0 = 0;
     for (uint32_t it = 0;; ++it) {
@@ -338,11 +340,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
             : "memory");
         if (ok) return true;
         if ((it & 255) == 0) {
-            if (*abort_flag) return false;
+            if (abort_flag && *abort_flag) return false;
             uint64_t t = globaltimer();
             if (t0 == 0) t0 = t;
-            else if (t - t0 > 2000000000ull) {
-                *abort_flag = 1;
+            else if (t - t0 > limit_ns) {
+                if (abort_flag) *abort_flag = 1;
                 return false;
             }
         }
@@ -425,7 +427,9 @@ struct TcGroup {
     CUtensorMap tmA[TC_MAXP], tmB[TC_MAXP];
     TcProblem p[TC_MAXP];
     int np;
-    const long long *cta_u;  // CTA c owns units [cta_u[c], cta_u[c + 1])
+    const long long *cta_u;     // CTA c owns units [cta_u[c], cta_u[c + 1])
+    unsigned long long wait_ns;  // limit of every pipeline wait
+    int stall_loads;             // test of the timeout path: the producer issues no loads
 };
 
 // advance p to the problem holding unit u (units are visited in increasing order)
@@ -447,13 +451,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
     unsigned char *gbase = smem_raw + (base - smem_u32(smem_raw));
     uint32_t sA0 = base, sB0 = base + TC_STAGES * TC_A_BYTES;
     uint64_t *bars = reinterpret_cast<uint64_t *>(gbase + TC_STAGES * TC_STAGE_BYTES);
-    // bars: full[S], empty[S], accf[2], acce[2]
+    // bars: full[S], empty[S], accf[2], acce[2], drain
     uint32_t bar0 = smem_u32(bars);
     auto full_b = [&](int s) { return bar0 + 8u * s; };
     auto empty_b = [&](int s) { return bar0 + 8u * (TC_STAGES + s); };
     auto accf_b = [&](int b) { return bar0 + 8u * (2 * TC_STAGES + b); };
     auto acce_b = [&](int b) { return bar0 + 8u * (2 * TC_STAGES + 2 + b); };
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(gbase + TC_STAGES * TC_STAGE_BYTES + 8 * (2 * TC_STAGES + 4));
+    const uint32_t drain_b = bar0 + 8u * (2 * TC_STAGES + 4);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(gbase + TC_STAGES * TC_STAGE_BYTES + 8 * (2 * TC_STAGES + 5));
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -469,6 +474,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
             mbar_init(accf_b(b), 1);
             mbar_init(acce_b(b), 4);
         }
+        mbar_init(drain_b, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -489,25 +495,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
             uint32_t ph = 0;
             bool ok = true;
             int p = 0;
-            for (long long u = u0; u < u1 && ok; ++u) {
+            unsigned used = 0;           // stages with a load issued
+            uint32_t used_ph[TC_STAGES];  // the phase of each stage's last load
+            for (long long u = u0; u < u1 && ok && !g.stall_loads; ++u) {
                 p = problem_of(g, u, p);
                 const long long lu = u - g.p[p].ustart;
                 const int m = (int)(lu / g.p[p].n_rtiles), t = (int)(lu % g.p[p].n_rtiles);
                 const int KB = g.p[p].KB;
                 for (int kb = 0; kb < KB; ++kb) {
-                    if (!mbar_wait(empty_b(s), ph ^ 1, abort_flag)) {
+                    if (!mbar_wait(empty_b(s), ph ^ 1, abort_flag, g.wait_ns)) {
                         ok = false;
                         break;
                     }
                     mbar_expect_tx(full_b(s), TC_STAGE_BYTES);
                     tma_load_2d(sA0 + s * TC_A_BYTES, &g.tmA[p], full_b(s), kb * TC_BK, m * TC_BM);
                     tma_load_2d(sB0 + s * TC_B_BYTES, &g.tmB[p], full_b(s), kb * TC_BK, t * TC_BN);
+                    used |= 1u << s;
+                    used_ph[s] = ph;
                     if (++s == TC_STAGES) {
                         s = 0;
                         ph ^= 1;
                     }
                 }
             }
+            // before the CTA can exit, every load this thread issued has landed (on the normal
+            // path the MMA warp has already consumed them; after a timeout they may still be
+            // in flight): a bounded wait per stage that does not stop on the abort flag
+            for (int st = 0; st < TC_STAGES; ++st)
+                if ((used >> st) & 1u)
+                    if (!mbar_wait(full_b(st), used_ph[st], nullptr, g.wait_ns)) ok = false;
             if (!ok) atomicOr(err, 1);
         }
     } else if (warp == 1) {
@@ -521,14 +537,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
                 p = problem_of(g, u, p);
                 const int KB = g.p[p].KB;
                 int b = lt & 1;
-                if (!mbar_wait(acce_b(b), ((lt >> 1) & 1) ^ 1, abort_flag)) {
+                if (!mbar_wait(acce_b(b), ((lt >> 1) & 1) ^ 1, abort_flag, g.wait_ns)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 uint32_t dt = tmem + (uint32_t)(b * TC_BN);
                 for (int kb = 0; kb < KB; ++kb) {
-                    if (!mbar_wait(full_b(s), ph, abort_flag)) {
+                    if (!mbar_wait(full_b(s), ph, abort_flag, g.wait_ns)) {
                         ok = false;
                         break;
                     }
@@ -545,6 +561,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
                 }
                 if (ok) umma_commit(accf_b(b));
             }
+            // every MMA this thread issued has completed before TMEM can be released (after a
+            // timeout some may still run): one more commit, and a bounded wait on it
+            umma_commit(drain_b);
+            if (!mbar_wait(drain_b, 0, nullptr, g.wait_ns)) ok = false;
             if (!ok) atomicOr(err, 1);
         }
     } else {
@@ -590,7 +610,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
             }
             const float *ca = g.p[p].ca, *cb = g.p[p].cb;
             int b = lt & 1;
-            if (!mbar_wait(accf_b(b), (lt >> 1) & 1, abort_flag)) {
+            if (!mbar_wait(accf_b(b), (lt >> 1) & 1, abort_flag, g.wait_ns)) {
                 ok = false;
                 break;
             }
@@ -635,6 +655,7 @@ struct SegInfo {
     int mode;       // 0: SIMT layout [ref tile][image]; 1: tcgen05 layout [cta][seg][row]
     int nseg;       // mode 0: reference tiles
     int nimg_pad;   // mode 0
+    int n_ref;                    // candidates outside [0, n_ref) are ignored
     long long ustart, G;          // mode 1: the problem's first unit, CTAs of the launch
     int n_rtiles, maxseg;
     const long long *cta_u;       // mode 1: CTA c owned units [cta_u[c], cta_u[c + 1])
@@ -656,10 +677,13 @@ __global__ void k_merge_rescore(SegInfo si, const float *pscore, const int *pidx
         s[k] = SCORE_INF;
         id[k] = -1;
     }
+    // a list is read only as far as its valid entries go: after a timed-out distance
+    // launch the lists hold whatever the buffers held, and no index outside [0, n_ref) may
+    // reach the re-scoring's model reads
     auto take = [&](long long o) {
         for (int k = 0; k < TOPK; ++k) {
             int r = pidx[o + k];
-            if (r < 0) break;
+            if (r < 0 || r >= si.n_ref) break;
             topk_insert(s, id, pscore[o + k], r);
         }
     };
@@ -801,6 +825,8 @@ struct Match {
     // the distance kernel and the re-scoring of the last calls
     bool timed = false;
     cudaEvent_t ev[7] = {};
+    double wait_s = 2.0;  // limit of the tensor-core pipeline's waits
+    int stall_loads = 0;  // test of the timeout path (cmt_match_stall_loads)
 };
 
 static void mark(const Match &m, int k)
@@ -939,6 +965,8 @@ static int tc_launch(int n, cmt_match *const *ms, cudaStream_t st, SegInfo *si)
     memset(&g, 0, sizeof g);
     g.np = n;
     g.cta_u = ms[0]->cta_u;
+    g.wait_ns = (unsigned long long)(ms[0]->wait_s * 1e9);
+    for (int i = 0; i < n; ++i) g.stall_loads |= ms[i]->stall_loads;
     for (int i = 0; i < n; ++i) {
         Match &m = *ms[i];
         int maxseg = 1;
@@ -958,6 +986,7 @@ static int tc_launch(int n, cmt_match *const *ms, cudaStream_t st, SegInfo *si)
         g.p[i] = TcProblem{ustart[i], n_rt[i], KB[i], maxseg, m.ca, m.cb, m.pscore, m.pidx};
         si[i] = SegInfo{};
         si[i].mode = 1;
+        si[i].n_ref = (int)m.n_ref;
         si[i].ustart = ustart[i];
         si[i].G = G;
         si[i].n_rtiles = n_rt[i];
@@ -1116,6 +1145,7 @@ extern "C" int cmt_match_run(cmt_match *m, int *best_idx, double *best_d, double
         int nimg_pad = n_it * 64;
         int64_t need = (int64_t)n_rt * nimg_pad * TOPK;
         si.mode = 0;
+        si.n_ref = (int)m->n_ref;
         si.nseg = n_rt;
         si.nimg_pad = nimg_pad;
         int64_t cap = m->cap_part;
@@ -1195,6 +1225,26 @@ extern "C" int cmt_match_stats(cmt_match *m, double *host_out)
     CMT_TRY_CUDA(cudaMemcpyAsync(host_out, m->stats, sizeof(double) * (m->nbatches + 1), cudaMemcpyDeviceToHost,
                                  m->stream));
     CMT_TRY_CUDA(cudaStreamSynchronize(m->stream));
+    return CMT_OK;
+}
+
+// Limit (seconds, 1e-3 .. 60) of every wait of the tensor-core pipeline; a wait that runs
+// out makes cmt_match_run return CMT_ERR_TIMEOUT with the context still usable.
+extern "C" int cmt_match_set_wait_limit(cmt_match *m, double seconds)
+{
+    CMT_CHECK_ARG(m, "null matcher");
+    CMT_CHECK_ARG(seconds >= 1e-3 && seconds <= 60.0, "wait limit must be in [1e-3, 60] seconds");
+    m->wait_s = seconds;
+    return CMT_OK;
+}
+
+// Test of the timeout path: while enabled, the tensor-core kernel's producer issues no loads,
+// so the MMA and epilogue waits run out after the wait limit; every role then unwinds (the
+// TMEM allocation is released) and the run returns CMT_ERR_TIMEOUT.
+extern "C" int cmt_match_stall_loads(cmt_match *m, int enable)
+{
+    CMT_CHECK_ARG(m, "null matcher");
+    m->stall_loads = enable != 0;
     return CMT_OK;
 }
 

@@ -81,16 +81,40 @@ int run_interp(Plan &p, int rs, void *out)
 }
 
 template <typename T>
+PairFn<T> pick_pair_tab(int w)
+{
+    switch (w) {
+    case 2: return k_pair_tab<T, 2>;
+    case 3: return k_pair_tab<T, 3>;
+    case 4: return k_pair_tab<T, 4>;
+    case 5: return k_pair_tab<T, 5>;
+    case 6: return k_pair_tab<T, 6>;
+    case 7: return k_pair_tab<T, 7>;
+    case 8: return k_pair_tab<T, 8>;
+    default: return nullptr;
+    }
+}
+
+// Widths 2..8 run the table-driven pair (k_pair_tab) when its two subgrids and tables fit
+// in shared memory; wider kernels (or larger subgrids) the per-point pair (k_pair).
+template <typename T>
 int run_pair(Plan &p, bool prepare_only)
 {
-    PairFn<T> k = pick_pair<T>(p.w);
-    int sm = (int)(4 * sub_bytes(p));
+    int dev = 0, max_sm = 0;
+    CMT_TRY_CUDA(cudaGetDevice(&dev));
+    CMT_TRY_CUDA(cudaDeviceGetAttribute(&max_sm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t tab_sm = pair_tab_smem<T>(sub_bytes(p), 8);
+    const bool tab = p.spread_tab && p.interp_tab && p.w >= 2 && p.w <= 8 && tab_sm <= (size_t)max_sm;
+    PairFn<T> k = tab ? pick_pair_tab<T>(p.w) : pick_pair<T>(p.w);
+    int sm = (int)(tab ? tab_sm : 4 * sub_bytes(p));
     CMT_TRY(prep_smem(k, sm));
     if (prepare_only) return CMT_OK;
+    prof_begin(p);
     k<<<(unsigned)p.nsub, 256, sm, p.stream>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start, (const T *)p.ux,
                                                 (const T *)p.uy, (const T *)p.uz, (const T *)p.fine, geom(p, p.n),
                                                 (T)p.beta, (T *)p.fine2);
     CMT_LAUNCH_CHECK();
+    prof_end(p, PROF_PAIR);
     return CMT_OK;
 }
 

@@ -1050,3 +1050,221 @@ __global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub
         atomicAdd(&g2[2 * g + 1], vi);
     }
 }
+
+// ------------------------------------------------------------------ table-driven fused pair
+
+// Shared-memory bytes of k_pair_tab: the two complex subgrids (G1 staged, G2 accumulated),
+// 16-byte aligned, then per warp a table of 32 records (32 values) and 32 x 8 complex
+// partial sums.
+template <typename T>
+__host__ __device__ inline size_t pair_tab_smem(size_t subgrid_bytes, int warps)
+{
+    return ((4 * subgrid_bytes + 15) & ~(size_t)15) + warps * 32 * (32 + 16) * sizeof(T);
+}
+
+// Table-driven fused type-2 then type-1 pair on one subproblem (kernel width W <= 8): the
+// complex subgrid G1 is staged in shared memory and a second one, G2, accumulates.  Per batch
+// of 32 points, lane t prepares point t's record once (window origin and its 3W kernel
+// values, tab_prepare).  Pass A walks the batch run by run like k_interp_tab: a lane keeps
+// its cells of G1's current window in registers and forms its partials of each point's
+// value; lane t then adds point t's eight partials, c_t = sum_k G1_k phi_k(x_t), and rewrites
+// its record's z part as (z c_t) pairs.  Pass B walks the batch again like k_spread_tab with
+// complex strengths c_t, adding into a register window of G2 that goes to shared memory
+// (atomics) when the window origin changes.  G2 is added to the fine grid once.  Kernel
+// values are evaluated once per point for both directions, and no N-sized intermediate is
+// written.
+template <typename T, int W>
+__device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_count, const int *bin_start, const T *ux,
+                                             const T *uy, const T *uz, const T *g1, const SubgridGeom &gm, T beta,
+                                             T *g2)
+{
+    static_assert(W >= 2 && W <= 8, "table pair needs a window of at most 8 columns");
+    constexpr int EW = 8, BR = 4, RX = (W + BR - 1) / BR, REC = 32;
+    using T2 = typename cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int S = gm.S, P = gm.P, h = W / 2, n = gm.n;
+    const int plane = S * P, copy = S * plane;
+    T *sa = reinterpret_cast<T *>(smem_raw);
+    T *sb = sa + 2 * copy;
+    const size_t sgb = ((size_t)4 * copy * sizeof(T) + 15) & ~(size_t)15;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    T *tab = reinterpret_cast<T *>(smem_raw + sgb) + warp * 32 * (REC + 16);
+    T *part = tab + 32 * REC;  // 32 points x 8 z lanes, (re, im)
+    for (int i = threadIdx.x; i < 2 * copy; i += blockDim.x) sb[i] = T(0);
+    load_subgrid<T, true>(g1, gm, b, sa);
+    __syncthreads();
+
+    const int cnt = min(gm.maxsub, bin_count[b] - off);
+    const int p0 = bin_start[b] + off;
+    const int e = lane % EW, bl = lane / EW;
+
+    // pass A state: G1 window (rows bl, bl + 4 at z offset e, all W columns)
+    T gr[RX][W], gi[RX][W];
+    int key_a = -1;
+    // pass B state: G2 accumulation window
+    T acc[RX][W], aci[RX][W];
+#pragma unroll
+    for (int r = 0; r < RX; ++r)
+#pragma unroll
+        for (int a = 0; a < W; ++a) acc[r][a] = aci[r][a] = T(0);
+    int key_b = -1, X0 = 0, Y0 = 0, Z0 = 0;
+    auto flush = [&]() {
+        if (key_b < 0) return;
+        const int zz = Z0 + e;
+#pragma unroll
+        for (int r = 0; r < RX; ++r) {
+            const int yy = Y0 + bl + r * BR;
+            const bool row_ok = e < W && bl + r * BR < W;
+#pragma unroll
+            for (int a = 0; a < W; ++a) {
+                if (row_ok) {
+                    const int idx = ((X0 + a) * S + yy) * P + zz;
+                    if (acc[r][a] != T(0)) atomicAdd(&sb[idx], acc[r][a]);
+                    if (aci[r][a] != T(0)) atomicAdd(&sb[copy + idx], aci[r][a]);
+                }
+                acc[r][a] = aci[r][a] = T(0);
+            }
+        }
+    };
+
+    int t0, t1;
+    warp_run(cnt, warp, nwarps, t0, t1);
+    const T cs = (T)gm.cscale;
+    for (int base = t0; base < t1; base += 32) {
+        const int tl = base + lane;
+        const bool valid = tl < t1;
+        const int pos = p0 + (valid ? tl : t0);
+        const T px = ux[pos] * cs, py = uy[pos] * cs, pz = uz[pos] * cs;
+        __syncwarp();  // the previous batch's records and partials have been read
+        T *rec = tab + lane * REC;
+        const int my_key = tab_prepare<T, W, false, 0>(px, py, pz, beta, T(1), T(0), rec);
+        __syncwarp();
+        const int nq = min(32, t1 - base);
+        const int prev_key = __shfl_up_sync(0xffffffffu, my_key, 1);
+        unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || my_key != prev_key);
+        starts &= nq >= 32 ? 0xffffffffu : ((1u << nq) - 1u);
+
+        // ---- pass A: interpolate every point of the batch from G1
+        for (int q = 0; q < nq;) {
+            const unsigned later = starts & ~((2u << q) - 1u);
+            const int qe = later ? __ffs(later) - 1 : nq;
+            const int key = __shfl_sync(0xffffffffu, my_key, q);  // warp-uniform
+            if (key != key_a) {
+                key_a = key;
+                const int XA = (key >> 12) - 16 + h, YA = ((key >> 6) & 63) - 16 + h, ZA = (key & 63) - 16 + h;
+                const int idx0 = (XA * S + YA + bl) * P + ZA + e;
+#pragma unroll
+                for (int r = 0; r < RX; ++r) {
+                    const bool ok = e < W && bl + r * BR < W;
+#pragma unroll
+                    for (int a = 0; a < W; ++a) {
+                        const int idx = idx0 + a * plane + r * BR * P;
+                        gr[r][a] = ok ? sa[idx] : T(0);
+                        gi[r][a] = ok ? sa[copy + idx] : T(0);
+                    }
+                }
+            }
+            for (; q < qe; ++q) {
+                const T *rq = tab + q * REC;
+                T xv[8];
+                load8(rq, xv);
+                const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
+                const T zv = rq[16 + e];
+                T ar0 = T(0), ai0 = T(0), ar1 = T(0), ai1 = T(0);
+#pragma unroll
+                for (int a = 0; a < W; ++a) {
+                    ar0 += xv[a] * gr[0][a];
+                    ai0 += xv[a] * gi[0][a];
+                    if (RX > 1) {
+                        ar1 += xv[a] * gr[RX - 1][a];
+                        ai1 += xv[a] * gi[RX - 1][a];
+                    }
+                }
+                T sr = (yv.x * ar0 + yv.y * ar1) * zv;
+                T si = (yv.x * ai0 + yv.y * ai1) * zv;
+                sr += __shfl_xor_sync(0xffffffffu, sr, 8);
+                sr += __shfl_xor_sync(0xffffffffu, sr, 16);
+                si += __shfl_xor_sync(0xffffffffu, si, 8);
+                si += __shfl_xor_sync(0xffffffffu, si, 16);
+                if (bl == 0) reinterpret_cast<T2 *>(part)[q * 8 + e] = T2{sr, si};
+            }
+        }
+        __syncwarp();
+        // ---- lane t: point t's value, folded into its record as (z c) pairs
+        {
+            T v[8], w2[8];
+            load8(part + lane * 16, v);
+            load8(part + lane * 16 + 8, w2);
+            T cr = ((v[0] + v[2]) + (v[4] + v[6])) + ((w2[0] + w2[2]) + (w2[4] + w2[6]));
+            T ci = ((v[1] + v[3]) + (v[5] + v[7])) + ((w2[1] + w2[3]) + (w2[5] + w2[7]));
+            if (!valid) cr = ci = T(0);
+            T z[8], o[8];
+            load8(rec + 16, z);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                o[2 * k] = z[k] * cr;
+                o[2 * k + 1] = z[k] * ci;
+            }
+            T o2[8];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                o2[2 * k] = z[k + 4] * cr;
+                o2[2 * k + 1] = z[k + 4] * ci;
+            }
+            store8(rec + 16, o);
+            store8(rec + 24, o2);
+        }
+        __syncwarp();
+        // ---- pass B: spread every point's value back into G2 with the same kernel values
+        for (int q = 0; q < nq;) {
+            const unsigned later = starts & ~((2u << q) - 1u);
+            const int qe = later ? __ffs(later) - 1 : nq;
+            const int key = __shfl_sync(0xffffffffu, my_key, q);  // warp-uniform
+            if (key != key_b) {
+                flush();
+                key_b = key;
+                X0 = (key >> 12) - 16 + h;
+                Y0 = ((key >> 6) & 63) - 16 + h;
+                Z0 = (key & 63) - 16 + h;
+            }
+            for (; q < qe; ++q) {
+                const T *rq = tab + q * REC;
+                T xv[8];
+                load8(rq, xv);
+                const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
+                const T2 zv = reinterpret_cast<const T2 *>(rq + 16)[e];
+                const T wr0 = yv.x * zv.x, wi0 = yv.x * zv.y, wr1 = yv.y * zv.x, wi1 = yv.y * zv.y;
+#pragma unroll
+                for (int a = 0; a < W; ++a) {
+                    acc[0][a] += xv[a] * wr0;
+                    aci[0][a] += xv[a] * wi0;
+                    if (RX > 1) {
+                        acc[RX - 1][a] += xv[a] * wr1;
+                        aci[RX - 1][a] += xv[a] * wi1;
+                    }
+                }
+            }
+        }
+    }
+    flush();
+    __syncthreads();
+    const int bx = b / (gm.nb * gm.nb), by = (b / gm.nb) % gm.nb, bz = b % gm.nb;
+    const int ox = bx * gm.bs - h, oy = by * gm.bs - h, oz = bz * gm.bs - h;
+    for (int i = threadIdx.x; i < S * S * S; i += blockDim.x) {
+        const int a = i / (S * S), rem = i - a * S * S, bb = rem / S, ee = rem - bb * S;
+        const int li = (a * S + bb) * P + ee;
+        const T vr = sb[li], vi = sb[copy + li];
+        if (vr == T(0) && vi == T(0)) continue;
+        const int64_t g = ((int64_t)wrapi(ox + a, n) * n + wrapi(oy + bb, n)) * n + wrapi(oz + ee, n);
+        atomicAdd(&g2[2 * g], vr);
+        atomicAdd(&g2[2 * g + 1], vi);
+    }
+}
+
+template <typename T, int W>
+__global__ void __launch_bounds__(256) k_pair_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
+                                                  const int *bin_start, const T *ux, const T *uy, const T *uz,
+                                                  const T *g1, SubgridGeom gm, T beta, T *g2)
+{
+    pair_tab_sub<T, W>(sub_bin[blockIdx.x], sub_off[blockIdx.x], bin_count, bin_start, ux, uy, uz, g1, gm, beta, g2);
+}

@@ -256,6 +256,16 @@ int cmt_match_run(cmt_match *match, int *best_idx, double *best_d, double *secon
 int cmt_match_run_many(int n, cmt_match *const *ms, int *const *best_idx, double *const *best_d,
                        double *const *second_d, int *const *near_tie, int *n_near);
 
+/* Limit (seconds, 1e-3 .. 60; default 2) of every wait of the tensor-core pipeline.  A wait
+ * that runs out unwinds the kernel (in-flight copies and MMAs drained, TMEM released) and
+ * cmt_match_run returns CMT_ERR_TIMEOUT with the context still usable. */
+int cmt_match_set_wait_limit(cmt_match *match, double seconds);
+
+/* Test of that timeout path: while enabled (1) the tensor-core kernel's producer issues no
+ * loads, so its consumers' waits run out; 0 restores normal runs.  No counterpart in the
+ * reference. */
+int cmt_match_stall_loads(cmt_match *match, int enable);
+
 /* CUDA-event timing of a matcher's stages (enable 0/1), and read-back (ms, 4 values) of the
  * last set_data (image operands), set_refs (reference statistics and operands), distance
  * kernel and exact re-scoring.  Used by benchmarks; no counterpart in the reference. */

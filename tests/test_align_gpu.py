@@ -170,3 +170,32 @@ def test_matcher_stage_timing(al):
     t = mt.last_ms()
     assert set(t) == {"set_data", "set_refs", "distance", "rescore"}
     assert all(v > 0 for v in t.values())
+
+
+def test_bounded_waits_time_out_and_recover(al):
+    # the tensor-core kernel's producer issues no loads (cmt_match_stall_loads), so the MMA and
+    # epilogue waits run out after a 20 ms limit: the run reports CMT_ERR_TIMEOUT, every role
+    # unwinds, and the same matcher then runs normally with the same results as before
+    import ctypes
+    from cmtip_gb300 import _lib
+    g = torch.Generator(device="cuda").manual_seed(4)
+    mt = al.Matcher(2048, "bf16")
+    mt.set_data(torch.rand(300, 2048, device="cuda", generator=g), np.full(2048, 1.0 / 2048))
+    mt.set_refs(torch.rand(700, 2048, device="cuda", generator=g))
+    before = [t.clone() for t in mt.run()[:3]]
+    lib = _lib.load()
+    mt.set_wait_limit(0.02)
+    _lib.check(lib.cmt_match_stall_loads(mt._h, 1))
+    with pytest.raises(_lib.CmtError) as e:
+        mt.run()
+    assert e.value.code == _lib.CMT_ERR_TIMEOUT
+    _lib.check(lib.cmt_match_stall_loads(mt._h, 0))
+    mt.set_wait_limit(2.0)
+    after = mt.run()[:3]
+    for a, b in zip(before, after):
+        assert torch.equal(a, b)
+    # the context is usable by other work as well
+    x = torch.ones(1000, device="cuda")
+    assert float(x.sum()) == 1000.0
+    with pytest.raises(ValueError):
+        mt.set_wait_limit(0.0)

@@ -249,6 +249,34 @@ def test_pair_is_normal_operator(nf, prec):
     assert rel_l2(got.cpu().numpy(), ref) < (TOL32 if prec == 32 else TOL64)
 
 
+@pytest.mark.parametrize("prec,eps", [(32, 1e-2), (32, 1e-4), (32, 1e-6), (64, 1e-7), (64, 1e-5)])
+@pytest.mark.parametrize("tuning", [None, (5, 2048)])
+def test_table_pair_matches_per_point_pair(nf, prec, eps, tuning, monkeypatch):
+    # widths 3..8: the table-driven fused pair (kernel values once per point for both
+    # directions) equals the per-point pair and the exact normal operator
+    rng = np.random.default_rng(25)
+    M, N = 21, 40000
+    x, y, z = _pts(rng, N)
+    f = rng.standard_normal((M,) * 3)
+    sup = (rng.random((M,) * 3) > 0.2).astype(np.float32)
+    pts = [torch.from_numpy(a) for a in (x, y, z)]
+
+    def plan():
+        p = nf.Plan(1, M, eps=eps, isign=1, prec=prec)
+        if tuning:
+            p.set_tuning(*tuning)
+        return p.set_pts(*pts)
+    tab = plan()
+    monkeypatch.setenv("CMT_INTERP_TAB", "0")
+    ref_plan = plan()
+    a = tab.execute_pair(torch.from_numpy(f), support=torch.from_numpy(sup)).cpu().numpy()
+    b = ref_plan.execute_pair(torch.from_numpy(f), support=torch.from_numpy(sup)).cpu().numpy()
+    assert rel_l2(a, b) < (1e-6 if prec == 32 else 1e-13)
+    c = on.type2(x, y, z, f * sup, eps=1e-13, isign=-1)
+    ref = on.type1(x, y, z, c, M, eps=1e-13, isign=1).real * sup
+    assert rel_l2(a, ref) < max(40 * eps, 1e-5)
+
+
 def test_adjointness_large(nf):
     # <A f, c> == <f, A^H c> at 4M points with FP32 kernels, FP64 inner products
     rng = np.random.default_rng(12)
