@@ -490,10 +490,12 @@ static int capture_iteration(Cg &c)
     return CMT_OK;
 }
 
-// Start of a solve (scipy's cg before its loop), stream-ordered with no host round trip:
-// b = d, x = x0, ||b||, threshold max(atol, rtol ||b||), r0 = b - W x0, rho = r0.r0.  scipy
-// skips the matvec when x0 is all zeros; W 0 is exactly 0, so r0 = b either way.  When
-// ||b|| = 0 the done flag is set and x = b (scipy returns b itself).
+// Start of a solve (scipy's cg before its loop), stream-ordered: b = d, x = x0, ||b||,
+// threshold max(atol, rtol ||b||), r0 = b - W x0, rho = r0.r0.  scipy skips the matvec when
+// x0 is all zeros; W 0 is exactly 0, so with the Toeplitz operator r0 = b - W x0 is computed
+// either way and the start needs no host round trip (the explicit pair, whose matvec costs a
+// NUFFT pair, checks x0 on the host).  When ||b|| = 0 the done flag is set and x = b (scipy
+// returns b itself).
 template <typename T>
 static int solve_begin(Cg &c, const T *d, T *x, double rtol, double atol)
 {
@@ -509,9 +511,24 @@ static int solve_begin(Cg &c, const T *d, T *x, double rtol, double atol)
     CMT_LAUNCH_CHECK();
     k_begin_scalars<<<1, 1, 0, st>>>(sc, rtol, atol);
     CMT_LAUNCH_CHECK();
-    CMT_TRY(matvec_impl<T>(c, (const T *)c.x, (T *)c.q, false));
-    k_residual<T><<<g, 256, 0, st>>>((const T *)c.b, (const T *)c.q, (T *)c.r, c.m3);
-    CMT_LAUNCH_CHECK();
+    bool x0_zero = false;
+    if (c.op == 1) {
+        // the explicit pair's matvec is a full NUFFT pair over the points: skip it for a zero
+        // x0 as scipy does, at the price of one host round trip
+        k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.x, (const T *)c.x, c.m3, c.partial,
+                                                     &sc->ticket[3], &sc->pq);
+        CMT_LAUNCH_CHECK();
+        CMT_TRY_CUDA(cudaMemcpyAsync(c.host_sc, sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, st));
+        CMT_TRY_CUDA(cudaStreamSynchronize(st));
+        x0_zero = c.host_sc->pq == 0.0;
+    }
+    if (x0_zero) {
+        CMT_TRY_CUDA(cudaMemcpyAsync(c.r, c.b, bytes, cudaMemcpyDeviceToDevice, st));
+    } else {
+        CMT_TRY(matvec_impl<T>(c, (const T *)c.x, (T *)c.q, false));
+        k_residual<T><<<g, 256, 0, st>>>((const T *)c.b, (const T *)c.q, (T *)c.r, c.m3);
+        CMT_LAUNCH_CHECK();
+    }
     k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.r, (const T *)c.r, c.m3, c.partial, &sc->ticket[2],
                                                  &sc->rho);
     CMT_LAUNCH_CHECK();

@@ -1053,13 +1053,17 @@ __global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub
 
 // ------------------------------------------------------------------ table-driven fused pair
 
+// Per-warp table of k_pair_tab: 32 records of PAIR_REC values (x 8, y pairs 8, then z 8
+// and later (z c) pairs 16; padded so that the owner lanes' 16-byte record accesses fall in
+// distinct banks) and 32 rows of PAIR_PART values (8 complex partial sums, padded likewise).
+constexpr int PAIR_REC = 36, PAIR_PART = 20;
+
 // Shared-memory bytes of k_pair_tab: the two complex subgrids (G1 staged, G2 accumulated),
-// 16-byte aligned, then per warp a table of 32 records (32 values) and 32 x 8 complex
-// partial sums.
+// 16-byte aligned, then the per-warp tables.
 template <typename T>
 __host__ __device__ inline size_t pair_tab_smem(size_t subgrid_bytes, int warps)
 {
-    return ((4 * subgrid_bytes + 15) & ~(size_t)15) + warps * 32 * (32 + 16) * sizeof(T);
+    return ((4 * subgrid_bytes + 15) & ~(size_t)15) + warps * 32 * (PAIR_REC + PAIR_PART) * sizeof(T);
 }
 
 // Table-driven fused type-2 then type-1 pair on one subproblem (kernel width W <= 8): the
@@ -1079,7 +1083,7 @@ __device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_coun
                                              T *g2)
 {
     static_assert(W >= 2 && W <= 8, "table pair needs a window of at most 8 columns");
-    constexpr int EW = 8, BR = 4, RX = (W + BR - 1) / BR, REC = 32;
+    constexpr int EW = 8, BR = 4, RX = (W + BR - 1) / BR, REC = PAIR_REC;
     using T2 = typename cplx<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int S = gm.S, P = gm.P, h = W / 2, n = gm.n;
@@ -1088,8 +1092,8 @@ __device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_coun
     T *sb = sa + 2 * copy;
     const size_t sgb = ((size_t)4 * copy * sizeof(T) + 15) & ~(size_t)15;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    T *tab = reinterpret_cast<T *>(smem_raw + sgb) + warp * 32 * (REC + 16);
-    T *part = tab + 32 * REC;  // 32 points x 8 z lanes, (re, im)
+    T *tab = reinterpret_cast<T *>(smem_raw + sgb) + warp * 32 * (REC + PAIR_PART);
+    T *part = tab + 32 * REC;  // per point a row of PAIR_PART: 8 z lanes' (re, im) partials
     for (int i = threadIdx.x; i < 2 * copy; i += blockDim.x) sb[i] = T(0);
     load_subgrid<T, true>(g1, gm, b, sa);
     __syncthreads();
@@ -1186,15 +1190,15 @@ __device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_coun
                 sr += __shfl_xor_sync(0xffffffffu, sr, 16);
                 si += __shfl_xor_sync(0xffffffffu, si, 8);
                 si += __shfl_xor_sync(0xffffffffu, si, 16);
-                if (bl == 0) reinterpret_cast<T2 *>(part)[q * 8 + e] = T2{sr, si};
+                if (bl == 0) reinterpret_cast<T2 *>(part + q * PAIR_PART)[e] = T2{sr, si};
             }
         }
         __syncwarp();
         // ---- lane t: point t's value, folded into its record as (z c) pairs
         {
             T v[8], w2[8];
-            load8(part + lane * 16, v);
-            load8(part + lane * 16 + 8, w2);
+            load8(part + lane * PAIR_PART, v);
+            load8(part + lane * PAIR_PART + 8, w2);
             T cr = ((v[0] + v[2]) + (v[4] + v[6])) + ((w2[0] + w2[2]) + (w2[4] + w2[6]));
             T ci = ((v[1] + v[3]) + (v[5] + v[7])) + ((w2[1] + w2[3]) + (w2[5] + w2[7]));
             if (!valid) cr = ci = T(0);
