@@ -54,14 +54,23 @@ struct Plan {
 
 enum { PROF_SPREAD = 1, PROF_INTERP = 2, PROF_PAIR = 3 };
 
+// A launch is timed only outside stream capture (inside, an event record would become a
+// node of the captured graph instead of a timestamp of this launch).
+static inline bool prof_on(const Plan &p)
+{
+    if (!p.prof || p.nev >= Plan::PROF_CAP) return false;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(p.stream, &st) == cudaSuccess && st == cudaStreamCaptureStatusNone;
+}
+
 static inline void prof_begin(Plan &p)
 {
-    if (p.prof && p.nev < Plan::PROF_CAP) cudaEventRecord(p.ev[2 * p.nev], p.stream);
+    if (prof_on(p)) cudaEventRecord(p.ev[2 * p.nev], p.stream);
 }
 
 static inline void prof_end(Plan &p, int kind)
 {
-    if (p.prof && p.nev < Plan::PROF_CAP) {
+    if (prof_on(p)) {
         cudaEventRecord(p.ev[2 * p.nev + 1], p.stream);
         p.kind[p.nev++] = kind;
     }
