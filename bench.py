@@ -842,6 +842,11 @@ def align_split(torch, nf, alm, ppr, rext, img, acd, refs, n_pix):
         out[mode] = {"ms": t, "distance_tflops": tf, "tensor_flops_per_launch": flops,
                      "frac_of_sustained_bf16": tf / peaks["bf16_tflops_sustained"] if peaks["bf16_tflops_sustained"]
                      else None, "peak_source": peaks["source"]}
+        if mode == "bf16":
+            from cmtip_gb300 import tune
+            mt.profile(False)
+            tt = tune.autotune_match([mt], cache=False)
+            out[mode]["tile_table_ms"] = {f"{r['bn']}x{r['stages']}": round(r["ms"], 3) for r in tt["table"]}
         mt.close()
     torch.cuda.empty_cache()
     return out

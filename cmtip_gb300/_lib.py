@@ -83,6 +83,7 @@ SIGNATURES = {
     "cmt_match_run_many": [_i32, _vp, _vp, _vp, _vp, _vp, _vp],
     "cmt_match_profile": [_vp, _i32],
     "cmt_match_set_wait_limit": [_vp, _f64],
+    "cmt_match_set_tile": [_vp, _i32, _i32],
     "cmt_match_stall_loads": [_vp, _i32],
     "cmt_match_last_ms": [_vp, ctypes.POINTER(ctypes.c_float)],
     "cmt_match_stats": [_vp, ctypes.POINTER(_f64)],

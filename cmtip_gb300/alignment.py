@@ -110,6 +110,11 @@ class Matcher:
                   arr([o[3].data_ptr() for o in outs]), nn)
         return [o + (int(nn[i]),) for i, o in enumerate(outs)]
 
+    def set_tile(self, bn=256, stages=4):
+        """Tile of the tensor-core distance kernel (references per tile, TMA ring stages)."""
+        _lib.call("cmt_match_set_tile", self._h, int(bn), int(stages))
+        self.tile = (int(bn), int(stages))
+
     def set_wait_limit(self, seconds):
         """Limit of the tensor-core pipeline's bounded waits (a run that exceeds it raises
         CmtError with code CMT_ERR_TIMEOUT; the matcher and the context stay usable)."""

@@ -262,6 +262,9 @@ class BatchedReconstruction:
                     matchers[k].set_data(torch.as_tensor(x.images).cuda().reshape(-1, x.n_pix), self._weights[i])
                     matchers[k].set_refs(models[k].reshape(len(refs), x.n_pix))
                 if grouped:
+                    if self.tuning == "auto":
+                        from . import tune
+                        tune.autotune_match(matchers)
                     return Matcher.run_many(matchers)
                 return [mt.run() for mt in matchers]
             outs = self._timed("match_gemm_s", run)

@@ -291,14 +291,17 @@ __global__ void __launch_bounds__(256) k_dist_simt(const T *X, const T *Y, int n
 // ------------------------------------------------------------------ tcgen05 BF16 form
 
 constexpr int TC_BM = 128;   // images per tile (TMEM lanes)
-constexpr int TC_BN = 256;   // references per tile (TMEM columns per accumulator)
+constexpr int TC_BN = 256;   // default references per tile (TMEM columns per accumulator; 128 or 256)
 constexpr int TC_BK = 64;    // K per stage: one 128-byte swizzle row of bf16
-constexpr int TC_STAGES = 4;
+constexpr int TC_STAGES = 4;  // default TMA ring depth
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
 constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 constexpr int TC_THREADS = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-5 epilogue
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
+
+// shared memory of a (BN, STAGES) instantiation: the TMA ring, 1 KB alignment, barriers
+constexpr int tc_smem(int bn, int stages) { return stages * (TC_A_BYTES + bn * TC_BK * 2) + 1024 + 256; }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -444,21 +447,24 @@ __device__ __forceinline__ int problem_of(const TcGroup &g, long long u, int p)
 // of the concatenated unit list, balanced by cost on the host, keeps each image's running
 // top-k across the reference tiles in the epilogue threads' registers and writes it once
 // per image tile it touched.
+template <int BN, int STAGES>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant__ TcGroup g, int *err)
 {
+    constexpr int B_BYTES = BN * TC_BK * 2, STAGE_BYTES = TC_A_BYTES + B_BYTES;
+    constexpr uint32_t TMEM_COLS = 2 * BN;  // two accumulators of BN columns
     extern __shared__ unsigned char smem_raw[];
     uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     unsigned char *gbase = smem_raw + (base - smem_u32(smem_raw));
-    uint32_t sA0 = base, sB0 = base + TC_STAGES * TC_A_BYTES;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(gbase + TC_STAGES * TC_STAGE_BYTES);
+    uint32_t sA0 = base, sB0 = base + STAGES * TC_A_BYTES;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(gbase + STAGES * STAGE_BYTES);
     // bars: full[S], empty[S], accf[2], acce[2], drain
     uint32_t bar0 = smem_u32(bars);
     auto full_b = [&](int s) { return bar0 + 8u * s; };
-    auto empty_b = [&](int s) { return bar0 + 8u * (TC_STAGES + s); };
-    auto accf_b = [&](int b) { return bar0 + 8u * (2 * TC_STAGES + b); };
-    auto acce_b = [&](int b) { return bar0 + 8u * (2 * TC_STAGES + 2 + b); };
-    const uint32_t drain_b = bar0 + 8u * (2 * TC_STAGES + 4);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(gbase + TC_STAGES * TC_STAGE_BYTES + 8 * (2 * TC_STAGES + 5));
+    auto empty_b = [&](int s) { return bar0 + 8u * (STAGES + s); };
+    auto accf_b = [&](int b) { return bar0 + 8u * (2 * STAGES + b); };
+    auto acce_b = [&](int b) { return bar0 + 8u * (2 * STAGES + 2 + b); };
+    const uint32_t drain_b = bar0 + 8u * (2 * STAGES + 4);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(gbase + STAGES * STAGE_BYTES + 8 * (2 * STAGES + 5));
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -466,7 +472,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
     if (u0 >= u1) return;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < TC_STAGES; ++s) {
+        for (int s = 0; s < STAGES; ++s) {
             mbar_init(full_b(s), 1);
             mbar_init(empty_b(s), 1);
         }
@@ -481,7 +487,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(512));
+                     "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     tc_fence_before();
@@ -496,7 +502,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
             bool ok = true;
             int p = 0;
             unsigned used = 0;           // stages with a load issued
-            uint32_t used_ph[TC_STAGES];  // the phase of each stage's last load
+            uint32_t used_ph[STAGES];  // the phase of each stage's last load
             for (long long u = u0; u < u1 && ok && !g.stall_loads; ++u) {
                 p = problem_of(g, u, p);
                 const long long lu = u - g.p[p].ustart;
@@ -507,12 +513,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(full_b(s), TC_STAGE_BYTES);
+                    mbar_expect_tx(full_b(s), STAGE_BYTES);
                     tma_load_2d(sA0 + s * TC_A_BYTES, &g.tmA[p], full_b(s), kb * TC_BK, m * TC_BM);
-                    tma_load_2d(sB0 + s * TC_B_BYTES, &g.tmB[p], full_b(s), kb * TC_BK, t * TC_BN);
+                    tma_load_2d(sB0 + s * B_BYTES, &g.tmB[p], full_b(s), kb * TC_BK, t * BN);
                     used |= 1u << s;
                     used_ph[s] = ph;
-                    if (++s == TC_STAGES) {
+                    if (++s == STAGES) {
                         s = 0;
                         ph ^= 1;
                     }
@@ -521,14 +527,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
             // before the CTA can exit, every load this thread issued has landed (on the normal
             // path the MMA warp has already consumed them; after a timeout they may still be
             // in flight): a bounded wait per stage that does not stop on the abort flag
-            for (int st = 0; st < TC_STAGES; ++st)
+            for (int st = 0; st < STAGES; ++st)
                 if ((used >> st) & 1u)
                     if (!mbar_wait(full_b(st), used_ph[st], nullptr, g.wait_ns)) ok = false;
             if (!ok) atomicOr(err, 1);
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(TC_BM, TC_BN);
+            const uint32_t idesc = idesc_bf16(TC_BM, BN);
             int s = 0;
             uint32_t ph = 0;
             bool ok = true;
@@ -542,19 +548,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
                     break;
                 }
                 tc_fence_after();
-                uint32_t dt = tmem + (uint32_t)(b * TC_BN);
+                uint32_t dt = tmem + (uint32_t)(b * BN);
                 for (int kb = 0; kb < KB; ++kb) {
                     if (!mbar_wait(full_b(s), ph, abort_flag, g.wait_ns)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    uint64_t ad = sw128_desc(sA0 + s * TC_A_BYTES), bd = sw128_desc(sB0 + s * TC_B_BYTES);
+                    uint64_t ad = sw128_desc(sA0 + s * TC_A_BYTES), bd = sw128_desc(sB0 + s * B_BYTES);
 #pragma unroll
                     for (int k = 0; k < TC_BK / 16; ++k)
                         umma_bf16(dt, ad + 2 * k, bd + 2 * k, idesc, (kb | k) != 0);
                     umma_commit(empty_b(s));
-                    if (++s == TC_STAGES) {
+                    if (++s == STAGES) {
                         s = 0;
                         ph ^= 1;
                     }
@@ -615,10 +621,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
                 break;
             }
             tc_fence_after();
-            uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_BN);
-            const int rbase = t * TC_BN;
+            uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
+            const int rbase = t * BN;
 #pragma unroll 1
-            for (int c = 0; c < TC_BN / 32; ++c) {
+            for (int c = 0; c < BN / 32; ++c) {
                 uint32_t v[32];
                 tmem_ld32(tbase + c * 32, v);
 #pragma unroll
@@ -638,7 +644,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_dist_tc(const __grid_constant
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
 // ------------------------------------------------------------------ merge + exact re-scoring
@@ -826,6 +832,7 @@ struct Match {
     bool timed = false;
     cudaEvent_t ev[7] = {};
     double wait_s = 2.0;  // limit of the tensor-core pipeline's waits
+    int tile_bn = TC_BN, stages = TC_STAGES;  // reference tile and TMA ring depth (cmt_match_set_tile)
     int stall_loads = 0;  // test of the timeout path (cmt_match_stall_loads)
 };
 
@@ -922,15 +929,30 @@ static void row_stats(const Match &m, const void *v, int64_t rows, double *rsum,
 // costs its K blocks plus a constant for the epilogue), so instances of very different
 // size share the GPU in one launch.  si[i] receives matcher i's segment layout for
 // k_merge_rescore; the CTA ranges live in ms[0]->cta_u until its next launch.
+typedef void (*TcKernel)(TcGroup, int *);
+
+// the instantiations a matcher's tile may select: (references per tile, ring stages)
+static TcKernel tc_kernel(int bn, int stages)
+{
+    if (bn == 256 && stages == 4) return k_dist_tc<256, 4>;
+    if (bn == 256 && stages == 3) return k_dist_tc<256, 3>;
+    if (bn == 128 && stages == 6) return k_dist_tc<128, 6>;
+    if (bn == 128 && stages == 4) return k_dist_tc<128, 4>;
+    return nullptr;
+}
+
 static int tc_launch(int n, cmt_match *const *ms, cudaStream_t st, SegInfo *si)
 {
+    const int bn = ms[0]->tile_bn, stages = ms[0]->stages;
+    TcKernel kern = tc_kernel(bn, stages);
+    CMT_CHECK_ARG(kern, "no tensor-core kernel for a %d-reference tile with %d stages", bn, stages);
     std::vector<long long> ustart(n + 1, 0), unit_cost(n);
     std::vector<int> n_rt(n), n_it(n), KB(n);
     long long cost_total = 0;
     for (int i = 0; i < n; ++i) {
         const Match &m = *ms[i];
         n_it[i] = (int)((m.n_img + TC_BM - 1) / TC_BM);
-        n_rt[i] = (int)(m.n_ref_pad / TC_BN);
+        n_rt[i] = (int)(m.n_ref_pad / bn);
         KB[i] = (int)((int64_t)m.Kp * m.terms / TC_BK);
         unit_cost[i] = KB[i] + 16;
         const long long U = (long long)n_it[i] * n_rt[i];
@@ -982,7 +1004,7 @@ static int tc_launch(int n, cmt_match *const *ms, cudaStream_t st, SegInfo *si)
         m.cap_part = std::min(cap, cap2);
         const int64_t kld = (int64_t)m.Kp * m.terms;
         CMT_TRY(make_map(&g.tmA[i], m.opA, m.n_img, kld, TC_BM));
-        CMT_TRY(make_map(&g.tmB[i], m.opB, m.n_ref, kld, TC_BN));
+        CMT_TRY(make_map(&g.tmB[i], m.opB, m.n_ref, kld, bn));
         g.p[i] = TcProblem{ustart[i], n_rt[i], KB[i], maxseg, m.ca, m.cb, m.pscore, m.pidx};
         si[i] = SegInfo{};
         si[i].mode = 1;
@@ -993,9 +1015,10 @@ static int tc_launch(int n, cmt_match *const *ms, cudaStream_t st, SegInfo *si)
         si[i].maxseg = maxseg;
         si[i].cta_u = ms[0]->cta_u;
     }
-    CMT_TRY_CUDA(cudaFuncSetAttribute(k_dist_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    const int smem = tc_smem(bn, stages);
+    CMT_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CMT_TRY_CUDA(cudaMemsetAsync(ms[0]->err, 0, sizeof(int), st));
-    k_dist_tc<<<(unsigned)G, TC_THREADS, TC_SMEM, st>>>(g, ms[0]->err);
+    kern<<<(unsigned)G, TC_THREADS, smem, st>>>(g, ms[0]->err);
     CMT_LAUNCH_CHECK();
     return CMT_OK;
 }
@@ -1230,6 +1253,19 @@ extern "C" int cmt_match_stats(cmt_match *m, double *host_out)
 
 // Limit (seconds, 1e-3 .. 60) of every wait of the tensor-core pipeline; a wait that runs
 // out makes cmt_match_run return CMT_ERR_TIMEOUT with the context still usable.
+// Tile of the tensor-core kernel: references per tile (bn: 128 or 256) and TMA ring stages
+// (256: 3 or 4; 128: 4 or 6).  Picked by the autotuner; the default is 256 x 4.  A grouped
+// run (cmt_match_run_many) uses the first matcher's tile.
+extern "C" int cmt_match_set_tile(cmt_match *m, int bn, int stages)
+{
+    CMT_CHECK_ARG(m, "null matcher");
+    CMT_CHECK_ARG(tc_kernel(bn, stages), "tile %d x %d stages is not one of 256 x 4, 256 x 3, 128 x 6, 128 x 4", bn,
+                  stages);
+    m->tile_bn = bn;
+    m->stages = stages;
+    return CMT_OK;
+}
+
 extern "C" int cmt_match_set_wait_limit(cmt_match *m, double seconds)
 {
     CMT_CHECK_ARG(m, "null matcher");

@@ -1,4 +1,5 @@
-"""Autotuner of the NUFFT plans: bin size and points per subproblem.
+"""Autotuner of the NUFFT plans (bin size and points per subproblem) and of the tensor-core
+distance kernel (reference tile and TMA ring depth).
 
 The bin size sets the shared-memory subgrid of a subproblem ((bin_size + w)^3 cells, so the
 CTAs per SM) and, with the point density, how many points share a window; the points per
@@ -10,6 +11,11 @@ has reuse 1, a plan applied to many mode sets more).  Results are cached in memo
 a JSON file (``CMT_TUNE_CACHE``, default ``~/.cache/cmtip_gb300/tune.json``) keyed by GPU,
 library version and problem signature.  The reference has no counterpart: finufft chooses
 its own bins.
+
+The distance kernel's tile (``TILES``: references per tile 128 / 256, ring stages) trades
+per-unit epilogue work and the unit count (how evenly the persistent CTAs share the work)
+against shared memory for the TMA ring; ``autotune_match`` times each on the caller's
+matchers (one grouped launch), results being independent of the tile.
 """
 from __future__ import annotations
 
@@ -23,6 +29,7 @@ from . import _lib
 from .nufft import DEFAULT_EPS, Plan
 
 BIN_SIZES = (4, 5, 8, 16)
+TILES = ((256, 4), (256, 3), (128, 6), (128, 4))
 MAXSUBS = (2048, 4096, 8192, 16384)
 
 _mem = {}
@@ -125,3 +132,44 @@ def autotune(nufft_type, M, set_points, data, prec=32, eps=DEFAULT_EPS, isign=No
 def apply(plan: Plan, cfg) -> Plan:
     """Set a tuned configuration on a plan (before set_pts)."""
     return plan.set_tuning(int(cfg["bin_size"]), int(cfg["maxsub"]))
+
+
+def match_signature(matchers):
+    """Cache key of a distance problem: GPU, library version, form and power-of-two buckets of
+    the image and reference counts and of the pixel count of every matcher."""
+    dev = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
+    b = lambda v: max(0, int(v).bit_length() - 1)
+    shapes = ",".join(f"{b(m.n_img)}/{b(m.n_ref)}/{b(m.n_pix)}" for m in matchers)
+    return f"{dev}|{_lib.version()}|match|m{matchers[0].mode}|{shapes}"
+
+
+def autotune_match(matchers, tiles=TILES, cache=True, reps=2):
+    """Best tile for one grouped tensor-core launch over ``matchers`` (data and references
+    set): each candidate is timed by CUDA events over ``reps`` runs after a warm-up, and the
+    winner is left set on the matchers.  Returns dict(bn, stages, ms, table)."""
+    from .alignment import Matcher
+    matchers = list(matchers)
+    key = match_signature(matchers)
+    if cache:
+        with _lock:
+            hit = _mem.get(key) or _load_file().get(key)
+        if hit:
+            _mem[key] = hit
+            for m in matchers:
+                m.set_tile(hit["bn"], hit["stages"])
+            return dict(hit, cached=True)
+    table = []
+    for bn, st in tiles:
+        for m in matchers:
+            m.set_tile(bn, st)
+        ms = _time_ms(lambda: Matcher.run_many(matchers), reps)
+        table.append(dict(bn=bn, stages=st, ms=ms))
+    best = min(table, key=lambda r: r["ms"])
+    for m in matchers:
+        m.set_tile(best["bn"], best["stages"])
+    res = dict(bn=best["bn"], stages=best["stages"], ms=best["ms"], table=table)
+    if cache:
+        with _lock:
+            _mem[key] = res
+        _store_file(key, res)
+    return dict(res, cached=False)

@@ -256,6 +256,12 @@ int cmt_match_run(cmt_match *match, int *best_idx, double *best_d, double *secon
 int cmt_match_run_many(int n, cmt_match *const *ms, int *const *best_idx, double *const *best_d,
                        double *const *second_d, int *const *near_tie, int *n_near);
 
+/* Tile of the tensor-core distance kernel (modes 0 / 3): references per tile bn (128 or
+ * 256) and TMA ring stages (256: 3 or 4; 128: 4 or 6); default 256 x 4.  The autotuner
+ * (tune.autotune_match) picks it per problem size; results do not depend on it.  No
+ * counterpart in the reference. */
+int cmt_match_set_tile(cmt_match *match, int bn, int stages);
+
 /* Limit (seconds, 1e-3 .. 60; default 2) of every wait of the tensor-core pipeline.  A wait
  * that runs out unwinds the kernel (in-flight copies and MMAs drained, TMEM released) and
  * cmt_match_run returns CMT_ERR_TIMEOUT with the context still usable. */

@@ -199,3 +199,26 @@ def test_bounded_waits_time_out_and_recover(al):
     assert float(x.sum()) == 1000.0
     with pytest.raises(ValueError):
         mt.set_wait_limit(0.0)
+
+
+@pytest.mark.parametrize("mode", ["bf16", "bf16x3"])
+def test_tiles_give_the_same_result(al, mode, tmp_path, monkeypatch):
+    # every tile of the tensor-core kernel (references per tile, ring stages) gives the same
+    # candidates and re-scored result; the autotuner leaves a valid tile set
+    from cmtip_gb300 import tune
+    monkeypatch.setenv("CMT_TUNE_CACHE", str(tmp_path / "tune.json"))
+    g = torch.Generator(device="cuda").manual_seed(6)
+    mt = al.Matcher(1536, mode)
+    mt.set_data(torch.rand(400, 1536, device="cuda", generator=g), np.full(1536, 1.0 / 1536))
+    mt.set_refs(torch.rand(900, 1536, device="cuda", generator=g))
+    ref = [t.clone() if torch.is_tensor(t) else t for t in mt.run()]
+    for bn, st in tune.TILES:
+        mt.set_tile(bn, st)
+        got = mt.run()
+        for a, b in zip(ref[:4], got[:4]):
+            assert torch.equal(a, b), (bn, st)
+    res = tune.autotune_match([mt])
+    assert (res["bn"], res["stages"]) in tune.TILES and len(res["table"]) == len(tune.TILES)
+    assert tune.autotune_match([mt])["cached"]
+    with pytest.raises(ValueError):
+        mt.set_tile(64, 4)
