@@ -81,6 +81,7 @@ class Matcher:
         _lib.call("cmt_match_set_refs", self._h, m.shape[0], _ptr(m), int(nbatches))
         self._keep["model"] = m
         self.nbatches = int(nbatches)
+        self.n_ref = m.shape[0]
 
     def run(self):
         n = self.n_img
