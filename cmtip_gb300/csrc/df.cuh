@@ -73,4 +73,40 @@ __device__ __forceinline__ DF df_add_f(DF a, float b)
 
 __device__ __forceinline__ double df_to_double(DF a) { return (double)a.hi + (double)a.lo; }
 
+// float32 of the dot product of three double-float pairs (x = hi, y = lo), sum_c a_c b_c
+// (Ogita, Rump & Oishi 2005, "Accurate sum and dot product", algorithm Dot2 with the exact
+// product by FMA).  The products' leading parts p_c = fl(a.hi b.hi) are summed with TwoSum
+// (Knuth); their exact rounding errors, the cross terms a.hi b.lo + a.lo b.hi (a.lo b.lo,
+// below 2^-48 of the product, is dropped) and the two sums' errors are gathered in floats
+// and added last, so the one final rounding sees the dot product to about 2^-46 of the
+// products' size.
+__device__ __forceinline__ float df_dot3_to_float(float2 a0, float2 b0, float2 a1, float2 b1, float2 a2, float2 b2)
+{
+    const float p0 = __fmul_rn(a0.x, b0.x), p1 = __fmul_rn(a1.x, b1.x), p2 = __fmul_rn(a2.x, b2.x);
+    float e0 = __fmaf_rn(a0.x, b0.x, -p0);
+    e0 = __fmaf_rn(a0.x, b0.y, e0);
+    e0 = __fmaf_rn(a0.y, b0.x, e0);
+    float e1 = __fmaf_rn(a1.x, b1.x, -p1);
+    e1 = __fmaf_rn(a1.x, b1.y, e1);
+    e1 = __fmaf_rn(a1.y, b1.x, e1);
+    float e2 = __fmaf_rn(a2.x, b2.x, -p2);
+    e2 = __fmaf_rn(a2.x, b2.y, e2);
+    e2 = __fmaf_rn(a2.y, b2.x, e2);
+    const float s = __fadd_rn(p0, p1), bs = __fsub_rn(s, p0);
+    float err = __fadd_rn(__fsub_rn(p0, __fsub_rn(s, bs)), __fsub_rn(p1, bs));
+    const float s2 = __fadd_rn(s, p2), bs2 = __fsub_rn(s2, s);
+    err = __fadd_rn(err, __fadd_rn(__fsub_rn(s, __fsub_rn(s2, bs2)), __fsub_rn(p2, bs2)));
+    return __fadd_rn(s2, __fadd_rn(err, __fadd_rn(__fadd_rn(e0, e1), e2)));
+}
+
+// float32 of x (s.x + s.y) for a float x and a double-float s: the exact product's leading
+// part plus its rounding error and the low-part term, rounded once
+__device__ __forceinline__ float df_scale_to_float(float x, float2 s)
+{
+    const float p = __fmul_rn(x, s.x);
+    float e = __fmaf_rn(x, s.x, -p);
+    e = __fmaf_rn(x, s.y, e);
+    return __fadd_rn(p, e);
+}
+
 }  // namespace cmt

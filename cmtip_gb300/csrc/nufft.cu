@@ -117,13 +117,13 @@ __device__ __forceinline__ void cell_and_frac(T x, T s_hi, T s_lo, int n, int &c
     int c = (int)fp;
     if (f >= T(1)) { f -= T(1); c += 1; }
     if (f < T(0)) { f += T(1); c -= 1; }
-    // c mod n: two corrections cover [-n, 2n) (|x| < pi); the division only beyond
-    if (c < 0) c += n;
-    if (c >= n) c -= n;
-    if ((unsigned)c >= (unsigned)n) {
-        c %= n;
-        if (c < 0) c += n;
-    }
+    // c mod n, branch-free: k_bin_count calls this only for |x| < 3 pi, where c lies in
+    // [-1.5 n - 2, 1.5 n + 1], inside the [-2n, 3n) that two corrections each way cover
+    // (n >= 2w >= 4)
+    c += n & -(int)(c < 0);
+    c += n & -(int)(c < 0);
+    c -= n & -(int)(c >= n);
+    c -= n & -(int)(c >= n);
     cell = c;
     frac = f;
 }
@@ -177,23 +177,20 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
         py = y[j];
         pz = z[j];
     } else if (sizeof(T) == 4) {
-        // the chain below in double-float: H = inv(R) . p, float32(H), * (pi / extent), with
-        // the rotations and q-vectors pre-split into (hi, lo) float pairs
+        // the chain below at FP32 throughput: float32(H) of H = inv(R) . p by a compensated
+        // dot product, then float32(H) * (pi / extent), with the rotations, q-vectors and
+        // pi / extent pre-split into (hi, lo) float pairs; both results are rounded once from
+        // values within ~2^-46 of the exact ones, so they equal the float64 chain's roundings
+        // except where that chain's value lies within ~2^-46 of a float32 rounding boundary
         // N < 2^31 (set_pts_impl), so 32-bit index arithmetic
         unsigned img, pix;
         img_pix(j, q, img, pix);
         const float2 *R = q.rot_df + 9 * img;
-        float2 a0 = q.ppr_df[pix], a1 = q.ppr_df[q.n_pix + pix], a2 = q.ppr_df[2 * q.n_pix + pix];
-        DF p0{a0.x, a0.y}, p1{a1.x, a1.y}, p2{a2.x, a2.y};
-        DF s{q.scale_df.x, q.scale_df.y};
+        const float2 a0 = q.ppr_df[pix], a1 = q.ppr_df[q.n_pix + pix], a2 = q.ppr_df[2 * q.n_pix + pix];
         float o[3];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            float2 r0 = R[3 * r], r1 = R[3 * r + 1], r2 = R[3 * r + 2];
-            DF h = df_add(df_add(df_mul(DF{r0.x, r0.y}, p0), df_mul(DF{r1.x, r1.y}, p1)), df_mul(DF{r2.x, r2.y}, p2));
-            DF hf{df_to_float(h), 0.0f};
-            o[r] = df_to_float(df_mul(hf, s));
-        }
+        for (int r = 0; r < 3; ++r)
+            o[r] = df_scale_to_float(df_dot3_to_float(R[3 * r], a0, R[3 * r + 1], a1, R[3 * r + 2], a2), q.scale_df);
         px = (T)o[0];
         py = (T)o[1];
         pz = (T)o[2];
@@ -382,6 +379,105 @@ __global__ void k_bin_scatter(int64_t N, const PtRec<T> *rec, const int *start, 
     }
 }
 
+// Pass 2 for FP32 plans, tile by tile: a CTA groups a tile of SCAT_TILE records (caller
+// order) by key in a shared-memory hash table, reserves each key's share of its sorted range
+// with one atomic per key and tile, and writes the tile's records of a key to consecutive
+// positions.  Caller order is image by image along detector rows, so a tile holds an
+// image's points of a window origin (about a dozen) together: each key receives them as
+// one contiguous run instead of one run per warp, which L2 merges into full sectors
+// before they reach DRAM.  Same output as k_bin_scatter up to the order within a key.
+constexpr int SCAT_THREADS = 256, SCAT_PER = 8, SCAT_TILE = SCAT_THREADS * SCAT_PER, SCAT_SLOTS = 2 * SCAT_TILE;
+static_assert(SCAT_SLOTS <= 4096 && SCAT_TILE <= 4096, "slot and rank are packed in 12 bits each");
+
+__global__ void __launch_bounds__(SCAT_THREADS, 4) k_bin_scatter_tiled(int64_t N, const PtRec<float> *rec,
+                                                                   const int *start, int *next,
+                                                                   SortedRec<float> *out, int *flag)
+{
+    __shared__ int hkey[SCAT_SLOTS];   // key of a slot, -1 empty
+    __shared__ int hval[SCAT_SLOTS];   // the key's count in the tile, then its first position
+    __shared__ short used[SCAT_TILE];  // slots taken in this tile
+    __shared__ int n_used;
+    const int lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < SCAT_SLOTS; i += blockDim.x) {
+        hkey[i] = -1;
+        hval[i] = 0;
+    }
+    if (threadIdx.x == 0) n_used = 0;
+    __syncthreads();
+    for (int64_t t0 = (int64_t)blockIdx.x * SCAT_TILE; t0 < N; t0 += (int64_t)gridDim.x * SCAT_TILE) {
+        float4 r[SCAT_PER];
+        int key[SCAT_PER], sr[SCAT_PER];  // sr: slot | rank << 12 (both < 4096), -1 without a key
+#pragma unroll
+        for (int k = 0; k < SCAT_PER; ++k) {
+            const int64_t j = t0 + k * SCAT_THREADS + threadIdx.x;
+            key[k] = -1;
+            if (j < N) {
+                r[k] = *reinterpret_cast<const float4 *>(rec + j);
+                key[k] = __float_as_int(r[k].x);
+            }
+        }
+        // group: the leader of each warp-level group of equal keys finds or takes the key's
+        // slot (linear probing; a tile has at most SCAT_TILE keys in 2 x SCAT_TILE slots, so
+        // a free slot is always found) and takes the group's ranks
+#pragma unroll
+        for (int k = 0; k < SCAT_PER; ++k) {
+            const unsigned peers = __match_any_sync(0xffffffffu, key[k]);
+            const int leader = __ffs(peers) - 1;
+            int sl = 0, base = 0;
+            if (key[k] >= 0 && lane == leader) {
+                sl = (int)(((unsigned)key[k] * 2654435761u) >> 20) & (SCAT_SLOTS - 1);
+                for (int probe = 0; probe < SCAT_SLOTS; ++probe) {
+                    const int prev = atomicCAS(&hkey[sl], -1, key[k]);
+                    if (prev == -1) {
+                        used[atomicAdd(&n_used, 1)] = (short)sl;
+                        break;
+                    }
+                    if (prev == key[k]) break;
+                    sl = (sl + 1) & (SCAT_SLOTS - 1);
+                }
+                base = atomicAdd(&hval[sl], __popc(peers));
+            }
+            sl = __shfl_sync(0xffffffffu, sl, leader);
+            base = __shfl_sync(0xffffffffu, base, leader) + __popc(peers & lanemask_lt());
+            sr[k] = key[k] >= 0 ? sl | base << 12 : -1;
+        }
+        __syncthreads();
+        // reserve each key's run: one global atomic per key of the tile
+        const int nu = n_used;
+        for (int u = threadIdx.x; u < nu; u += blockDim.x) {
+            const int sl = used[u], k = hkey[sl], c = hval[sl];
+            const int first = atomicAdd(&next[k], c);
+            if (first + c > start[k + 1]) {  // counts and keys disagree: never write out of the key's range
+                atomicOr(flag, 2);
+                hval[sl] = -1;
+            } else {
+                hval[sl] = first;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SCAT_PER; ++k) {
+            if (sr[k] < 0) continue;
+            const int first = hval[sr[k] & (SCAT_SLOTS - 1)];
+            if (first < 0) continue;
+            SortedRec<float> o;
+            o.x = r[k].y;
+            o.y = r[k].z;
+            o.z = r[k].w;
+            o.perm = (int)(t0 + k * SCAT_THREADS + threadIdx.x);
+            out[first + (sr[k] >> 12)] = o;
+        }
+        __syncthreads();
+        for (int u = threadIdx.x; u < nu; u += blockDim.x) {
+            const int sl = used[u];
+            hkey[sl] = -1;
+            hval[sl] = 0;
+        }
+        if (threadIdx.x == 0) n_used = 0;
+        __syncthreads();
+    }
+}
+
 // Records -> the plan's coordinate and permutation arrays without reordering (plans whose
 // subproblem sort does not fit in shared memory).
 template <typename T>
@@ -534,6 +630,108 @@ __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin
             uy_o[dst] = r.y;
             uz_o[dst] = r.z;
         }
+    }
+}
+
+// k_subsort for FP32 plans whose global passes ordered every bin by its full window origin
+// (fine_sort 4): the CTA walks its subproblem in chunks of SUBSORT_PER records per thread,
+// held in registers, so each record is read from memory once (k_subsort reads it twice,
+// once for the counts and once for the scatter).  The input is in origin order, so a
+// chunk's keys span only the origins between its first and last record: that range of
+// counters is cleared and scanned per chunk.  Sorting chunk by chunk keeps the origin
+// order; an origin whose points straddle a chunk boundary has its refinement classes in
+// two runs (the earlier chunk's part first), which the spreading kernels treat as two
+// runs of one window.  The sorted chunk is assembled in shared memory and then written to
+// the four output arrays in order, so every warp store is one contiguous 128-byte line
+// (scattered 4-byte stores straight to the arrays are bound by L2 sector writes).
+constexpr int SUBSORT_PER = 8, SUBSORT_THREADS = 256, SUBSORT_CHUNK = SUBSORT_PER * SUBSORT_THREADS;
+
+__global__ void __launch_bounds__(SUBSORT_THREADS, 4)
+    k_subsort_chunked(const int *sub_bin, const int *sub_off, const int *bin_count, const int *bin_start, int w,
+                      int bs, int maxsub, int nsk, const SortedRec<float> *in, int *perm_o, float *ux_o,
+                      float *uy_o, float *uz_o)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *stage = reinterpret_cast<float4 *>(smem_raw);                   // SUBSORT_CHUNK records
+    int *cnt_s = reinterpret_cast<int *>(smem_raw + SUBSORT_CHUNK * 16);  // nsk counters, indexed key - lo
+    __shared__ int sh[32];
+    __shared__ int range[2];
+    const int b = sub_bin[blockIdx.x];
+    const int off = sub_off[blockIdx.x];
+    const int cnt = min(maxsub, bin_count[b] - off);
+    const int p0 = bin_start[b] + off;
+    const int lane = threadIdx.x & 31;
+    const int chunk = SUBSORT_CHUNK;  // blockDim.x == SUBSORT_THREADS
+    for (int c0 = 0; c0 < cnt; c0 += chunk) {
+        const int n = min(chunk, cnt - c0);
+        const SortedRec<float> *src = in + p0 + c0;
+        float4 r[SUBSORT_PER];
+        int key[SUBSORT_PER];
+        int kmin = 0x7fffffff, kmax = -1;
+#pragma unroll
+        for (int k = 0; k < SUBSORT_PER; ++k) {
+            const int i = k * blockDim.x + threadIdx.x;
+            key[k] = -1;
+            if (i < n) {
+                r[k] = __ldcs(reinterpret_cast<const float4 *>(src + i));  // read once: evict first
+                key[k] = (int)point_key<float>(0, r[k].x, r[k].y, r[k].z, w, bs, 1);  // in [0, nsk)
+                kmin = min(kmin, key[k]);
+                kmax = max(kmax, key[k]);
+            }
+        }
+        if (threadIdx.x == 0) {
+            range[0] = 0x7fffffff;
+            range[1] = -1;
+        }
+        __syncthreads();  // also: the previous chunk's scatter is done with cnt_s
+        kmin = __reduce_min_sync(0xffffffffu, kmin);
+        kmax = __reduce_max_sync(0xffffffffu, kmax);
+        if (lane == 0 && kmax >= 0) {
+            atomicMin(&range[0], kmin);
+            atomicMax(&range[1], kmax);
+        }
+        __syncthreads();
+        const int lo = range[0], nr = range[1] - range[0] + 1;  // n >= 1: 1 <= nr <= nsk
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) cnt_s[i] = 0;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SUBSORT_PER; ++k) {
+            const unsigned peers = __match_any_sync(0xffffffffu, key[k]);
+            if (key[k] >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt_s[key[k] - lo], __popc(peers));
+        }
+        __syncthreads();
+        const int per = (nr + blockDim.x - 1) / blockDim.x;
+        const int a0 = min((int)threadIdx.x * per, nr), a1 = min(a0 + per, nr);
+        int s = 0;
+        for (int i = a0; i < a1; ++i) s += cnt_s[i];
+        int total;
+        int run = block_exclusive_scan(s, sh, total);
+        for (int i = a0; i < a1; ++i) {
+            const int c = cnt_s[i];
+            cnt_s[i] = run;
+            run += c;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SUBSORT_PER; ++k) {
+            const unsigned peers = __match_any_sync(0xffffffffu, key[k]);
+            const int leader = __ffs(peers) - 1;
+            int base = 0;
+            if (key[k] >= 0 && lane == leader) base = atomicAdd(&cnt_s[key[k] - lo], __popc(peers));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (key[k] >= 0) stage[base + __popc(peers & lanemask_lt())] = r[k];  // < n
+        }
+        __syncthreads();
+        float *const ux_c = ux_o + p0 + c0, *const uy_c = uy_o + p0 + c0, *const uz_c = uz_o + p0 + c0;
+        int *const perm_c = perm_o + p0 + c0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const float4 v = stage[i];
+            ux_c[i] = v.x;
+            uy_c[i] = v.y;
+            uz_c[i] = v.z;
+            perm_c[i] = __float_as_int(v.w);
+        }
+        // the next chunk's first barrier orders these reads of `stage` before its writes
     }
 }
 
@@ -1029,12 +1227,24 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     // pass 2: scatter, key_next starting at each key's first position
     CMT_TRY_CUDA(cudaMemcpyAsync(p.key_next, p.key_start, sizeof(int) * (nkeys + 1), cudaMemcpyDeviceToDevice, st));
     SortedRec<T> *srec = reinterpret_cast<SortedRec<T> *>(p.pts_block);
-    k_bin_scatter<T><<<g, 256, 0, st>>>(N, (const PtRec<T> *)scratch, p.key_start, p.key_next, srec, p.dflag);
+    if (sizeof(T) == 4)
+        k_bin_scatter_tiled<<<(unsigned)std::min<int64_t>(ceil_div(N, (int64_t)SCAT_TILE), 152 * 8), SCAT_THREADS, 0,
+                              st>>>(N, reinterpret_cast<const PtRec<float> *>(scratch), p.key_start, p.key_next,
+                                    reinterpret_cast<SortedRec<float> *>(srec), p.dflag);
+    else
+        k_bin_scatter<T><<<g, 256, 0, st>>>(N, (const PtRec<T> *)scratch, p.key_start, p.key_next, srec, p.dflag);
     CMT_LAUNCH_CHECK();
     {
         Plan o = p;
         set_pts_pointers<T>(o, scratch, N);
-        if (do_subsort && p.nsub > 0) {
+        const int csm = SUBSORT_CHUNK * 16 + nsk * (int)sizeof(int);
+        if (do_subsort && p.nsub > 0 && sizeof(T) == 4 && fine_sort == 4 && csm <= 200 * 1024) {
+            CMT_TRY(prep_smem(k_subsort_chunked, csm));
+            k_subsort_chunked<<<(unsigned)p.nsub, SUBSORT_THREADS, csm, st>>>(
+                p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.w, p.bs, p.maxsub, nsk,
+                reinterpret_cast<const SortedRec<float> *>(srec), o.perm, (float *)o.ux, (float *)o.uy,
+                (float *)o.uz);
+        } else if (do_subsort && p.nsub > 0) {
             CMT_TRY(prep_smem(k_subsort<T>, sub_smem));
             k_subsort<T><<<(unsigned)p.nsub, 512, sub_smem, st>>>(p.sub_bin, p.sub_off, p.bin_count, p.bin_start,
                                                                   p.w, p.bs, p.maxsub, nsk, srec, o.perm, (T *)o.ux,

@@ -155,6 +155,37 @@ def test_quaternion_points_match_reference_chain(nf):
     assert np.allclose(inv, np.linalg.inv(geometry.quaternion2rot3d(quats)), rtol=0, atol=1e-15)
 
 
+def test_quaternion_coordinates_equal_float64_chain(nf):
+    # An FP32 plan's quaternion points evaluate the float64 chain float32(inv(R) . p), then
+    # / extent * pi, at FP32 throughput (a compensated dot product).  A type-2 output depends
+    # only on its point's coordinates, so against the same plan fed the float64 chain's
+    # float32 coordinates the outputs are bit-equal wherever the coordinates are; the two
+    # may differ only for a value within ~2^-46 of a float32 rounding boundary (about one
+    # coordinate in 10^7).
+    from cmtip_gb300 import geometry
+    rng = np.random.default_rng(8)
+    ppr, rext = geometry.ewald_detector(64)
+    rext = rext / 0.9
+    quats = geometry.random_quaternions(64, rng).astype(np.float32)
+    inv = nf.inverse_rotations(quats)
+    R = inv.cpu().numpy().reshape(-1, 3, 3)
+    pp = ppr.reshape(3, -1)
+    xs = [np.ascontiguousarray(((R[:, r, 0, None] * pp[0] + R[:, r, 1, None] * pp[1]) + R[:, r, 2, None] * pp[2])
+                               .astype(np.float32).astype(np.float64).ravel() / rext * np.pi).astype(np.float32)
+          for r in range(3)]
+    M = 41
+    f = torch.from_numpy(rng.standard_normal((M,) * 3).astype(np.float32)).cuda()
+    p = nf.Plan(2, M, isign=-1)
+    p.set_pts(*(torch.from_numpy(a).cuda() for a in xs))
+    ref = p.execute(f, real_out=True).cpu().numpy()
+    p.set_pts_quat(inv, torch.from_numpy(pp).cuda(), rext)
+    got = p.execute(f, real_out=True).cpu().numpy()
+    p.close()
+    assert got.size == 64 * pp.shape[1]
+    assert np.count_nonzero(got != ref) <= 8
+    assert rel_l2(got, ref) < 1e-6
+
+
 @pytest.mark.parametrize("prec", [32, 64])
 def test_derived_plan_on_twice_finer_grid(nf, prec):
     # the 2M-mode plan borrowing an M-mode plan's sorted points equals an independent plan
@@ -171,6 +202,9 @@ def test_derived_plan_on_twice_finer_grid(nf, prec):
     assert rel_l2(got.cpu().numpy(), 0.5 * np.fft.ifftshift(ref.real)) < tol
     assert rel_l2(d.execute(None, real_out=True).cpu().numpy(),
                   on.type1(x, y, z, np.ones(N), 2 * M, eps=1e-13).real) < tol
+    # complex strengths through the extended window as well
+    cc = c + 1j * rng.standard_normal(N)
+    assert rel_l2(d.execute(torch.from_numpy(cc)).cpu().numpy(), on.type1(x, y, z, cc, 2 * M, eps=1e-13)) < tol
     # new points on the source are followed by the derived plan
     x2 = x[::-1].copy()
     src.set_pts(*(torch.from_numpy(a) for a in (x2, y, z)))
