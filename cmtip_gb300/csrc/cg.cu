@@ -13,7 +13,11 @@
 // autocorrelation.py:239): no preconditioner, convergence test ||r|| < max(atol, rtol ||b||)
 // at the top of each iteration, r0 = b - W x0 only if x0 has a nonzero entry.  Vectors
 // live in the solver precision (float for the mixed form, double for the FP64 form);
-// every inner product, residual norm and the alpha/beta scalars are FP64.  One iteration
+// every inner product and residual norm is accumulated to FP64 accuracy and the alpha/beta
+// scalars are FP64.  With float vectors the per-element work stays in FP32 error-free
+// arithmetic (compensated dot products, Dot2, per thread, then FP64 across threads; vector
+// updates x + alpha p rounded once from their exact value), since GB300 runs FP64 at a small
+// fraction of its FP32 rate.  One iteration
 // is a fixed launch sequence with no host synchronisation, so it is captured once into a
 // CUDA graph and replayed; a device-side flag turns the updates into no-ops after
 // convergence.
@@ -25,17 +29,19 @@
 #include <vector>
 
 #include "cmt_common.cuh"
+#include "df.cuh"
 
 namespace cmt {
 
 struct CgScalars {
-    double rho, rho_prev, pq, alpha, atol, bnorm;
+    double rho, rho_prev, pq, alpha, atol, bnorm, beta;
+    float alpha_hi, alpha_lo, beta_hi, beta_lo;  // alpha, beta as float pairs (float vectors' updates)
     int it, done;
     unsigned ticket[4];
 };
 
 constexpr int RED_THREADS = 256;
-constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
+constexpr int RED_BLOCKS = 1216;  // 8 x 152 SMs (a few elements per thread; no per-thread FP64 work)
 
 struct Cg {
     int M = 0, prec = 32, op = 0;  // op 0 Toeplitz, 1 explicit pair
@@ -45,17 +51,26 @@ struct Cg {
     // device buffers
     void *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *b = nullptr;
     void *sx = nullptr, *pad = nullptr, *conv = nullptr, *spec = nullptr, *spec2 = nullptr, *reg = nullptr;
+    void *spec_in = nullptr;  // (2M)x(2M)x(M+1) complex: 2D transforms of the M data slices, zero beyond
     void *kern_hat = nullptr;  // (2M)x(2M)x(M+1) complex: FFT of T / (2M)^3
     void *mask_hat = nullptr;  // M x M x (M/2+1) real: Hermitian part of ifftshift(antisupport) / M^3
     float *support = nullptr;  // M^3
     double *partial = nullptr;
     CgScalars *sc = nullptr;
     CgScalars *host_sc = nullptr;  // pinned host copy of sc, read after a solve
-    cufftHandle r2c_big = 0, c2r_big = 0, r2c_small = 0, c2r_small = 0;
+    // (2M)^3 convolution of a vector padded into the [0, M)^3 corner, pruned to the slices
+    // that hold data: 2D R2C of the first M slices (r2c_2d), the 1D transform along the
+    // slice axis of all (2M)x(M+1) columns (c2c_x, both directions), 2D C2R back to the
+    // first M slices (c2r_2d).  r2c_big (the full 3D R2C) transforms the Toeplitz kernel.
+    cufftHandle r2c_big = 0, r2c_2d = 0, c2c_x = 0, c2r_2d = 0, r2c_small = 0, c2r_small = 0;
     bool have_big = false, have_small = false;
     cmt_plan *pair_plan = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaStream_t cap_stream = nullptr;  // private stream the iteration is captured on
+    // the Fourier-regulariser branch of the Toeplitz matvec runs on a side stream, beside
+    // the (2M)^3 convolution (fork / join events; inside a capture they become graph edges)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool ready = false;
 };
 
@@ -71,18 +86,48 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// Sum of the block's compensated float pairs: the warps combine their (s, c) pairs in FP32
+// (TwoSum of the leading parts, the errors added to c), thread 0 adds the warps' pairs in
+// FP64.  Keeps the FP64 work to one thread per block.
+__device__ __forceinline__ double block_sum_dot2(Dot2 d)
+{
+    __shared__ float ss[RED_THREADS / 32], cs[RED_THREADS / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_down_sync(0xffffffffu, d.s, o), c2 = __shfl_down_sync(0xffffffffu, d.c, o);
+        const float s = __fadd_rn(d.s, s2), bs = __fsub_rn(s, d.s);
+        const float e = __fadd_rn(__fsub_rn(d.s, __fsub_rn(s, bs)), __fsub_rn(s2, bs));
+        d.s = s;
+        d.c = __fadd_rn(__fadd_rn(d.c, c2), e);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        ss[threadIdx.x >> 5] = d.s;
+        cs[threadIdx.x >> 5] = d.c;
+    }
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < RED_THREADS / 32; ++i) t += (double)ss[i] + (double)cs[i];
+    return t;  // in thread 0
+}
+
 // Block partial of a sum; the last block to finish reduces all partials in a fixed
 // order (deterministic) and returns true in thread 0 with the total in *out.
-__device__ bool block_reduce_last(double v, double *partial, unsigned *ticket, double *out)
+// With block_total, v in thread 0 already holds the block's sum (block_sum_dot2).
+__device__ bool block_reduce_last(double v, double *partial, unsigned *ticket, double *out, bool block_total = false)
 {
     __shared__ double s[RED_THREADS / 32];
     __shared__ bool last;
-    v = warp_sum(v);
-    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
-    __syncthreads();
+    if (!block_total) {
+        v = warp_sum(v);
+        if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+        __syncthreads();
+    }
     if (threadIdx.x < 32) {
-        double t = threadIdx.x < RED_THREADS / 32 ? s[threadIdx.x] : 0.0;
-        t = warp_sum(t);
+        double t = v;
+        if (!block_total) {
+            t = threadIdx.x < RED_THREADS / 32 ? s[threadIdx.x] : 0.0;
+            t = warp_sum(t);
+        }
         if (threadIdx.x == 0) {
             partial[blockIdx.x] = t;
             __threadfence();
@@ -114,33 +159,64 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot(const T *a, const T *b, int
                                                      unsigned *ticket, double *out)
 {
     double v = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        v += (double)a[i] * (double)b[i];
-    block_reduce_last(v, partial, ticket, out);
+    Dot2 v2{0.f, 0.f};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if constexpr (sizeof(T) == 4)
+            dot2_add(v2, a[i], b[i]);
+        else
+            v += (double)a[i] * (double)b[i];
+    }
+    if constexpr (sizeof(T) == 4)
+        block_reduce_last(block_sum_dot2(v2), partial, ticket, out, true);
+    else
+        block_reduce_last(v, partial, ticket, out);
 }
 
-// Start of an iteration: convergence test, p = r (+ beta p), S p into the padded corner
-// (Toeplitz) and into the M^3 buffer for the Fourier regulariser.
-template <typename T>
-__global__ void k_iter_begin(CgScalars *sc, const T *r, T *p, const float *support, int M, int use_pad, T *pad,
-                             T *sx)
+// scipy's convergence test before the next iteration and that iteration's beta, once rho
+// has changed (the start of a solve, the end of an iteration); one thread, FP64.
+__device__ void next_step_scalars(CgScalars *sc)
 {
     if (sc->done) return;
-    double rho = sc->rho;
-    if (sqrt(rho) < sc->atol) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
+    if (sqrt(sc->rho) < sc->atol) {
+        sc->done = 1;
         return;
     }
-    int64_t m3 = (int64_t)M * M * M;
-    double beta = sc->it > 0 ? rho / sc->rho_prev : 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += (int64_t)gridDim.x * blockDim.x) {
-        T pv = sc->it > 0 ? (T)((double)r[i] + beta * (double)p[i]) : r[i];
+    const double beta = sc->it > 0 ? sc->rho / sc->rho_prev : 0.0;
+    sc->beta = beta;
+    sc->beta_hi = (float)beta;
+    sc->beta_lo = (float)(beta - (double)(float)beta);
+}
+
+__global__ void k_next_step(CgScalars *sc) { next_step_scalars(sc); }
+
+// Start of an iteration: p = r (+ beta p), S p into the padded corner (Toeplitz) and into the
+// M^3 buffer for the Fourier regulariser; the convergence test and beta were evaluated when
+// rho last changed (next_step_scalars).  With float vectors, p = r + beta p is the FP64 value
+// rounded to float, computed in float error-free arithmetic (axpy_rn): GB300's FP64 pipe runs
+// at a small fraction of its FP32 rate.  Indices fit 32 bits ((2M)^3 <= 2^30).
+template <typename T>
+__global__ void k_iter_begin(CgScalars *sc, const T *__restrict__ r, T *__restrict__ p,
+                             const float *__restrict__ support, int M, int use_pad, T *__restrict__ pad,
+                             T *__restrict__ sx)
+{
+    if (sc->done) return;
+    const bool first = sc->it == 0;
+    const float bh = sc->beta_hi, bl = sc->beta_lo;
+    const int m3 = M * M * M, mm = M * M, M2 = 2 * M;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += gridDim.x * blockDim.x) {
+        T pv;
+        if (first) {
+            pv = r[i];
+        } else if constexpr (sizeof(T) == 4) {
+            pv = axpy_rn(r[i], bh, bl, p[i]);
+        } else {
+            pv = (T)((double)r[i] + sc->beta * (double)p[i]);
+        }
         p[i] = pv;
-        T v = pv * (T)support[i];
+        const T v = pv * (T)support[i];
         sx[i] = v;
         if (use_pad) {
-            int64_t a = i / ((int64_t)M * M), rem = i - a * M * M, bb = rem / M, c = rem - bb * M;
-            int64_t M2 = 2 * M;
+            const int a = i / mm, rem = i - a * mm, bb = rem / M, c = rem - bb * M;
             pad[(a * M2 + bb) * M2 + c] = v;
         }
     }
@@ -150,13 +226,12 @@ __global__ void k_iter_begin(CgScalars *sc, const T *r, T *p, const float *suppo
 template <typename T>
 __global__ void k_apply_support(const T *v, const float *support, int M, int use_pad, T *pad, T *sx)
 {
-    int64_t m3 = (int64_t)M * M * M;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += (int64_t)gridDim.x * blockDim.x) {
+    const int m3 = M * M * M, mm = M * M, M2 = 2 * M;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += gridDim.x * blockDim.x) {
         T s = v[i] * (T)support[i];
         sx[i] = s;
         if (use_pad) {
-            int64_t a = i / ((int64_t)M * M), rem = i - a * M * M, bb = rem / M, c = rem - bb * M;
-            int64_t M2 = 2 * M;
+            const int a = i / mm, rem = i - a * mm, bb = rem / M, c = rem - bb * M;
             pad[(a * M2 + bb) * M2 + c] = s;
         }
     }
@@ -184,57 +259,79 @@ __global__ void k_mul_real(cplx_t<T> *a, const T *m, int64_t n, const CgScalars 
 }
 
 // q = a S conv + r v + f S reg; conv read from the (2M)^3 corner (stride 2M) or an M^3 grid.
-// With dot: pq = v . q -> alpha = rho / pq.
+// With dot: pq = v . q -> alpha = rho / pq (float vectors: per-thread compensated sums, Dot2,
+// then FP64 across threads).
 template <typename T>
-__global__ void __launch_bounds__(RED_THREADS) k_combine(CgScalars *sc, const T *v, const T *conv, int conv_pad,
-                                                         const T *reg, const float *support, int M, double al,
-                                                         double rl, double fl, T *q, int with_dot, double *partial)
+__global__ void __launch_bounds__(RED_THREADS)
+    k_combine(CgScalars *sc, const T *__restrict__ v, const T *__restrict__ conv, int conv_pad,
+              const T *__restrict__ reg, const float *__restrict__ support, int M, T al, T rl, T fl,
+              T *__restrict__ q, int with_dot, double *partial)
 {
     if (with_dot && sc->done) return;
-    int64_t m3 = (int64_t)M * M * M;
+    const int m3 = M * M * M, mm = M * M, M2 = 2 * M;
     double acc = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += (int64_t)gridDim.x * blockDim.x) {
+    Dot2 acc2{0.f, 0.f};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += gridDim.x * blockDim.x) {
         T cv;
         if (conv_pad) {
-            int64_t a = i / ((int64_t)M * M), rem = i - a * M * M, bb = rem / M, c = rem - bb * M;
-            int64_t M2 = 2 * M;
+            const int a = i / mm, rem = i - a * mm, bb = rem / M, c = rem - bb * M;
             cv = conv[(a * M2 + bb) * M2 + c];
         } else {
             cv = conv[i];
         }
-        T s = (T)support[i];
-        T out = (T)al * s * cv + (T)rl * v[i] + (T)fl * s * reg[i];
+        const T s = (T)support[i], vi = v[i];
+        const T out = al * s * cv + rl * vi + fl * s * reg[i];
         q[i] = out;
-        acc += (double)v[i] * (double)out;
+        if constexpr (sizeof(T) == 4)
+            dot2_add(acc2, vi, out);
+        else
+            acc += (double)vi * (double)out;
     }
     if (!with_dot) return;
+    if constexpr (sizeof(T) == 4) acc = block_sum_dot2(acc2);
     double tot;
-    if (block_reduce_last(acc, partial, &sc->ticket[0], &tot)) {
+    if (block_reduce_last(acc, partial, &sc->ticket[0], &tot, sizeof(T) == 4)) {
+        const double alpha = sc->rho / tot;
         sc->pq = tot;
-        sc->alpha = sc->rho / tot;
+        sc->alpha = alpha;
+        sc->alpha_hi = (float)alpha;
+        sc->alpha_lo = (float)(alpha - (double)(float)alpha);
     }
 }
 
-// x += alpha p ; r -= alpha q ; rho_new = r . r
+// x += alpha p ; r -= alpha q ; rho_new = r . r.  Float vectors: the FP64 updates rounded to
+// float (axpy_rn) and a per-thread compensated r . r (Dot2), FP64 across threads.
 template <typename T>
-__global__ void __launch_bounds__(RED_THREADS) k_update(CgScalars *sc, T *x, T *r, const T *p, const T *q, int M,
+__global__ void __launch_bounds__(RED_THREADS) k_update(CgScalars *sc, T *__restrict__ x, T *__restrict__ r,
+                                                        const T *__restrict__ p, const T *__restrict__ q, int M,
                                                         double *partial)
 {
     if (sc->done) return;
-    int64_t m3 = (int64_t)M * M * M;
-    double alpha = sc->alpha;
+    const int m3 = M * M * M;
+    const double alpha = sc->alpha;
+    const float ah = sc->alpha_hi, al = sc->alpha_lo;
     double acc = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] = (T)((double)x[i] + alpha * (double)p[i]);
-        T rn = (T)((double)r[i] - alpha * (double)q[i]);
-        r[i] = rn;
-        acc += (double)rn * (double)rn;
+    Dot2 acc2{0.f, 0.f};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m3; i += gridDim.x * blockDim.x) {
+        if constexpr (sizeof(T) == 4) {
+            x[i] = axpy_rn(x[i], ah, al, p[i]);
+            const float rn = axpy_rn(r[i], -ah, -al, q[i]);
+            r[i] = rn;
+            dot2_add(acc2, rn, rn);
+        } else {
+            x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+            T rn = (T)((double)r[i] - alpha * (double)q[i]);
+            r[i] = rn;
+            acc += (double)rn * (double)rn;
+        }
     }
+    if constexpr (sizeof(T) == 4) acc = block_sum_dot2(acc2);
     double tot;
-    if (block_reduce_last(acc, partial, &sc->ticket[1], &tot)) {
+    if (block_reduce_last(acc, partial, &sc->ticket[1], &tot, sizeof(T) == 4)) {
         sc->rho_prev = sc->rho;
         sc->rho = tot;
         sc->it += 1;
+        next_step_scalars(sc);
     }
 }
 
@@ -349,31 +446,24 @@ static int matvec_impl(Cg &c, const T *v, T *out, bool in_iteration)
     CgScalars *sc = in_iteration ? c.sc : nullptr;
     int64_t hbig = (int64_t)(2 * M) * (2 * M) * (M + 1);
     int64_t hsmall = (int64_t)M * M * (M / 2 + 1);
-    if (toe) {
-        if (c.prec == 64) {
-            CMT_TRY_CUFFT(cufftExecD2Z(c.r2c_big, (double *)c.pad, (cufftDoubleComplex *)c.spec));
-        } else {
-            CMT_TRY_CUFFT(cufftExecR2C(c.r2c_big, (float *)c.pad, (cufftComplex *)c.spec));
-        }
-        k_mul_complex<T><<<grid_elems(hbig), 256, 0, st>>>((cplx_t<T> *)c.spec, (const cplx_t<T> *)c.kern_hat, hbig, sc);
-        CMT_LAUNCH_CHECK();
-        if (c.prec == 64) {
-            CMT_TRY_CUFFT(cufftExecZ2D(c.c2r_big, (cufftDoubleComplex *)c.spec, (double *)c.conv));
-        } else {
-            CMT_TRY_CUFFT(cufftExecC2R(c.c2r_big, (cufftComplex *)c.spec, (float *)c.conv));
-        }
-    } else {
-        // explicit pair: conv = Re(A^H A (S v)) S / (2M)^3 on the M^3 grid
-        CMT_TRY(cmt_execute_pair(c.pair_plan, in_iteration ? c.p : v, c.conv, c.support,
-                                 1.0 / ((double)(2 * M) * (2 * M) * (2 * M))));
+    // the regulariser's M^3 transforms are small, latency-bound launches: with the Toeplitz
+    // operator they run on the side stream while the (2M)^3 convolution runs on st
+    const bool fork = toe && c.flambda != 0.0 && c.side;
+    if (fork) {
+        CMT_TRY_CUDA(cudaEventRecord(c.ev_fork, st));
+        CMT_TRY_CUDA(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
+        CMT_TRY_CUFFT(cufftSetStream(c.r2c_small, c.side));
+        CMT_TRY_CUFFT(cufftSetStream(c.c2r_small, c.side));
     }
+    cudaStream_t st_reg = fork ? c.side : st;
     if (c.flambda != 0.0) {
         if (c.prec == 64) {
             CMT_TRY_CUFFT(cufftExecD2Z(c.r2c_small, (double *)c.sx, (cufftDoubleComplex *)c.spec2));
         } else {
             CMT_TRY_CUFFT(cufftExecR2C(c.r2c_small, (float *)c.sx, (cufftComplex *)c.spec2));
         }
-        k_mul_real<T><<<grid_elems(hsmall), 256, 0, st>>>((cplx_t<T> *)c.spec2, (const T *)c.mask_hat, hsmall, sc);
+        k_mul_real<T><<<grid_elems(hsmall), 256, 0, st_reg>>>((cplx_t<T> *)c.spec2, (const T *)c.mask_hat, hsmall,
+                                                               sc);
         CMT_LAUNCH_CHECK();
         if (c.prec == 64) {
             CMT_TRY_CUFFT(cufftExecZ2D(c.c2r_small, (cufftDoubleComplex *)c.spec2, (double *)c.reg));
@@ -383,10 +473,44 @@ static int matvec_impl(Cg &c, const T *v, T *out, bool in_iteration)
     } else {
         CMT_TRY_CUDA(cudaMemsetAsync(c.reg, 0, esz(c) * c.m3, st));
     }
+    if (fork) {
+        CMT_TRY_CUDA(cudaEventRecord(c.ev_join, c.side));
+        CMT_TRY_CUFFT(cufftSetStream(c.r2c_small, st));
+        CMT_TRY_CUFFT(cufftSetStream(c.c2r_small, st));
+    }
+    if (toe) {
+        // conv = IFFT(kern_hat . FFT(pad)) over (2M)^3, pruned: pad is zero outside slices
+        // [0, M) (2D R2C of those slices into spec_in, whose other slices stay zero), and
+        // only slices [0, M) of the result are read (2D C2R of those slices)
+        if (c.prec == 64) {
+            CMT_TRY_CUFFT(cufftExecD2Z(c.r2c_2d, (double *)c.pad, (cufftDoubleComplex *)c.spec_in));
+            CMT_TRY_CUFFT(cufftExecZ2Z(c.c2c_x, (cufftDoubleComplex *)c.spec_in, (cufftDoubleComplex *)c.spec,
+                                       CUFFT_FORWARD));
+        } else {
+            CMT_TRY_CUFFT(cufftExecR2C(c.r2c_2d, (float *)c.pad, (cufftComplex *)c.spec_in));
+            CMT_TRY_CUFFT(cufftExecC2C(c.c2c_x, (cufftComplex *)c.spec_in, (cufftComplex *)c.spec, CUFFT_FORWARD));
+        }
+        k_mul_complex<T><<<grid_elems(hbig), 256, 0, st>>>((cplx_t<T> *)c.spec, (const cplx_t<T> *)c.kern_hat, hbig, sc);
+        CMT_LAUNCH_CHECK();
+        if (c.prec == 64) {
+            CMT_TRY_CUFFT(cufftExecZ2Z(c.c2c_x, (cufftDoubleComplex *)c.spec, (cufftDoubleComplex *)c.spec,
+                                       CUFFT_INVERSE));
+            CMT_TRY_CUFFT(cufftExecZ2D(c.c2r_2d, (cufftDoubleComplex *)c.spec, (double *)c.conv));
+        } else {
+            CMT_TRY_CUFFT(cufftExecC2C(c.c2c_x, (cufftComplex *)c.spec, (cufftComplex *)c.spec, CUFFT_INVERSE));
+            CMT_TRY_CUFFT(cufftExecC2R(c.c2r_2d, (cufftComplex *)c.spec, (float *)c.conv));
+        }
+    } else {
+        // explicit pair: conv = Re(A^H A (S v)) S / (2M)^3 on the M^3 grid
+        CMT_TRY(cmt_execute_pair(c.pair_plan, in_iteration ? c.p : v, c.conv, c.support,
+                                 1.0 / ((double)(2 * M) * (2 * M) * (2 * M))));
+    }
+    if (fork) CMT_TRY_CUDA(cudaStreamWaitEvent(st, c.ev_join, 0));
     // the pair already applied S and the 1/(2M)^3; the Toeplitz conv is unscaled (kern_hat holds it)
     k_combine<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>(c.sc, in_iteration ? (const T *)c.p : v, (const T *)c.conv,
-                                                     toe ? 1 : 0, (const T *)c.reg, c.support, M, c.alambda,
-                                                     c.rlambda, c.flambda, out, in_iteration ? 1 : 0, c.partial);
+                                                     toe ? 1 : 0, (const T *)c.reg, c.support, M, (T)c.alambda,
+                                                     (T)c.rlambda, (T)c.flambda, out, in_iteration ? 1 : 0,
+                                                     c.partial);
     CMT_LAUNCH_CHECK();
     return CMT_OK;
 }
@@ -409,13 +533,15 @@ static int iteration(Cg &c)
 static void cg_destroy(Cg *c)
 {
     if (!c) return;
-    void *bufs[] = {c->x, c->r, c->p, c->q, c->b, c->sx, c->pad, c->conv, c->spec, c->spec2, c->reg,
+    void *bufs[] = {c->x, c->r, c->p, c->q, c->b, c->sx, c->pad, c->conv, c->spec, c->spec_in, c->spec2, c->reg,
                     c->kern_hat, c->mask_hat, c->support, c->partial, c->sc};
     for (void *b : bufs) cudaFree(b);
     if (c->host_sc) cudaFreeHost(c->host_sc);
     if (c->have_big) {
         cufftDestroy(c->r2c_big);
-        cufftDestroy(c->c2r_big);
+        cufftDestroy(c->r2c_2d);
+        cufftDestroy(c->c2c_x);
+        cufftDestroy(c->c2r_2d);
     }
     if (c->have_small) {
         cufftDestroy(c->r2c_small);
@@ -423,6 +549,9 @@ static void cg_destroy(Cg *c)
     }
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
 }
 
 // Route every launch of the solver (its kernels, its cuFFT plans, the pair plan) to s.
@@ -431,7 +560,9 @@ static int route_to(Cg &c, cudaStream_t s)
     c.stream = s;
     if (c.have_big) {
         CMT_TRY_CUFFT(cufftSetStream(c.r2c_big, s));
-        CMT_TRY_CUFFT(cufftSetStream(c.c2r_big, s));
+        CMT_TRY_CUFFT(cufftSetStream(c.r2c_2d, s));
+        CMT_TRY_CUFFT(cufftSetStream(c.c2c_x, s));
+        CMT_TRY_CUFFT(cufftSetStream(c.c2r_2d, s));
     }
     if (c.have_small) {
         CMT_TRY_CUFFT(cufftSetStream(c.r2c_small, s));
@@ -532,6 +663,8 @@ static int solve_begin(Cg &c, const T *d, T *x, double rtol, double atol)
     k_dot<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>((const T *)c.r, (const T *)c.r, c.m3, c.partial, &sc->ticket[2],
                                                  &sc->rho);
     CMT_LAUNCH_CHECK();
+    k_next_step<<<1, 1, 0, st>>>(sc);
+    CMT_LAUNCH_CHECK();
     k_copy_if_done<T><<<g, 256, 0, st>>>(sc, (const T *)c.b, (T *)c.x, c.m3);
     CMT_LAUNCH_CHECK();
     return CMT_OK;
@@ -594,6 +727,15 @@ extern "C" int cmt_cg_create(int M, int prec, int op, void *stream, cmt_cg **out
             return fail(CMT_ERR_OOM);
         }
     }
+    if (op == 0) {  // the regulariser branch's side stream and its fork / join events
+        cudaError_t err = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+        if (err != cudaSuccess) {
+            set_error("cg side stream: %s", cudaGetErrorString(err));
+            return fail(CMT_ERR_CUDA);
+        }
+    }
     {
         cudaError_t err = cudaMallocHost((void **)&c->host_sc, sizeof(CgScalars));
         if (err != cudaSuccess) {
@@ -603,7 +745,9 @@ extern "C" int cmt_cg_create(int M, int prec, int op, void *stream, cmt_cg **out
         memset(c->host_sc, 0, sizeof(CgScalars));
     }
     if (op == 0) {
-        struct A big[] = {{&c->pad, e * c->m2}, {&c->conv, e * c->m2}, {&c->spec, 2 * e * hbig}, {&c->kern_hat, 2 * e * hbig}};
+        struct A big[] = {{&c->pad, e * c->m2},          {&c->conv, e * c->m2},
+                          {&c->spec, 2 * e * hbig},      {&c->spec_in, 2 * e * hbig},
+                          {&c->kern_hat, 2 * e * hbig}};
         for (auto &a : big) {
             cudaError_t err = cudaMalloc(a.p, a.n);
             if (err != cudaSuccess) {
@@ -611,16 +755,28 @@ extern "C" int cmt_cg_create(int M, int prec, int op, void *stream, cmt_cg **out
                 return fail(CMT_ERR_OOM);
             }
         }
+        // the padding (outside the [0, M)^3 corner) and spec_in's slices from M on stay zero
         cudaMemset(c->pad, 0, e * c->m2);
-        int n2 = 2 * M;
-        if (cufftPlan3d(&c->r2c_big, n2, n2, n2, prec == 64 ? CUFFT_D2Z : CUFFT_R2C) != CUFFT_SUCCESS ||
-            cufftPlan3d(&c->c2r_big, n2, n2, n2, prec == 64 ? CUFFT_Z2D : CUFFT_C2R) != CUFFT_SUCCESS) {
-            set_error("cuFFT plan (2M)^3 failed");
+        cudaMemset(c->spec_in, 0, 2 * e * hbig);
+        int n2 = 2 * M, h = M + 1;
+        int n2d[2] = {n2, n2}, real2d[2] = {n2, n2}, half2d[2] = {n2, h}, n1d[1] = {n2};
+        const int col = n2 * h;  // complex elements per slice of the half spectrum
+        const bool dp = prec == 64;
+        if (cufftPlan3d(&c->r2c_big, n2, n2, n2, dp ? CUFFT_D2Z : CUFFT_R2C) != CUFFT_SUCCESS ||
+            cufftPlanMany(&c->r2c_2d, 2, n2d, real2d, 1, n2 * n2, half2d, 1, col, dp ? CUFFT_D2Z : CUFFT_R2C, M) !=
+                CUFFT_SUCCESS ||
+            cufftPlanMany(&c->c2c_x, 1, n1d, n1d, col, 1, n1d, col, 1, dp ? CUFFT_Z2Z : CUFFT_C2C, col) !=
+                CUFFT_SUCCESS ||
+            cufftPlanMany(&c->c2r_2d, 2, n2d, half2d, 1, col, real2d, 1, n2 * n2, dp ? CUFFT_Z2D : CUFFT_C2R, M) !=
+                CUFFT_SUCCESS) {
+            set_error("cuFFT plans for the (2M)^3 convolution failed");
             return fail(CMT_ERR_CUFFT);
         }
         c->have_big = true;
         cufftSetStream(c->r2c_big, c->stream);
-        cufftSetStream(c->c2r_big, c->stream);
+        cufftSetStream(c->r2c_2d, c->stream);
+        cufftSetStream(c->c2c_x, c->stream);
+        cufftSetStream(c->c2r_2d, c->stream);
     } else {
         cudaError_t err = cudaMalloc(&c->conv, e * c->m3);
         if (err != cudaSuccess) return fail(CMT_ERR_OOM);

@@ -109,4 +109,36 @@ __device__ __forceinline__ float df_scale_to_float(float x, float2 s)
     return __fadd_rn(p, e);
 }
 
+// fl32(x + (ah + al) y) for floats x, y and a double-float a: the product ah y split
+// exactly (FMA), x + ah y by TwoSum, the low parts added, one final rounding.  Equal to the
+// FP64 value x + a y rounded to float except within ~2^-46 of a rounding boundary.
+__device__ __forceinline__ float axpy_rn(float x, float ah, float al, float y)
+{
+    const float ph = __fmul_rn(ah, y);
+    float pe = __fmaf_rn(ah, y, -ph);
+    pe = __fmaf_rn(al, y, pe);
+    const float s = __fadd_rn(x, ph), bs = __fsub_rn(s, x);
+    const float se = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bs)), __fsub_rn(ph, bs));
+    return __fadd_rn(s, __fadd_rn(se, pe));
+}
+
+// Compensated sum of float products (Ogita, Rump & Oishi 2005, algorithm Dot2): s carries
+// the rounded running sum, c the exact errors of the products (FMA) and of the additions
+// (TwoSum); s + c is the sum as if accumulated in twice the working precision.
+struct Dot2 {
+    float s, c;
+};
+
+__device__ __forceinline__ void dot2_add(Dot2 &d, float a, float b)
+{
+    const float h = __fmul_rn(a, b);
+    const float l = __fmaf_rn(a, b, -h);
+    const float s = __fadd_rn(d.s, h), bs = __fsub_rn(s, d.s);
+    const float e = __fadd_rn(__fsub_rn(d.s, __fsub_rn(s, bs)), __fsub_rn(h, bs));
+    d.s = s;
+    d.c = __fadd_rn(d.c, __fadd_rn(e, l));
+}
+
+__device__ __forceinline__ double dot2_value(const Dot2 &d) { return (double)d.s + (double)d.c; }
+
 }  // namespace cmt

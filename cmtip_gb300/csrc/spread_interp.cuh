@@ -406,11 +406,21 @@ __device__ __forceinline__ void spread_tab_sub(int b, int off, const int *bin_co
     const int p0 = bin_start[b] + off;
     const int e = lane % EW, bl = lane / EW;
 
+    // FP32 real strengths: the window's columns in pairs, updated with the packed FP32 FMA
+    // (fma.rn.f32x2: two independent round-to-nearest FMAs per instruction, so the sums are
+    // those of scalar FMAs with fewer instructions issued); an odd width's last column keeps
+    // scalar FMAs (acc[r][NX - 1]).
+    constexpr bool PK = sizeof(T) == 4 && !CPLX;
+    constexpr int NP = NX / 2;
     T acc[RX][NX], aci[RX][NX];
+    float2 ap[RX][NP];
 #pragma unroll
-    for (int r = 0; r < RX; ++r)
+    for (int r = 0; r < RX; ++r) {
 #pragma unroll
         for (int a = 0; a < NX; ++a) acc[r][a] = aci[r][a] = T(0);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) ap[r][k] = make_float2(0.f, 0.f);
+    }
     int cur_key = -1, X0 = 0, Y0 = 0, Z0 = 0;  // subgrid cell of the register window's corner
     auto flush = [&]() {
         if (cur_key < 0) return;
@@ -422,14 +432,17 @@ __device__ __forceinline__ void spread_tab_sub(int b, int off, const int *bin_co
 #pragma unroll
             for (int a = 0; a < NX; ++a) {
                 const int xx = X0 + a;
+                const T v = PK && a < 2 * NP ? T((a & 1) ? ap[r][a >> 1].y : ap[r][a >> 1].x) : acc[r][a];
                 // extended cells outside the subgrid never receive a contribution
                 if (row_ok && (!EXT || (xx >= 0 && xx < S))) {
                     const int idx = (xx * S + yy) * P + zz;
-                    if (acc[r][a] != T(0)) atomicAdd(&sg[idx], acc[r][a]);
+                    if (v != T(0)) atomicAdd(&sg[idx], v);
                     if (CPLX && aci[r][a] != T(0)) atomicAdd(&sg[copy + idx], aci[r][a]);
                 }
                 acc[r][a] = aci[r][a] = T(0);
             }
+#pragma unroll
+            for (int k = 0; k < NP; ++k) ap[r][k] = make_float2(0.f, 0.f);
         }
     };
 
@@ -495,6 +508,20 @@ __device__ __forceinline__ void spread_tab_sub(int b, int off, const int *bin_co
                             acc[RX - 1][a] += xv[a] * wr1;
                             aci[RX - 1][a] += xv[a] * wi1;
                         }
+                    }
+                } else if constexpr (PK) {
+                    const T zv = rq[16 + e];
+                    const float w0 = yv.x * zv, w1 = yv.y * zv;
+                    const float2 w0p = make_float2(w0, w0), w1p = make_float2(w1, w1);
+#pragma unroll
+                    for (int k = 0; k < NP; ++k) {
+                        const float2 xk = make_float2(xv[2 * k], xv[2 * k + 1]);
+                        ap[0][k] = __ffma2_rn(xk, w0p, ap[0][k]);
+                        if (RX > 1) ap[RX - 1][k] = __ffma2_rn(xk, w1p, ap[RX - 1][k]);
+                    }
+                    if (NX % 2) {
+                        acc[0][NX - 1] += xv[NX - 1] * w0;
+                        if (RX > 1) acc[RX - 1][NX - 1] += xv[NX - 1] * w1;
                     }
                 } else {
                     const T zv = rq[16 + e];
