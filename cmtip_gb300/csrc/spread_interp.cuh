@@ -665,6 +665,12 @@ __device__ __forceinline__ void interp_tab_sub(int b, int off, const int *bin_co
     const int p0 = bin_start[b] + off;
     const int e = lane % EW, bl = lane / EW;
     T gr[RX][W], gi[RX][W];
+    // real output in FP32: the window's column pairs as float2 and each row's dot product as
+    // two partial sums (even / odd columns) updated with the packed FP32 FMA (fma.rn.f32x2);
+    // an odd width's last column is added with a scalar FMA
+    constexpr bool PK = sizeof(T) == 4 && !CPLX;
+    constexpr int NP = W / 2;
+    float2 gp[RX][NP > 0 ? NP : 1];
     int cur_key = -1;
     int t0, t1;
     warp_run(cnt, warp, nwarps, t0, t1);
@@ -700,6 +706,10 @@ __device__ __forceinline__ void interp_tab_sub(int b, int off, const int *bin_co
                         gr[r][a] = ok ? sg[idx] : T(0);
                         if (CPLX) gi[r][a] = ok ? sg[copy + idx] : T(0);
                     }
+                    if constexpr (PK) {
+#pragma unroll
+                        for (int k = 0; k < NP; ++k) gp[r][k] = make_float2(gr[r][2 * k], gr[r][2 * k + 1]);
+                    }
                 }
             }
 #pragma unroll 2
@@ -710,13 +720,29 @@ __device__ __forceinline__ void interp_tab_sub(int b, int off, const int *bin_co
                 const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
                 const T zv = rq[16 + e];
                 T ar0 = T(0), ai0 = T(0), ar1 = T(0), ai1 = T(0);
+                if constexpr (PK) {
+                    float2 s0 = make_float2(0.f, 0.f), s1 = make_float2(0.f, 0.f);
 #pragma unroll
-                for (int a = 0; a < W; ++a) {
-                    ar0 += xv[a] * gr[0][a];
-                    if (CPLX) ai0 += xv[a] * gi[0][a];
-                    if (RX > 1) {
-                        ar1 += xv[a] * gr[RX - 1][a];
-                        if (CPLX) ai1 += xv[a] * gi[RX - 1][a];
+                    for (int k = 0; k < NP; ++k) {
+                        const float2 xk = make_float2(xv[2 * k], xv[2 * k + 1]);
+                        s0 = __ffma2_rn(xk, gp[0][k], s0);
+                        if (RX > 1) s1 = __ffma2_rn(xk, gp[RX - 1][k], s1);
+                    }
+                    if (W % 2) {
+                        s0.x = fmaf(xv[W - 1], gr[0][W - 1], s0.x);
+                        if (RX > 1) s1.x = fmaf(xv[W - 1], gr[RX - 1][W - 1], s1.x);
+                    }
+                    ar0 = s0.x + s0.y;
+                    ar1 = s1.x + s1.y;
+                } else {
+#pragma unroll
+                    for (int a = 0; a < W; ++a) {
+                        ar0 += xv[a] * gr[0][a];
+                        if (CPLX) ai0 += xv[a] * gi[0][a];
+                        if (RX > 1) {
+                            ar1 += xv[a] * gr[RX - 1][a];
+                            if (CPLX) ai1 += xv[a] * gi[RX - 1][a];
+                        }
                     }
                 }
                 T sr = (yv.x * ar0 + yv.y * ar1) * zv;
@@ -753,7 +779,7 @@ __device__ __forceinline__ void interp_tab_sub(int b, int off, const int *bin_co
 
 // One subproblem per CTA (sub_bin / sub_off list of one plan).
 template <typename T, int OUT, int W>
-__global__ void __launch_bounds__(256) k_interp_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
+__global__ void __launch_bounds__(256, 4) k_interp_tab(const int *sub_bin, const int *sub_off, const int *bin_count,
                                                     const int *bin_start, const int *perm, const T *ux,
                                                     const T *uy, const T *uz, const T *fine, SubgridGeom gm, T beta,
                                                     T *out)
@@ -764,7 +790,7 @@ __global__ void __launch_bounds__(256) k_interp_tab(const int *sub_bin, const in
 
 // Interpolation over the subproblems of all plans of a batch, one persistent launch.
 template <typename T, int OUT, int W>
-__global__ void __launch_bounds__(256) k_interp_tab_batch(const WorkItem *work, int nwork, const InstDesc<T> *inst,
+__global__ void __launch_bounds__(256, 4) k_interp_tab_batch(const WorkItem *work, int nwork, const InstDesc<T> *inst,
                                                           T beta, int *next)
 {
     for (;;) {
