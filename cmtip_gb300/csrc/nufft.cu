@@ -633,15 +633,16 @@ __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin
     }
 }
 
-// k_subsort for FP32 plans whose global passes ordered every bin by its full window origin
-// (fine_sort 4): the CTA walks its subproblem in chunks of SUBSORT_PER records per thread,
-// held in registers, so each record is read from memory once (k_subsort reads it twice,
-// once for the counts and once for the scatter).  The input is in origin order, so a
-// chunk's keys span only the origins between its first and last record: that range of
-// counters is cleared and scanned per chunk.  Sorting chunk by chunk keeps the origin
-// order; an origin whose points straddle a chunk boundary has its refinement classes in
-// two runs (the earlier chunk's part first), which the spreading kernels treat as two
-// runs of one window.  The sorted chunk is assembled in shared memory and then written to
+// k_subsort for FP32 plans whose global passes ordered every bin by its window origin, whole
+// (fine_sort 4) or its x, y part (fine_sort 3): the CTA walks its subproblem in chunks of
+// SUBSORT_PER records per thread, held in registers, so each record is read from memory
+// once (k_subsort reads it twice, once for the counts and once for the scatter).  The input
+// is in origin order, so a chunk's keys span only the origins between its first and last
+// record: that range of counters is cleared and scanned per chunk.  Sorting chunk by chunk
+// keeps the global order; the origin classes of the key a chunk boundary cuts (its
+// refinement classes, or with x, y keys its z origins) come out as two runs each (the
+// earlier chunk's part first), which the kernels treat as two runs of one window.  The
+// sorted chunk is assembled in shared memory and then written to
 // the four output arrays in order, so every warp store is one contiguous 128-byte line
 // (scattered 4-byte stores straight to the arrays are bound by L2 sector writes).
 constexpr int SUBSORT_PER = 8, SUBSORT_THREADS = 256, SUBSORT_CHUNK = SUBSORT_PER * SUBSORT_THREADS;
@@ -1116,10 +1117,11 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     // ranges of origins and points that share a window land next to each other; k_subsort
     // then orders each subproblem by origin and refinement (point_key).  The scatter writes
     // one 16-byte record per point, one write stream per key, which L2 still merges at this
-    // key count.  CMT_SORT_KEYS = 1..3 sets the number of origin coordinates keyed, for
-    // comparison.  Plans without sort_origin, and grids with too many keys, sort by bin only.
+    // key count.  The plan's sort_keys sets the number of origin coordinates keyed
+    // (CMT_SORT_KEYS = 1..3 overrides, for comparison).  Plans without sort_origin, and grids
+    // with too many keys, sort by bin only.
     const int64_t O = p.bs + 1;
-    int kd = 3;
+    int kd = std::min(3, std::max(1, p.sort_keys));
     if (const char *env = getenv("CMT_SORT_KEYS")) kd = std::min(3, std::max(1, atoi(env)));
     const int64_t kbo = kd == 1 ? O : (kd == 2 ? O * O : O * O * O);
     const int fine_sort = p.sort_origin && (int64_t)nbins * kbo < (1LL << 27) ? 1 + kd : 0;
@@ -1238,7 +1240,7 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
         Plan o = p;
         set_pts_pointers<T>(o, scratch, N);
         const int csm = SUBSORT_CHUNK * 16 + nsk * (int)sizeof(int);
-        if (do_subsort && p.nsub > 0 && sizeof(T) == 4 && fine_sort == 4 && csm <= 200 * 1024) {
+        if (do_subsort && p.nsub > 0 && sizeof(T) == 4 && fine_sort >= 3 && csm <= 200 * 1024) {
             CMT_TRY(prep_smem(k_subsort_chunked, csm));
             k_subsort_chunked<<<(unsigned)p.nsub, SUBSORT_THREADS, csm, st>>>(
                 p.sub_bin, p.sub_off, p.bin_count, p.bin_start, p.w, p.bs, p.maxsub, nsk,
@@ -1526,10 +1528,13 @@ extern "C" int cmt_plan_create(int type, int M, int prec, double eps, int isign,
     // kernels for every width, for comparison
     if (const char *env = getenv("CMT_SPREAD_TAB")) p->spread_tab = atoi(env) != 0;
     if (const char *env = getenv("CMT_INTERP_TAB")) p->interp_tab = atoi(env) != 0;
-    // Spreading plans sort each bin by window origin (long runs of shared windows across the
-    // whole bin); interpolation plans sort by bin only, which costs less and loses little.
+    // Spreading plans sort each bin by the whole window origin (long runs of shared windows
+    // across the bin, for this plan and a derived one); FP32 interpolation plans by its x, y
+    // part, which keeps the scatter's key streams few and lets the per-subproblem sort read
+    // each record once (k_subsort_chunked); FP64 interpolation plans by bin only.
     // CMT_SORT_ORIGIN=0/1 overrides, for comparison.
-    p->sort_origin = type == 1;
+    p->sort_origin = type == 1 || prec == 32;
+    p->sort_keys = type == 1 ? 3 : 2;
     if (const char *env = getenv("CMT_SORT_ORIGIN")) p->sort_origin = atoi(env) != 0;
     int rc = CMT_OK;
     size_t bytes = 2 * elem(*p) * (size_t)p->n * p->n * p->n;

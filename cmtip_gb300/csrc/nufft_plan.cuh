@@ -16,6 +16,7 @@ struct Plan {
     int spread_tab = 1;                        // widths <= 8: table-driven spreading kernel
     int interp_tab = 1;                        // widths <= 8: table-driven interpolation kernel
     int sort_origin = 1;                       // global sort by bin and window origin (else bin)
+    int sort_keys = 3;                         // origin coordinates in the global key (1: x, 2: x y, 3: x y z)
     double cscale = 1.0;                       // coordinate scale of borrowed points
     const Plan *points_of = nullptr;           // set: the point arrays belong to this plan
     double beta = 0.0;
