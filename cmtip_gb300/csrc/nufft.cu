@@ -1164,19 +1164,21 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     const size_t scratch_bytes = std::max(blk, sizeof(PtRec<T>) * (size_t)N);
     // pass 1 writes records (caller order) to the scratch block, pass 2 sorted records to the
     // plan block, the subproblem sort (or a plain copy) the final arrays to the scratch block,
-    // and the blocks swap
+    // and the blocks swap.  Both blocks come from the stream-ordered pool, which keeps freed
+    // memory: the block the first call frees is the next call's scratch, so only the first
+    // call maps new memory.
+    cudaStream_t st = p.stream;
+    keep_pool_memory();
     if (N > p.cap_pts) {
-        cudaFree(p.pts_block);
+        if (p.pts_block) cudaFreeAsync(p.pts_block, st);
         p.pts_block = nullptr;
         p.perm = nullptr;
         p.ux = p.uy = p.uz = nullptr;
         p.cap_pts = 0;
-        CMT_TRY_CUDA(cudaMalloc(&p.pts_block, blk));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.pts_block, blk, st));
         p.cap_pts = N;
     }
     set_pts_pointers<T>(p, p.pts_block, p.cap_pts);
-    cudaStream_t st = p.stream;
-    keep_pool_memory();
     void *scratch = nullptr;
     CMT_TRY_CUDA(cudaMallocAsync(&scratch, scratch_bytes, st));
     struct ScratchGuard {
