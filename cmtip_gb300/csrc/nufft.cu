@@ -379,6 +379,15 @@ __global__ void k_bin_scatter(int64_t N, const PtRec<T> *rec, const int *start, 
     }
 }
 
+// 16-byte asynchronous global -> shared copies (cp.async, completion by commit groups)
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // Pass 2 for FP32 plans, tile by tile: a CTA groups a tile of SCAT_TILE records (caller
 // order) by key in a shared-memory hash table, reserves each key's share of its sorted range
 // with one atomic per key and tile, and writes the tile's records of a key to consecutive
@@ -636,7 +645,8 @@ __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin
 // k_subsort for FP32 plans whose global passes ordered every bin by its window origin, whole
 // (fine_sort 4) or its x, y part (fine_sort 3): the CTA walks its subproblem in chunks of
 // SUBSORT_PER records per thread, held in registers, so each record is read from memory
-// once (k_subsort reads it twice, once for the counts and once for the scatter).  The input
+// once (k_subsort reads it twice, once for the counts and once for the scatter), the next
+// chunk arriving in shared memory while the current one is sorted.  The input
 // is in origin order, so a chunk's keys span only the origins between its first and last
 // record: that range of counters is cleared and scanned per chunk.  Sorting chunk by chunk
 // keeps the global order; the origin classes of the key a chunk boundary cuts (its
@@ -647,14 +657,16 @@ __global__ void k_subsort(const int *sub_bin, const int *sub_off, const int *bin
 // (scattered 4-byte stores straight to the arrays are bound by L2 sector writes).
 constexpr int SUBSORT_PER = 8, SUBSORT_THREADS = 256, SUBSORT_CHUNK = SUBSORT_PER * SUBSORT_THREADS;
 
-__global__ void __launch_bounds__(SUBSORT_THREADS, 4)
+__global__ void __launch_bounds__(SUBSORT_THREADS, 3)
     k_subsort_chunked(const int *sub_bin, const int *sub_off, const int *bin_count, const int *bin_start, int w,
                       int bs, int maxsub, int nsk, const SortedRec<float> *in, int *perm_o, float *ux_o,
                       float *uy_o, float *uz_o)
 {
+    // two chunk buffers: the next chunk's records arrive by cp.async while the current one is
+    // sorted; a chunk's buffer then receives its sorted records for the copy-out
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *stage = reinterpret_cast<float4 *>(smem_raw);                   // SUBSORT_CHUNK records
-    int *cnt_s = reinterpret_cast<int *>(smem_raw + SUBSORT_CHUNK * 16);  // nsk counters, indexed key - lo
+    float4 *buf = reinterpret_cast<float4 *>(smem_raw);                       // 2 x SUBSORT_CHUNK records
+    int *cnt_s = reinterpret_cast<int *>(smem_raw + 2 * SUBSORT_CHUNK * 16);  // nsk counters, indexed key - lo
     __shared__ int sh[32];
     __shared__ int range[2];
     const int b = sub_bin[blockIdx.x];
@@ -663,18 +675,38 @@ __global__ void __launch_bounds__(SUBSORT_THREADS, 4)
     const int p0 = bin_start[b] + off;
     const int lane = threadIdx.x & 31;
     const int chunk = SUBSORT_CHUNK;  // blockDim.x == SUBSORT_THREADS
-    for (int c0 = 0; c0 < cnt; c0 += chunk) {
+    auto prefetch = [&](int c0, float4 *dst) {
         const int n = min(chunk, cnt - c0);
         const SortedRec<float> *src = in + p0 + c0;
+#pragma unroll
+        for (int k = 0; k < SUBSORT_PER; ++k) {
+            const int i = k * SUBSORT_THREADS + threadIdx.x;
+            if (i < n) cp_async16(dst + i, src + i);
+        }
+        cp_async_commit();
+    };
+    if (cnt > 0) prefetch(0, buf);
+    int cur = 0;
+    for (int c0 = 0; c0 < cnt; c0 += chunk, cur ^= 1) {
+        const int n = min(chunk, cnt - c0);
+        float4 *stage = buf + cur * SUBSORT_CHUNK;
+        // the other buffer held the previous chunk, whose copy-out ended with a barrier
+        if (c0 + chunk < cnt) {
+            prefetch(c0 + chunk, buf + (cur ^ 1) * SUBSORT_CHUNK);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();  // every thread's copies of this chunk have landed
         float4 r[SUBSORT_PER];
         int key[SUBSORT_PER];
         int kmin = 0x7fffffff, kmax = -1;
 #pragma unroll
         for (int k = 0; k < SUBSORT_PER; ++k) {
-            const int i = k * blockDim.x + threadIdx.x;
+            const int i = k * SUBSORT_THREADS + threadIdx.x;
             key[k] = -1;
             if (i < n) {
-                r[k] = __ldcs(reinterpret_cast<const float4 *>(src + i));  // read once: evict first
+                r[k] = stage[i];
                 key[k] = (int)point_key<float>(0, r[k].x, r[k].y, r[k].z, w, bs, 1);  // in [0, nsk)
                 kmin = min(kmin, key[k]);
                 kmax = max(kmax, key[k]);
@@ -684,7 +716,7 @@ __global__ void __launch_bounds__(SUBSORT_THREADS, 4)
             range[0] = 0x7fffffff;
             range[1] = -1;
         }
-        __syncthreads();  // also: the previous chunk's scatter is done with cnt_s
+        __syncthreads();
         kmin = __reduce_min_sync(0xffffffffu, kmin);
         kmax = __reduce_max_sync(0xffffffffu, kmax);
         if (lane == 0 && kmax >= 0) {
@@ -712,7 +744,7 @@ __global__ void __launch_bounds__(SUBSORT_THREADS, 4)
             cnt_s[i] = run;
             run += c;
         }
-        __syncthreads();
+        __syncthreads();  // also: every thread has its records in registers, the buffer is free
 #pragma unroll
         for (int k = 0; k < SUBSORT_PER; ++k) {
             const unsigned peers = __match_any_sync(0xffffffffu, key[k]);
@@ -732,7 +764,7 @@ __global__ void __launch_bounds__(SUBSORT_THREADS, 4)
             uz_c[i] = v.z;
             perm_c[i] = __float_as_int(v.w);
         }
-        // the next chunk's first barrier orders these reads of `stage` before its writes
+        __syncthreads();  // the copy-out has read this buffer before the next prefetch into it
     }
 }
 
@@ -1231,17 +1263,18 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     // pass 2: scatter, key_next starting at each key's first position
     CMT_TRY_CUDA(cudaMemcpyAsync(p.key_next, p.key_start, sizeof(int) * (nkeys + 1), cudaMemcpyDeviceToDevice, st));
     SortedRec<T> *srec = reinterpret_cast<SortedRec<T> *>(p.pts_block);
-    if (sizeof(T) == 4)
+    if (sizeof(T) == 4) {
         k_bin_scatter_tiled<<<(unsigned)std::min<int64_t>(ceil_div(N, (int64_t)SCAT_TILE), 152 * 8), SCAT_THREADS, 0,
                               st>>>(N, reinterpret_cast<const PtRec<float> *>(scratch), p.key_start, p.key_next,
                                     reinterpret_cast<SortedRec<float> *>(srec), p.dflag);
-    else
+    } else {
         k_bin_scatter<T><<<g, 256, 0, st>>>(N, (const PtRec<T> *)scratch, p.key_start, p.key_next, srec, p.dflag);
+    }
     CMT_LAUNCH_CHECK();
     {
         Plan o = p;
         set_pts_pointers<T>(o, scratch, N);
-        const int csm = SUBSORT_CHUNK * 16 + nsk * (int)sizeof(int);
+        const int csm = 2 * SUBSORT_CHUNK * 16 + nsk * (int)sizeof(int);
         if (do_subsort && p.nsub > 0 && sizeof(T) == 4 && fine_sort >= 3 && csm <= 200 * 1024) {
             CMT_TRY(prep_smem(k_subsort_chunked, csm));
             k_subsort_chunked<<<(unsigned)p.nsub, SUBSORT_THREADS, csm, st>>>(

@@ -449,25 +449,46 @@ __device__ __forceinline__ void spread_tab_sub(int b, int off, const int *bin_co
     int t0, t1;
     warp_run(cnt, warp, nwarps, t0, t1);
     const T cs = (T)gm.cscale;
-    for (int base = t0; base < t1; base += 32) {
-        // ---- lane `lane` prepares point base + lane
+    // point base + lane's coordinates and strength; FP32 real strengths on the plan's own grid
+    // load the next batch's while the current one is walked (the strength is a gather through
+    // the permutation; the extended-window form has no spare registers for it)
+    auto fetch = [&](int base, T &fx, T &fy, T &fz, T &fr, T &fi) {
         const int tl = base + lane;
         const bool valid = tl < t1;
         const int pos = p0 + (valid ? tl : t0);
-        const T px = ux[pos] * cs, py = uy[pos] * cs, pz = uz[pos] * cs;
-        T vr = T(1), vi = T(0);
+        fx = ux[pos];
+        fy = uy[pos];
+        fz = uz[pos];
+        fr = T(1);
+        fi = T(0);
         if (!valid) {
-            vr = T(0);
+            fr = T(0);
         } else if (c) {
             const int64_t j = perm[pos];
             if (CPLX) {
                 const T2 cv = reinterpret_cast<const T2 *>(c)[j];
-                vr = cv.x;
-                vi = cv.y;
+                fr = cv.x;
+                fi = cv.y;
             } else {
-                vr = c[j];
+                fr = c[j];
             }
         }
+    };
+    constexpr bool PREF = sizeof(T) == 4 && !CPLX && !EXT;
+    T nx = T(0), ny = T(0), nz = T(0), nr = T(0), ni = T(0);
+    if (PREF && t0 < t1) fetch(t0, nx, ny, nz, nr, ni);
+    for (int base = t0; base < t1; base += 32) {
+        // ---- lane `lane` prepares point base + lane
+        T px, py, pz, vr, vi;
+        if constexpr (PREF) {
+            px = nx, py = ny, pz = nz, vr = nr, vi = ni;
+            if (base + 32 < t1) fetch(base + 32, nx, ny, nz, nr, ni);
+        } else {
+            fetch(base, px, py, pz, vr, vi);
+        }
+        px *= cs;
+        py *= cs;
+        pz *= cs;
         __syncwarp();  // the previous batch's records have been read
         const int my_key = tab_prepare<T, W, EXT, CPLX ? 2 : 1>(px, py, pz, beta, vr, vi, tab + lane * REC);
         __syncwarp();
