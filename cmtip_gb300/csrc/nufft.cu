@@ -1142,6 +1142,11 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
 {
     unborrow(p);
     p.N = 0;
+    // the sort's buffers come from the stream-ordered pool (cudaMallocAsync on the plan's
+    // stream): a plan created and sorted afresh reuses pool memory instead of cudaMalloc,
+    // which maps new memory and synchronises the device
+    cudaStream_t st = p.stream;
+    keep_pool_memory();
     CMT_CHECK_ARG(N > 0 && N <= 0x7fffffffLL, "number of points %lld outside [1, 2^31-1]", (long long)N);
     int nbins = p.nb * p.nb * p.nb;
     // Global passes sort by bin and by the window origin on this grid ((bs+1)^3 keys per bin,
@@ -1164,29 +1169,29 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     const int64_t nkeys = (int64_t)nbins * kb;
     const int64_t ntiles = (nkeys + 1 + SCAN_TILE - 1) / SCAN_TILE;
     if (!p.dflag) {
-        CMT_TRY_CUDA(cudaMalloc(&p.dflag, sizeof(int) * 4));
-        CMT_TRY_CUDA(cudaMalloc(&p.dtot, sizeof(long long) * 2));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.dflag, sizeof(int) * 4, st));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.dtot, sizeof(long long) * 2, st));
     }
     if (nbins > p.cap_bins) {  // first points, or a retuned bin size
-        cudaFree(p.bin_count);
-        cudaFree(p.bin_fill);
-        cudaFree(p.bin_start);
+        if (p.bin_count) cudaFreeAsync(p.bin_count, st);
+        if (p.bin_fill) cudaFreeAsync(p.bin_fill, st);
+        if (p.bin_start) cudaFreeAsync(p.bin_start, st);
         p.bin_count = p.bin_fill = p.bin_start = nullptr;
         p.cap_bins = 0;
-        CMT_TRY_CUDA(cudaMalloc(&p.bin_count, sizeof(int) * nbins));
-        CMT_TRY_CUDA(cudaMalloc(&p.bin_fill, sizeof(int) * nbins));
-        CMT_TRY_CUDA(cudaMalloc(&p.bin_start, sizeof(int) * nbins));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.bin_count, sizeof(int) * nbins, st));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.bin_fill, sizeof(int) * nbins, st));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.bin_start, sizeof(int) * nbins, st));
         p.cap_bins = nbins;
     }
     if (nkeys + 1 > p.cap_keys) {
-        cudaFree(p.key_start);
-        cudaFree(p.key_next);
-        cudaFree(p.tile_sums);
+        if (p.key_start) cudaFreeAsync(p.key_start, st);
+        if (p.key_next) cudaFreeAsync(p.key_next, st);
+        if (p.tile_sums) cudaFreeAsync(p.tile_sums, st);
         p.key_start = p.key_next = p.tile_sums = nullptr;
         p.cap_keys = 0;
-        CMT_TRY_CUDA(cudaMalloc(&p.key_start, sizeof(int) * (nkeys + 1)));
-        CMT_TRY_CUDA(cudaMalloc(&p.key_next, sizeof(int) * (nkeys + 1)));
-        CMT_TRY_CUDA(cudaMalloc(&p.tile_sums, sizeof(int) * ntiles));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.key_start, sizeof(int) * (nkeys + 1), st));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.key_next, sizeof(int) * (nkeys + 1), st));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.tile_sums, sizeof(int) * ntiles, st));
         p.cap_keys = nkeys + 1;
     }
     // Sorted points live in one block (x, y, z coordinates, then the permutation).  A scratch
@@ -1199,8 +1204,6 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     // and the blocks swap.  Both blocks come from the stream-ordered pool, which keeps freed
     // memory: the block the first call frees is the next call's scratch, so only the first
     // call maps new memory.
-    cudaStream_t st = p.stream;
-    keep_pool_memory();
     if (N > p.cap_pts) {
         if (p.pts_block) cudaFreeAsync(p.pts_block, st);
         p.pts_block = nullptr;
@@ -1250,12 +1253,12 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     }
     p.nsub = tot[0];
     if (p.nsub > p.cap_sub) {
-        cudaFree(p.sub_bin);
-        cudaFree(p.sub_off);
+        if (p.sub_bin) cudaFreeAsync(p.sub_bin, st);
+        if (p.sub_off) cudaFreeAsync(p.sub_off, st);
         p.sub_bin = p.sub_off = nullptr;
         p.cap_sub = 0;
-        CMT_TRY_CUDA(cudaMalloc(&p.sub_bin, sizeof(int) * p.nsub));
-        CMT_TRY_CUDA(cudaMalloc(&p.sub_off, sizeof(int) * p.nsub));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.sub_bin, sizeof(int) * p.nsub, st));
+        CMT_TRY_CUDA(cudaMallocAsync(&p.sub_off, sizeof(int) * p.nsub, st));
         p.cap_sub = p.nsub;
     }
     k_sub_list<<<ceil_div(nbins, 256), 256, 0, st>>>(nbins, p.bin_count, sub_start, p.maxsub, p.sub_bin, p.sub_off);
@@ -1491,6 +1494,9 @@ static void unborrow(Plan &p)
 static void destroy(Plan *p)
 {
     if (!p) return;
+    // the sort's buffers are pool allocations, which cudaFree releases without waiting for
+    // work still using them: let every launch finish first
+    cudaDeviceSynchronize();
     unborrow(*p);
     cudaFree(p->bin_count);
     cudaFree(p->bin_fill);
