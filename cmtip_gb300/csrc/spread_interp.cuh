@@ -1176,15 +1176,25 @@ __device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_coun
     const int p0 = bin_start[b] + off;
     const int e = lane % EW, bl = lane / EW;
 
+    // FP32: both walks pair the window's columns (2k, 2k + 1) and update them with the packed
+    // FP32 FMA (fma.rn.f32x2), pass A as even / odd partial sums, pass B as the accumulators
+    // themselves; an odd width's last column stays scalar
+    constexpr bool PK = sizeof(T) == 4;
+    constexpr int NP = W / 2;
     // pass A state: G1 window (rows bl, bl + 4 at z offset e, all W columns)
     T gr[RX][W], gi[RX][W];
+    float2 grp[RX][NP > 0 ? NP : 1], gip[RX][NP > 0 ? NP : 1];
     int key_a = -1;
     // pass B state: G2 accumulation window
     T acc[RX][W], aci[RX][W];
+    float2 acp[RX][NP > 0 ? NP : 1], aip[RX][NP > 0 ? NP : 1];
 #pragma unroll
-    for (int r = 0; r < RX; ++r)
+    for (int r = 0; r < RX; ++r) {
 #pragma unroll
         for (int a = 0; a < W; ++a) acc[r][a] = aci[r][a] = T(0);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) acp[r][k] = aip[r][k] = make_float2(0.f, 0.f);
+    }
     int key_b = -1, X0 = 0, Y0 = 0, Z0 = 0;
     auto flush = [&]() {
         if (key_b < 0) return;
@@ -1195,13 +1205,18 @@ __device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_coun
             const bool row_ok = e < W && bl + r * BR < W;
 #pragma unroll
             for (int a = 0; a < W; ++a) {
+                const bool pk = PK && a < 2 * NP;
+                const T vr = pk ? T((a & 1) ? acp[r][a >> 1].y : acp[r][a >> 1].x) : acc[r][a];
+                const T vi = pk ? T((a & 1) ? aip[r][a >> 1].y : aip[r][a >> 1].x) : aci[r][a];
                 if (row_ok) {
                     const int idx = ((X0 + a) * S + yy) * P + zz;
-                    if (acc[r][a] != T(0)) atomicAdd(&sb[idx], acc[r][a]);
-                    if (aci[r][a] != T(0)) atomicAdd(&sb[copy + idx], aci[r][a]);
+                    if (vr != T(0)) atomicAdd(&sb[idx], vr);
+                    if (vi != T(0)) atomicAdd(&sb[copy + idx], vi);
                 }
                 acc[r][a] = aci[r][a] = T(0);
             }
+#pragma unroll
+            for (int k = 0; k < NP; ++k) acp[r][k] = aip[r][k] = make_float2(0.f, 0.f);
         }
     };
 
@@ -1240,6 +1255,13 @@ __device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_coun
                         gr[r][a] = ok ? sa[idx] : T(0);
                         gi[r][a] = ok ? sa[copy + idx] : T(0);
                     }
+                    if constexpr (PK) {
+#pragma unroll
+                        for (int k = 0; k < NP; ++k) {
+                            grp[r][k] = make_float2(gr[r][2 * k], gr[r][2 * k + 1]);
+                            gip[r][k] = make_float2(gi[r][2 * k], gi[r][2 * k + 1]);
+                        }
+                    }
                 }
             }
             for (; q < qe; ++q) {
@@ -1249,13 +1271,39 @@ __device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_coun
                 const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
                 const T zv = rq[16 + e];
                 T ar0 = T(0), ai0 = T(0), ar1 = T(0), ai1 = T(0);
+                if constexpr (PK) {
+                    float2 r0 = make_float2(0.f, 0.f), i0 = r0, r1 = r0, i1 = r0;
 #pragma unroll
-                for (int a = 0; a < W; ++a) {
-                    ar0 += xv[a] * gr[0][a];
-                    ai0 += xv[a] * gi[0][a];
-                    if (RX > 1) {
-                        ar1 += xv[a] * gr[RX - 1][a];
-                        ai1 += xv[a] * gi[RX - 1][a];
+                    for (int k = 0; k < NP; ++k) {
+                        const float2 xk = make_float2(xv[2 * k], xv[2 * k + 1]);
+                        r0 = __ffma2_rn(xk, grp[0][k], r0);
+                        i0 = __ffma2_rn(xk, gip[0][k], i0);
+                        if (RX > 1) {
+                            r1 = __ffma2_rn(xk, grp[RX - 1][k], r1);
+                            i1 = __ffma2_rn(xk, gip[RX - 1][k], i1);
+                        }
+                    }
+                    if (W % 2) {
+                        r0.x = fmaf(xv[W - 1], gr[0][W - 1], r0.x);
+                        i0.x = fmaf(xv[W - 1], gi[0][W - 1], i0.x);
+                        if (RX > 1) {
+                            r1.x = fmaf(xv[W - 1], gr[RX - 1][W - 1], r1.x);
+                            i1.x = fmaf(xv[W - 1], gi[RX - 1][W - 1], i1.x);
+                        }
+                    }
+                    ar0 = r0.x + r0.y;
+                    ai0 = i0.x + i0.y;
+                    ar1 = r1.x + r1.y;
+                    ai1 = i1.x + i1.y;
+                } else {
+#pragma unroll
+                    for (int a = 0; a < W; ++a) {
+                        ar0 += xv[a] * gr[0][a];
+                        ai0 += xv[a] * gi[0][a];
+                        if (RX > 1) {
+                            ar1 += xv[a] * gr[RX - 1][a];
+                            ai1 += xv[a] * gi[RX - 1][a];
+                        }
                     }
                 }
                 T sr = (yv.x * ar0 + yv.y * ar1) * zv;
@@ -1312,13 +1360,36 @@ __device__ __forceinline__ void pair_tab_sub(int b, int off, const int *bin_coun
                 const T2 yv = reinterpret_cast<const T2 *>(rq + 8)[bl];
                 const T2 zv = reinterpret_cast<const T2 *>(rq + 16)[e];
                 const T wr0 = yv.x * zv.x, wi0 = yv.x * zv.y, wr1 = yv.y * zv.x, wi1 = yv.y * zv.y;
+                if constexpr (PK) {
+                    const float2 wr0p = make_float2(wr0, wr0), wi0p = make_float2(wi0, wi0),
+                                 wr1p = make_float2(wr1, wr1), wi1p = make_float2(wi1, wi1);
 #pragma unroll
-                for (int a = 0; a < W; ++a) {
-                    acc[0][a] += xv[a] * wr0;
-                    aci[0][a] += xv[a] * wi0;
-                    if (RX > 1) {
-                        acc[RX - 1][a] += xv[a] * wr1;
-                        aci[RX - 1][a] += xv[a] * wi1;
+                    for (int k = 0; k < NP; ++k) {
+                        const float2 xk = make_float2(xv[2 * k], xv[2 * k + 1]);
+                        acp[0][k] = __ffma2_rn(xk, wr0p, acp[0][k]);
+                        aip[0][k] = __ffma2_rn(xk, wi0p, aip[0][k]);
+                        if (RX > 1) {
+                            acp[RX - 1][k] = __ffma2_rn(xk, wr1p, acp[RX - 1][k]);
+                            aip[RX - 1][k] = __ffma2_rn(xk, wi1p, aip[RX - 1][k]);
+                        }
+                    }
+                    if (W % 2) {
+                        acc[0][W - 1] += xv[W - 1] * wr0;
+                        aci[0][W - 1] += xv[W - 1] * wi0;
+                        if (RX > 1) {
+                            acc[RX - 1][W - 1] += xv[W - 1] * wr1;
+                            aci[RX - 1][W - 1] += xv[W - 1] * wi1;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int a = 0; a < W; ++a) {
+                        acc[0][a] += xv[a] * wr0;
+                        aci[0][a] += xv[a] * wi0;
+                        if (RX > 1) {
+                            acc[RX - 1][a] += xv[a] * wr1;
+                            aci[RX - 1][a] += xv[a] * wi1;
+                        }
                     }
                 }
             }
