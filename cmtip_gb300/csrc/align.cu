@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "cmt_common.cuh"
@@ -87,10 +88,21 @@ __global__ void k_row_stats(const TI *v, int64_t n_pix, double *rsum, double *rs
     int64_t row = blockIdx.x;
     const TI *src = v + row * n_pix;
     double a = 0.0, b = 0.0, c = 0.0;
-    for (int64_t p = threadIdx.x; p < n_pix; p += blockDim.x) {
-        double x = (double)src[p];
-        a += x;
-        b += x * x;
+    if constexpr (sizeof(TI) == 4) {  // float rows: compensated float sums (Dot2), FP64 per thread
+        Dot2 sa{0.f, 0.f}, sb{0.f, 0.f};
+        for (int64_t p = threadIdx.x; p < n_pix; p += blockDim.x) {
+            const float x = src[p];
+            dot2_add1(sa, x);
+            dot2_add(sb, x, x);
+        }
+        a = dot2_value(sa);
+        b = dot2_value(sb);
+    } else {
+        for (int64_t p = threadIdx.x; p < n_pix; p += blockDim.x) {
+            double x = (double)src[p];
+            a += x;
+            b += x * x;
+        }
     }
     block_sum3(a, b, c);
     if (threadIdx.x == 0) {
@@ -104,13 +116,20 @@ __global__ void k_row_stats(const TI *v, int64_t n_pix, double *rsum, double *rs
 // share (the radial intensity fall-off), so the cross term no longer cancels against
 // |x|^2 and reduced-precision operands keep their accuracy on the distance itself.
 template <typename TI>
-__global__ void k_col_mean(const TI *x, const double *w, int64_t n_img, int64_t n_pix, double *c)
+__global__ void k_col_mean(const TI *x, const double *w, int64_t n_img, int64_t n_pix, double *c, float *cf)
 {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n_pix) return;
     double s = 0.0;
-    for (int64_t i = 0; i < n_img; ++i) s += (double)x[i * n_pix + p];
+    if constexpr (sizeof(TI) == 4) {  // the column sum in float error-free arithmetic (FP64 is slow)
+        Dot2 d{0.f, 0.f};
+        for (int64_t i = 0; i < n_img; ++i) dot2_add1(d, x[i * n_pix + p]);
+        s = dot2_value(d);
+    } else {
+        for (int64_t i = 0; i < n_img; ++i) s += (double)x[i * n_pix + p];
+    }
     c[p] = w[p] * s / (double)n_img;
+    cf[p] = (float)c[p];
 }
 
 template <typename TO> __device__ __forceinline__ TO to_op(double v) { return (TO)v; }
@@ -124,8 +143,8 @@ template <> __device__ __forceinline__ double from_op<__nv_bfloat16>(__nv_bfloat
 //   side 0 (images):     [hi, hi, lo]      side 1 (references): [hi, lo, hi]
 // Also |u|^2 (of the unrounded values) when norm2 is given.
 template <typename TI, typename TO>
-__global__ void k_build_op(const TI *v, const double *w, const double *c, const double *scale, int64_t n_pix, int Kp,
-                           int terms, int side, TO *op, double *norm2)
+__global__ void k_build_op(const TI *v, const double *w, const double *c, const float2 *wdf, const float *cf,
+                           const double *scale, int64_t n_pix, int Kp, int terms, int side, TO *op, double *norm2)
 {
     int64_t row = blockIdx.x;
     const TI *src = v + row * n_pix;
@@ -133,18 +152,40 @@ __global__ void k_build_op(const TI *v, const double *w, const double *c, const 
     TO *dst = op + row * ld;
     double sr = scale ? scale[row] : 1.0;
     double a = 0.0, b = 0.0, cc = 0.0;
-    for (int64_t p = threadIdx.x; p < Kp; p += blockDim.x) {
-        double u = 0.0;
-        if (p < n_pix) u = sr * w[p] * (double)src[p] - c[p];
-        a += u * u;
-        TO hi = to_op<TO>(u);
-        if (terms == 1) {
-            dst[p] = hi;
-        } else {
-            TO lo = to_op<TO>(u - from_op<TO>(hi));
-            dst[p] = hi;
-            dst[Kp + p] = side == 0 ? hi : lo;
-            dst[2 * (int64_t)Kp + p] = side == 0 ? lo : hi;
+    if constexpr (std::is_same<TO, __nv_bfloat16>::value && sizeof(TI) == 4) {
+        // BF16 operands (8 significant bits) from float inputs: u in FP32 (the FP64 pipe is
+        // slow), rounded once to BF16; |u|^2 by compensated float sums
+        const float srf = (float)sr;
+        Dot2 nn{0.f, 0.f};
+        for (int64_t p = threadIdx.x; p < Kp; p += blockDim.x) {
+            float u = 0.f;
+            if (p < n_pix) u = fmaf(srf * wdf[p].x, src[p], -cf[p]);
+            dot2_add(nn, u, u);
+            const __nv_bfloat16 hi = __float2bfloat16(u);
+            if (terms == 1) {
+                dst[p] = hi;
+            } else {
+                const __nv_bfloat16 lo = __float2bfloat16(u - __bfloat162float(hi));
+                dst[p] = hi;
+                dst[Kp + p] = side == 0 ? hi : lo;
+                dst[2 * (int64_t)Kp + p] = side == 0 ? lo : hi;
+            }
+        }
+        a = dot2_value(nn);
+    } else {
+        for (int64_t p = threadIdx.x; p < Kp; p += blockDim.x) {
+            double u = 0.0;
+            if (p < n_pix) u = sr * w[p] * (double)src[p] - c[p];
+            a += u * u;
+            TO hi = to_op<TO>(u);
+            if (terms == 1) {
+                dst[p] = hi;
+            } else {
+                TO lo = to_op<TO>(u - from_op<TO>(hi));
+                dst[p] = hi;
+                dst[Kp + p] = side == 0 ? hi : lo;
+                dst[2 * (int64_t)Kp + p] = side == 0 ? lo : hi;
+            }
         }
     }
     block_sum3(a, b, cc);
@@ -745,15 +786,25 @@ __global__ void k_merge_rescore(SegInfo si, const float *pscore, const int *pidx
             sr[k] = df_from(sref[r]);
             mr[k] = reinterpret_cast<const float *>(model) + (int64_t)r * n_pix;
         }
-        for (int64_t p = lane; p < n_pix; p += 32) {
-            const float xp = (float)x[p];
-            const float2 wp = wdf[p];
-            const DF wv{wp.x, wp.y};
+        // two pixels per lane and step, all loads first (the loop is bound by load latency);
+        // an empty candidate slot reads row 0 and is discarded below, so the loop has no
+        // branch; a pixel past the end has weight 0
+        for (int64_t p = lane; p < n_pix; p += 64) {
+            const bool two = p + 32 < n_pix;
+            const float xa = (float)x[p], xb = two ? (float)x[p + 32] : 0.0f;
+            const float2 wa = wdf[p], wb = two ? wdf[p + 32] : make_float2(0.0f, 0.0f);
+            float ma[TOPK], mb[TOPK];
 #pragma unroll
             for (int k = 0; k < TOPK; ++k) {
-                if (cand[k] < 0) continue;  // warp-uniform
-                const DF dv = df_mul(df_add_f(df_mul_f(sr[k], mr[k][p]), -xp), wv);
-                acc[k] = df_add(acc[k], df_mul(dv, dv));
+                ma[k] = mr[k][p];
+                mb[k] = two ? mr[k][p + 32] : 0.0f;
+            }
+            const DF wva{wa.x, wa.y}, wvb{wb.x, wb.y};
+#pragma unroll
+            for (int k = 0; k < TOPK; ++k) {
+                const DF da = df_mul(df_add_f(df_mul_f(sr[k], ma[k]), -xa), wva);
+                const DF db = df_mul(df_add_f(df_mul_f(sr[k], mb[k]), -xb), wvb);
+                acc[k] = df_add(acc[k], df_add(df_mul(da, da), df_mul(db, db)));
             }
         }
 #pragma unroll
@@ -806,6 +857,7 @@ struct Match {
     int64_t n_pix = 0;
     int Kp = 0;
     double *cen = nullptr;                         // mean weighted image (operand centre)
+    float *cenf = nullptr;                         // the centre rounded to float (BF16 operands)
     cudaStream_t stream = nullptr;
     int num_sms = 152;
     int64_t n_img = 0, n_ref = 0, n_ref_pad = 0;
@@ -905,14 +957,15 @@ static void build_op(const Match &m, const void *v, int64_t rows, const double *
 {
     unsigned g = (unsigned)rows;
     if (m.mode == 0 || m.mode == 3)
-        k_build_op<float, __nv_bfloat16><<<g, 256, 0, m.stream>>>((const float *)v, m.w, m.cen, scale, m.n_pix, m.Kp,
-                                                                  m.terms, side, (__nv_bfloat16 *)op, norm2);
+        k_build_op<float, __nv_bfloat16><<<g, 256, 0, m.stream>>>((const float *)v, m.w, m.cen, m.wdf, m.cenf, scale,
+                                                                  m.n_pix, m.Kp, m.terms, side, (__nv_bfloat16 *)op,
+                                                                  norm2);
     else if (m.mode == 1)
-        k_build_op<float, float><<<g, 256, 0, m.stream>>>((const float *)v, m.w, m.cen, scale, m.n_pix, m.Kp, 1, side,
-                                                          (float *)op, norm2);
+        k_build_op<float, float><<<g, 256, 0, m.stream>>>((const float *)v, m.w, m.cen, m.wdf, m.cenf, scale, m.n_pix,
+                                                          m.Kp, 1, side, (float *)op, norm2);
     else
-        k_build_op<double, double><<<g, 256, 0, m.stream>>>((const double *)v, m.w, m.cen, scale, m.n_pix, m.Kp, 1,
-                                                            side, (double *)op, norm2);
+        k_build_op<double, double><<<g, 256, 0, m.stream>>>((const double *)v, m.w, m.cen, m.wdf, m.cenf, scale,
+                                                            m.n_pix, m.Kp, 1, side, (double *)op, norm2);
 }
 
 static void row_stats(const Match &m, const void *v, int64_t rows, double *rsum, double *rsq)
@@ -1068,6 +1121,7 @@ extern "C" int cmt_match_create(int64_t n_pix, int mode, void *stream, cmt_match
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaMalloc(&m->w, sizeof(double) * n_pix) != cudaSuccess || cudaMalloc(&m->cen, sizeof(double) * n_pix) != cudaSuccess ||
+        cudaMalloc(&m->cenf, sizeof(float) * n_pix) != cudaSuccess ||
         cudaMalloc(&m->wdf, sizeof(float2) * n_pix) != cudaSuccess ||
         cudaMalloc(&m->err, sizeof(int) * 2) != cudaSuccess ||
         cudaMalloc(&m->stats, sizeof(double) * 1025) != cudaSuccess) {
@@ -1098,9 +1152,9 @@ extern "C" int cmt_match_set_data(cmt_match *m, int64_t n_img, const void *data,
     m->cap_img = std::min(capd, capq);
     unsigned gp = (unsigned)ceil_div(m->n_pix, 256);
     if (m->mode == 2)
-        k_col_mean<double><<<gp, 256, 0, m->stream>>>((const double *)data, m->w, n_img, m->n_pix, m->cen);
+        k_col_mean<double><<<gp, 256, 0, m->stream>>>((const double *)data, m->w, n_img, m->n_pix, m->cen, m->cenf);
     else
-        k_col_mean<float><<<gp, 256, 0, m->stream>>>((const float *)data, m->w, n_img, m->n_pix, m->cen);
+        k_col_mean<float><<<gp, 256, 0, m->stream>>>((const float *)data, m->w, n_img, m->n_pix, m->cen, m->cenf);
     row_stats(*m, data, n_img, m->dsum, m->dsq);
     build_op(*m, data, n_img, nullptr, 0, m->opA, nullptr);
     CMT_LAUNCH_CHECK();
@@ -1311,7 +1365,7 @@ extern "C" int cmt_match_destroy(cmt_match *m)
     if (!m) return CMT_OK;
     for (auto e : m->ev)
         if (e) cudaEventDestroy(e);
-    void *bufs[] = {m->w, m->wdf, m->cen, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
+    void *bufs[] = {m->w, m->wdf, m->cen, m->cenf, m->opA, m->opB, m->dsum, m->dsq, m->msum, m->msq, m->mnorm, m->sref,
                     m->ca, m->cb, m->stats, m->pscore, m->pidx, m->err, m->near, m->scratch_d, m->cta_u};
     for (void *b : bufs) cudaFree(b);
     delete m;

@@ -139,6 +139,14 @@ __device__ __forceinline__ void dot2_add(Dot2 &d, float a, float b)
     d.c = __fadd_rn(d.c, __fadd_rn(e, l));
 }
 
+// d += x (the sum's TwoSum error into c)
+__device__ __forceinline__ void dot2_add1(Dot2 &d, float x)
+{
+    const float s = __fadd_rn(d.s, x), bs = __fsub_rn(s, d.s);
+    d.c = __fadd_rn(d.c, __fadd_rn(__fsub_rn(d.s, __fsub_rn(s, bs)), __fsub_rn(x, bs)));
+    d.s = s;
+}
+
 __device__ __forceinline__ double dot2_value(const Dot2 &d) { return (double)d.s + (double)d.c; }
 
 }  // namespace cmt
