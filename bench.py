@@ -509,7 +509,7 @@ def pair_and_nufft(torch, nf, acm, ws, cfg, dev, N, args):
 def fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_mixed, t_cg_mixed):
     """The same solve in the plain-FP64 GPU form (FP64 NUFFT at eps 1e-12, FP64 vectors and
     FFTs) and in the reference's own precision split (FP32 NUFFT, FP64 CG), each warmed up
-    (plans, sort buffers, cuFFT plans, captured graph) before it is timed by CUDA events;
+    (plans, fine grids, cuFFT plans, captured graph) before it is timed by CUDA events;
     whole-solve and pure CG-iteration times separately.  Errors of the mixed form against
     the FP64 form after 10, 30, 60 and 100 iterations of the same CG, and the sensitivity of
     the FP64 form itself: its 100-iteration result when only its Toeplitz kernel is
@@ -522,7 +522,12 @@ def fp64_form(torch, acm, cfg, ppr_d, rext, slices, quats_d, est, t_mixed, t_cg_
                              / torch.linalg.norm(b.double().reshape(-1)))
 
     def timed(**kwargs):
-        acm.solve_ac(0, ppr_d, rext, slices, M, ac_estimate=est.clone(), maxiter=2, **kw, **kwargs)  # warm-up
+        # warm-up on a few images: the workspace (plans, fine grids, cuFFT plans, the captured
+        # iteration) is per (M, precision, eps), so it is warm for the full call, whose larger
+        # sort buffers come from the stream-ordered pool
+        nw = min(16, slices.shape[0])
+        acm.solve_ac(0, ppr_d, rext, slices[:nw], M, ac_estimate=est.clone(), maxiter=2,
+                     **dict(kw, orientations=quats_d[:nw]), **kwargs)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
