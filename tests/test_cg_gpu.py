@@ -73,18 +73,20 @@ def test_pair_fixed_iterations_match_reference(ac_mod, golden, prec, tol):
     assert rel_l2(x.cpu().numpy(), g["x_cg10"].real) < tol
 
 
-# solve_ac stops at ||r|| < 1e-5 ||d|| (scipy's default rtol) after ~90 iterations here (the
-# generation-0 solve has no support and starts from zero).  Over that many iterations this
-# unpreconditioned CG amplifies any perturbation of its operator or right-hand side a
-# thousandfold and more (at the benchmark's size an FP64 solve whose Toeplitz kernel alone is
-# perturbed by a relative 1e-9 moves by ~3e-5 after 100 iterations), so single-precision CG
-# vectors and FFT convolutions meet 2e-4 here and the reference's own precision split -- FP32
-# NUFFT, FP64 CG (cg_prec=64) -- and the FP64 form meet 1e-4.  At the fixed iteration counts
-# of the configurations the FP32 forms meet 1e-4 (tests above).
-@pytest.mark.parametrize("prec,cg_prec,operator,tol", [
+# solve_ac stops at ||r|| < 1e-5 ||d|| (scipy's default rtol).  The generation-1 solve starts
+# from the masked estimate and every form meets 1e-4 (FP32 vectors: ~7e-6).  The generation-0
+# solve has no support and starts from zero: ~90 iterations, over which this unpreconditioned
+# CG amplifies any perturbation of its operator or right-hand side a thousandfold and more (at
+# the benchmark's size an FP64 solve whose Toeplitz kernel alone is perturbed by a relative
+# 1e-9 moves by ~3e-5 after 100 iterations), so with single-precision CG vectors and FFT
+# convolutions it lands at 9.3e-5 - 1.05e-4 (run to run, with the order of the spreading
+# atomics) and is held to 2e-4, while the reference's own precision split -- FP32 NUFFT, FP64
+# CG (cg_prec=64) -- and the FP64 form meet 1e-4 (1.3e-5 - 2.1e-5).  At the fixed iteration
+# counts of the configurations the FP32 forms meet 1e-4 (tests above).
+@pytest.mark.parametrize("prec,cg_prec,operator,tol0", [
     (64, None, "toeplitz", TOL_AC), (64, None, "pair", TOL_AC), (32, 64, "toeplitz", TOL_AC),
     (32, None, "toeplitz", 2e-4), (32, None, "pair", 2e-4)])
-def test_solve_ac_matches_reference(ac_mod, golden, prec, cg_prec, operator, tol):
+def test_solve_ac_matches_reference(ac_mod, golden, prec, cg_prec, operator, tol0):
     g = golden("autocorrelation")
     M = int(g["M"])
     eps = 1e-6 if prec == 32 else 1e-12
@@ -92,12 +94,12 @@ def test_solve_ac_matches_reference(ac_mod, golden, prec, cg_prec, operator, tol
     ac, info = ac_mod.solve_ac(1, g["ppr"], g["rext"], g["slices"], M, orientations=g["quats"], ac_estimate=est,
                                prec=prec, operator=operator, eps=eps, return_info=True, cg_prec=cg_prec)
     assert ac.dtype == np.float64 and ac.shape == (M,) * 3
-    assert rel_l2(ac, g["ac_solved"]) < tol
+    assert rel_l2(ac, g["ac_solved"]) < TOL_AC
     # the reference masks the estimate in place (autocorrelation.py:220)
     assert np.array_equal(est, g["estimate"] * g["ac_support"])
     ac0 = ac_mod.solve_ac(0, g["ppr"], g["rext"], g["slices"], M, orientations=g["quats"], ac_estimate=None,
                           prec=prec, operator=operator, eps=eps, cg_prec=cg_prec)
-    assert rel_l2(ac0, g["ac_gen0"]) < tol
+    assert rel_l2(ac0, g["ac_gen0"]) < tol0
 
 
 def test_support_matches_ndimage(ac_mod):
