@@ -82,7 +82,9 @@ int cmt_plan_info(const cmt_plan *plan, int *n_fine, int *width, double *beta, i
 
 /* Set nonuniform points from coordinate arrays (device, prec-typed, length N, radians,
  * |x| < 3 pi).  Points are counting-sorted into spatial bins of the fine grid; the plan
- * keeps the sorted coordinates and the permutation.  Replaces plan.set_pts (forward.py:77-79:
+ * keeps the sorted coordinates and the permutation.  The sort's buffers come from the
+ * device's default stream-ordered memory pool on the plan's stream; the library sets that
+ * pool to keep freed memory, so repeated calls reuse it without new mappings.  Replaces plan.set_pts (forward.py:77-79:
  * cufinufft is given (L, K, H) so that H pairs with array axis 0; here x pairs with axis 0). */
 int cmt_set_pts(cmt_plan *plan, int64_t N, const void *x, const void *y, const void *z);
 
@@ -104,6 +106,9 @@ int cmt_execute(cmt_plan *plan, void *c, void *f, const float *support, double s
  * with S the optional support.  f_in / f_out are real M^3 grids of the plan's precision. */
 int cmt_execute_pair(cmt_plan *plan, const void *f_in, void *f_out, const float *support, double scale);
 
+/* Release the plan.  Waits for the device first (cudaDeviceSynchronize): the sorted points
+ * and the sort's buffers are stream-ordered pool allocations, which cudaFree would release
+ * without waiting for launches still reading them. */
 int cmt_plan_destroy(cmt_plan *plan);
 
 /* Per-launch CUDA-event timing of the spread / interpolation kernels (enable 0/1), and
