@@ -269,6 +269,33 @@ def test_table_interp_matches_per_point_kernel(nf, prec, eps, real_out, monkeypa
 
 
 @pytest.mark.parametrize("prec", [32, 64])
+def test_plan_repointed_with_growing_and_shrinking_point_sets(nf, prec):
+    # one plan (and a derived plan on its points) set to 20k, 90k, then 5k points: the sort's
+    # buffers grow from the stream-ordered pool and are reused; every execute matches the
+    # oracle for the points it was given last
+    rng = np.random.default_rng(31)
+    M = 17
+    eps, tol = (1e-6, TOL32) if prec == 32 else (1e-12, TOL64)
+    p = nf.Plan(1, M, eps=eps, isign=1, prec=prec)
+    d = p.derive(1, 2 * M, isign=1)
+    q = nf.Plan(2, M, eps=eps, isign=-1, prec=prec)
+    f = rng.standard_normal((M,) * 3)
+    for N in (20000, 90000, 5000):
+        x, y, z = _pts(rng, N)
+        c = rng.standard_normal(N)
+        pts = [torch.from_numpy(a) for a in (x, y, z)]
+        p.set_pts(*pts)
+        q.set_pts(*pts)
+        assert rel_l2(p.execute(torch.from_numpy(c)).cpu().numpy(), on.type1(x, y, z, c, M, eps=1e-13)) < tol
+        assert rel_l2(d.execute(None, real_out=True).cpu().numpy(),
+                      on.type1(x, y, z, np.ones(N), 2 * M, eps=1e-13).real) < tol
+        assert rel_l2(q.execute(torch.from_numpy(f)).cpu().numpy(), on.type2(x, y, z, f, eps=1e-13, isign=-1)) < tol
+    d.close()
+    p.close()
+    q.close()
+
+
+@pytest.mark.parametrize("prec", [32, 64])
 def test_pair_is_normal_operator(nf, prec):
     rng = np.random.default_rng(11)
     M, N = 15, 30000
