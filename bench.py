@@ -1373,8 +1373,12 @@ def summarize(line):
 def reference_arm(args, cfg, metric, config):
     """--impl reference: W untimed then K timed steps of the reference's CPU path on all host
     threads (ReferenceStep); ms_per_step is the measured time of one sampled step, value the
-    workload's s/CG-iteration from the sample (spreads extrapolated by points)."""
-    ref = ReferenceStep(cfg)
+    workload's s/CG-iteration from the sample (spreads extrapolated by points).  The images
+    spread per step shrink as K + W grows (100 at the default 3 + 3, 24 at 20 + 5), so the
+    whole run stays near two minutes on 16 host cores; the value is a per-point rate and does
+    not depend on the sample's size."""
+    images = max(20, min(100, int(600 / max(1, args.steps + args.warmup))))
+    ref = ReferenceStep(cfg, images=images)
     for _ in range(args.warmup):
         ref.step()
     ref.t_spread, ref.t_pos, ref.t_fixed, ref.t_iter, ref.pts = [], [], [], [], 0
