@@ -16,6 +16,7 @@
 // The reference calls cufinufft/finufft for these transforms
 // (cmtip/nufft/forward.py:40,77-79; cmtip/nufft/adjoint.py:33,73-75).
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdlib>
@@ -253,17 +254,17 @@ __device__ __forceinline__ unsigned lanemask_lt()
 // finer grid, so the kernels can keep a window in registers across runs of such points.
 // Keys per bin: kb = 1 (fine_sort 0: bin only), (bs+1)^(fine_sort - 1) (2..4: x / x, y /
 // x, y, z window origin) or (bs+1)^3 * 8 (1: origin and refinement).
-template <typename T>
-__device__ __forceinline__ int64_t point_key(int b, T rx, T ry, T rz, int w, int bs, int fine_sort)
+template <typename T, typename K = int64_t>
+__device__ __forceinline__ K point_key(int b, T rx, T ry, T rz, int w, int bs, int fine_sort)
 {
     if (!fine_sort) return b;
     const T hw = T(0.5) * T(w);
     const int h = w / 2, O = bs + 1;
     int lx = (int)ceil(rx - hw), ly = (int)ceil(ry - hw), lz = (int)ceil(rz - hw);
     int ox = min(max(lx + h, 0), bs), oy = min(max(ly + h, 0), bs), oz = min(max(lz + h, 0), bs);
-    if (fine_sort == 2) return ((int64_t)b * O + ox);                            // origin x
-    if (fine_sort == 3) return ((int64_t)b * O + ox) * O + oy;                   // origin x, y
-    if (fine_sort == 4) return (((int64_t)b * O + ox) * O + oy) * O + oz;        // origin
+    if (fine_sort == 2) return ((K)b * O + ox);                     // origin x
+    if (fine_sort == 3) return ((K)b * O + ox) * O + oy;            // origin x, y
+    if (fine_sort == 4) return (((K)b * O + ox) * O + oy) * O + oz; // origin
     // On the twice finer grid the origin is 2l + base + d with d in {0, 1} (even w) or
     // {0, 1, 2} (odd w); the refinement splits d = 2 off, so within one refined group the fine
     // origins differ by at most one per dimension.
@@ -274,7 +275,7 @@ __device__ __forceinline__ int64_t point_key(int b, T rx, T ry, T rz, int w, int
     dx = min(max(dx, 0), 2) >> 1;
     dy = min(max(dy, 0), 2) >> 1;
     dz = min(max(dz, 0), 2) >> 1;
-    return ((((int64_t)b * O + ox) * O + oy) * O + oz) * 8 + dx * 4 + dy * 2 + dz;
+    return ((((K)b * O + ox) * O + oy) * O + oz) * 8 + dx * 4 + dy * 2 + dz;
 }
 
 struct SortGeom {
@@ -315,9 +316,12 @@ __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T
 {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t base = (int64_t)blockIdx.x * blockDim.x;
+    // FP32 plans keep 32-bit keys (their records hold an int key; set_pts_impl bounds the key
+    // count below 2^27 when origins are keyed): 32-bit key arithmetic and warp match
+    using K = typename std::conditional<sizeof(T) == 4, int, long long>::type;
     for (; base < N; base += stride) {
         int64_t j = base + threadIdx.x;
-        long long key = -1;
+        K key = -1;
         if (j < N) {
             T px, py, pz, rx = 0, ry = 0, rz = 0;
             bool bad;
@@ -326,7 +330,7 @@ __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T
                 atomicOr(flag, 1);
             } else {
                 int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.bs, sg.bs_magic, sg.nb, rx, ry, rz);
-                key = point_key<T>(b, rx, ry, rz, sg.w, sg.bs, sg.fine_sort);
+                key = point_key<T, K>(b, rx, ry, rz, sg.w, sg.bs, sg.fine_sort);
             }
             PtRec<T> r;
             r.key = key;
