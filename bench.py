@@ -1367,6 +1367,15 @@ def summarize(line):
            "tikhonov_s": g(ex, "tikhonov", "solve_s"), "tikhonov_rel_l2_vs_fp64": g(ex, "tikhonov", "rel_l2_mixed_vs_fp64"),
            "cpu_baseline_s_per_cg_iteration": g(line, "cpu_baseline", "value"),
            "cpu_baseline_single_thread": g(line, "cpu_baseline", "single_thread", "value")}
+    # The metric's "<=1e-5 err" is the NUFFT bound at eps 1e-6; the solved autocorrelation's
+    # bound is 1e-4 after fixed iterations.  Each measured error beside its bound, met or not.
+    bound = lambda v, lim: None if v is None else {"value": v, "bound": lim, "met": bool(v <= lim)}
+    ac = ex.get("ac_rel_l2_mixed_vs_fp64_by_iterations") or {}
+    bounds = {"nufft_type1": bound(out["type1_rel_l2_vs_fp64"], 1e-5),
+              "nufft_type2": bound(out["type2_rel_l2_vs_fp64"], 1e-5),
+              "ac_mixed_10it": bound(ac.get("10"), 1e-4), "ac_mixed_100it": bound(ac.get("100"), 1e-4),
+              "ac_fp32_nufft_fp64_cg_100it": bound(g(ex, "fp32_nufft_fp64_cg", "ac_rel_l2_vs_fp64_100it"), 1e-4)}
+    out["error_bounds"] = {k: v for k, v in bounds.items() if v is not None} or None
     return {k: v for k, v in out.items() if v is not None}
 
 
