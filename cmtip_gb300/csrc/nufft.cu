@@ -107,7 +107,7 @@ namespace cmt {
 
 // Split u (fine-grid units, any real) into the integer cell and the fraction.
 template <typename T>
-__device__ __forceinline__ void cell_and_frac(T x, T s_hi, T s_lo, int n, int &cell, T &frac)
+__device__ __forceinline__ void cell_and_frac(T x, T s_hi, T s_lo, int n, unsigned n_magic, int &cell, T &frac)
 {
     // u = x * (s_hi + s_lo) carried as p + lo with p = fl(x s_hi) and lo its exact error
     T p = x * s_hi;
@@ -115,16 +115,24 @@ __device__ __forceinline__ void cell_and_frac(T x, T s_hi, T s_lo, int n, int &c
     lo = fma(x, s_lo, lo);
     T fp = floor(p);
     T f = (p - fp) + lo;
-    int c = (int)fp;
-    if (f >= T(1)) { f -= T(1); c += 1; }
-    if (f < T(0)) { f += T(1); c -= 1; }
-    // c mod n, branch-free: k_bin_count calls this only for |x| < 3 pi, where c lies in
-    // [-1.5 n - 2, 1.5 n + 1], inside the [-2n, 3n) that two corrections each way cover
-    // (n >= 2w >= 4)
-    c += n & -(int)(c < 0);
-    c += n & -(int)(c < 0);
-    c -= n & -(int)(c >= n);
-    c -= n & -(int)(c >= n);
+    // p - fp is in [0, 1] (1 where it rounds up, for p just below an integer) and |lo| is
+    // about an ulp of p, so f lies in (-1, 2) and t = floor(f) is -1, 0 or 1: f - t is
+    // f + 1 / f / f - 1, one fix-up either way (f is never -0: p - fp is +0 or positive)
+    const T t = floor(f);
+    f -= t;
+    int c = (int)fp + (int)t;
+    // c mod n: k_bin_count calls this only for |x| < 3 pi, where c lies in [-1.5 n - 2,
+    // 1.5 n + 1], inside [-2n, 3n) (n >= 2w >= 4); u = c + 2n is in [0, 5n), below 2^32 / n
+    // when n_magic is set, so u / n is the multiply-high quotient (div_magic)
+    if (n_magic) {
+        const unsigned u = (unsigned)(c + 2 * n);
+        c = (int)(u - __umulhi(u, n_magic) * (unsigned)n);
+    } else {
+        c += n & -(int)(c < 0);
+        c += n & -(int)(c < 0);
+        c -= n & -(int)(c >= n);
+        c -= n & -(int)(c >= n);
+    }
     cell = c;
     frac = f;
 }
@@ -146,7 +154,9 @@ struct QuatSrc {
     const double *ppr;
     int64_t n_pix;
     double rext;
-    const float2 *rot_df;  // FP32 plans: inv_rot and ppr split into double-float pairs
+    // FP32 plans: inv_rot and ppr split into double-float pairs and padded for 16-byte loads
+    // (k_split_quat): 10 pairs per image (inv(R) row-major, one pad), 4 per pixel (x, y, z, pad)
+    const float2 *rot_df;
     const float2 *ppr_df;
     float2 scale_df;       // pi / rext as a double-float pair
     unsigned long long npix_magic;  // ceil(2^64 / n_pix) (n_pix >= 2), else 0
@@ -160,13 +170,27 @@ __device__ __forceinline__ void img_pix(int64_t j, const QuatSrc &q, unsigned &i
     pix = (unsigned)j - img * (unsigned)q.n_pix;
 }
 
-__global__ void k_split_df(const double *in, int64_t n, float2 *out)
+__device__ __forceinline__ float2 split_df(double v)
 {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double v = in[i];
-    float h = __double2float_rn(v);
-    out[i] = make_float2(h, __double2float_rn(v - (double)h));
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+}
+
+// The rotations (n_img x 9, row-major inv(R)) and q-vectors (3 x n_pix, component-major) as
+// double-float pairs in QuatSrc's padded layout; one thread per output pair
+__global__ void k_split_quat(const double *rot, int64_t n_img, const double *ppr, int64_t n_pix, float2 *rot_out,
+                             float2 *ppr_out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 10 * n_img) {
+        const int64_t img = i / 10;
+        const int k = (int)(i - 10 * img);
+        rot_out[i] = k < 9 ? split_df(rot[9 * img + k]) : make_float2(0.f, 0.f);
+    } else if (i < 10 * n_img + 4 * n_pix) {
+        const int64_t t = i - 10 * n_img, pix = t / 4;
+        const int c = (int)(t - 4 * pix);
+        ppr_out[t] = c < 3 ? split_df(ppr[c * n_pix + pix]) : make_float2(0.f, 0.f);
+    }
 }
 
 template <typename T>
@@ -186,8 +210,13 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
         // N < 2^31 (set_pts_impl), so 32-bit index arithmetic
         unsigned img, pix;
         img_pix(j, q, img, pix);
-        const float2 *R = q.rot_df + 9 * img;
-        const float2 a0 = q.ppr_df[pix], a1 = q.ppr_df[q.n_pix + pix], a2 = q.ppr_df[2 * q.n_pix + pix];
+        const float4 *R4 = reinterpret_cast<const float4 *>(q.rot_df) + 5 * img;
+        const float4 *P4 = reinterpret_cast<const float4 *>(q.ppr_df) + 2 * pix;
+        const float4 r0 = R4[0], r1 = R4[1], r2 = R4[2], r3 = R4[3], r4 = R4[4], pa = P4[0], pb = P4[1];
+        const float2 R[9] = {make_float2(r0.x, r0.y), make_float2(r0.z, r0.w), make_float2(r1.x, r1.y),
+                             make_float2(r1.z, r1.w), make_float2(r2.x, r2.y), make_float2(r2.z, r2.w),
+                             make_float2(r3.x, r3.y), make_float2(r3.z, r3.w), make_float2(r4.x, r4.y)};
+        const float2 a0 = make_float2(pa.x, pa.y), a1 = make_float2(pa.z, pa.w), a2 = make_float2(pb.x, pb.y);
         float o[3];
 #pragma unroll
         for (int r = 0; r < 3; ++r)
@@ -219,14 +248,14 @@ __device__ __forceinline__ void point_coords(int mode, int64_t j, const T *x, co
 }
 
 template <typename T>
-__device__ __forceinline__ int bin_of(T px, T py, T pz, T s_hi, T s_lo, int n, int bs, unsigned bs_magic, int nb,
-                                      T &rx, T &ry, T &rz)
+__device__ __forceinline__ int bin_of(T px, T py, T pz, T s_hi, T s_lo, int n, unsigned n_magic, int bs,
+                                      unsigned bs_magic, int nb, T &rx, T &ry, T &rz)
 {
     int cx, cy, cz;
     T fx, fy, fz;
-    cell_and_frac(px, s_hi, s_lo, n, cx, fx);
-    cell_and_frac(py, s_hi, s_lo, n, cy, fy);
-    cell_and_frac(pz, s_hi, s_lo, n, cz, fz);
+    cell_and_frac(px, s_hi, s_lo, n, n_magic, cx, fx);
+    cell_and_frac(py, s_hi, s_lo, n, n_magic, cy, fy);
+    cell_and_frac(pz, s_hi, s_lo, n, n_magic, cz, fz);
     int bx, by, bz;
     if (bs_magic) {
         bx = (int)div_magic((unsigned)cx, bs_magic);
@@ -281,6 +310,7 @@ __device__ __forceinline__ K point_key(int b, T rx, T ry, T rz, int w, int bs, i
 struct SortGeom {
     int n, bs, nb, w, fine_sort;
     unsigned bs_magic;  // ceil(2^32 / bs) for cells below 2^32 / bs, else 0 (plain division)
+    unsigned n_magic;   // ceil(2^32 / n) when 5 n^2 < 2^32 (cell wrap by multiply-high), else 0
 };
 
 // A point between the two counting passes: its sort key (-1: out of range) and its
@@ -329,7 +359,7 @@ __global__ void k_bin_count(int mode, int64_t N, const T *x, const T *y, const T
             if (bad) {
                 atomicOr(flag, 1);
             } else {
-                int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.bs, sg.bs_magic, sg.nb, rx, ry, rz);
+                int b = bin_of<T>(px, py, pz, s_hi, s_lo, sg.n, sg.n_magic, sg.bs, sg.bs_magic, sg.nb, rx, ry, rz);
                 key = point_key<T, K>(b, rx, ry, rz, sg.w, sg.bs, sg.fine_sort);
             }
             PtRec<T> r;
@@ -1231,7 +1261,8 @@ static int set_pts_impl(Plan &p, int mode, int64_t N, const T *x, const T *y, co
     T s_hi = (T)s, s_lo = (T)(s - (double)s_hi);
     // cells are below n <= 2^20, so the multiply-high division is exact for bs <= 4096
     SortGeom sgeo{p.n, p.bs, p.nb, p.w, fine_sort,
-                  p.bs >= 2 && (uint64_t)p.n * p.bs < (1ULL << 32) ? magic32((unsigned)p.bs) : 0u};
+                  p.bs >= 2 && (uint64_t)p.n * p.bs < (1ULL << 32) ? magic32((unsigned)p.bs) : 0u,
+                  p.n >= 2 && 5ULL * p.n * p.n < (1ULL << 32) ? magic32((unsigned)p.n) : 0u};
     int g = grid_for(N);
     // pass 1: counts per key (into key_next), then key_start = exclusive scan (with the total
     // at key_start[nkeys])
@@ -1745,15 +1776,20 @@ extern "C" int cmt_set_pts_quat(cmt_plan *p, int64_t n_img, const double *inv_ro
     int64_t N = n_img * n_pix;
     if (p->prec == 64) return set_pts_impl<double>(*p, 1, N, nullptr, nullptr, nullptr, q);
     // FP32 plans evaluate the float64 coordinate chain in double-float arithmetic
-    float2 *split = nullptr;
-    int64_t ns = 9 * n_img + 3 * n_pix;
+    float2 *split = nullptr;  // pool blocks start 256-byte aligned; 80 n_img bytes keep ppr_df 16-byte aligned
+    int64_t ns = 10 * n_img + 4 * n_pix;
     CMT_TRY_CUDA(cudaMallocAsync(&split, sizeof(float2) * ns, p->stream));
-    k_split_df<<<ceil_div(9 * n_img, 256), 256, 0, p->stream>>>(inv_rot, 9 * n_img, split);
-    k_split_df<<<ceil_div(3 * n_pix, 256), 256, 0, p->stream>>>(ppr, 3 * n_pix, split + 9 * n_img);
+    k_split_quat<<<(unsigned)ceil_div(ns, 256), 256, 0, p->stream>>>(inv_rot, n_img, ppr, n_pix, split,
+                                                                     split + 10 * n_img);
+    if (cudaError_t e = cudaGetLastError()) {
+        cudaFreeAsync(split, p->stream);
+        set_error("%s:%d k_split_quat launch: %s", __FILE__, __LINE__, cudaGetErrorString(e));
+        return CMT_ERR_CUDA;
+    }
     double s = kPi / rext;
     float sh = (float)s;
     q.rot_df = split;
-    q.ppr_df = split + 9 * n_img;
+    q.ppr_df = split + 10 * n_img;
     q.scale_df = make_float2(sh, (float)(s - (double)sh));
     int rc = set_pts_impl<float>(*p, 1, N, nullptr, nullptr, nullptr, q);
     cudaFreeAsync(split, p->stream);
