@@ -446,9 +446,10 @@ def gpu_arm(args):
         h2d = slices_h.numel() * 4 + quats_h.numel() * 4 + ppr_h.numel() * 8 + est_h.numel() * 4
         out["e2e"] = {"value": t_e2e / maxiter, "unit": "s/CG-iteration", "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(res.numel() * 8)}
-        # this library's kernel launches per step, by the launch list of one step (531): the
-        # point sort, both spreads with their crops, rotations, support filter, Toeplitz-kernel
-        # scale and mask and the CG start (31 together), and 5 graph kernels per CG iteration
+        # this library's kernel launches per step (531; a launch list of one step counted 532
+        # while two launches split the rotation and q-vector tables, one since): the point
+        # sort, both spreads with their crops, rotations, support filter, Toeplitz-kernel scale
+        # and mask and the CG start (31 together), and 5 graph kernels per CG iteration
         out["gpu_launches"] = args.steps * (2 * 6 + 1 + 4 + 2 + 12 + 5 * maxiter)
     if dist is not None:
         dist.destroy_process_group()
