@@ -48,3 +48,20 @@ def test_max_over_ranks_single_process():
     sys.path.insert(0, REPO)
     import bench
     assert bench.max_over_ranks(3.25) == 3.25
+
+
+def test_summary_states_each_error_against_its_bound():
+    # the line's summary repeats every measured error beside its bound (NUFFT 1e-5 at eps 1e-6,
+    # solved autocorrelation 1e-4) and says whether it was met
+    sys.path.insert(0, REPO)
+    import bench
+    line = {"value": 1.36e-3, "extras": {
+        "nufft_parity": {"type1_rel_l2_vs_fp64_plan": 2.0e-6, "type2_rel_l2_vs_fp64_oracle": 3.2e-6},
+        "ac_rel_l2_mixed_vs_fp64_by_iterations": {"10": 4.3e-6, "100": 1.36e-4},
+        "fp32_nufft_fp64_cg": {"ac_rel_l2_vs_fp64_100it": 1.08e-4}}}
+    b = bench.summarize(line)["error_bounds"]
+    assert b["nufft_type1"] == {"value": 2.0e-6, "bound": 1e-5, "met": True}
+    assert b["nufft_type2"]["met"] and b["ac_mixed_10it"]["met"]
+    assert not b["ac_mixed_100it"]["met"] and not b["ac_fp32_nufft_fp64_cg_100it"]["met"]
+    # a line without those legs carries no bounds block
+    assert "error_bounds" not in bench.summarize({"value": 1.0})
