@@ -84,8 +84,9 @@ int cmt_plan_info(const cmt_plan *plan, int *n_fine, int *width, double *beta, i
  * |x| < 3 pi).  Points are counting-sorted into spatial bins of the fine grid; the plan
  * keeps the sorted coordinates and the permutation.  The sort's buffers come from the
  * device's default stream-ordered memory pool on the plan's stream; the library sets that
- * pool to keep freed memory, so repeated calls reuse it without new mappings.  Replaces plan.set_pts (forward.py:77-79:
- * cufinufft is given (L, K, H) so that H pairs with array axis 0; here x pairs with axis 0). */
+ * pool to keep freed memory, so repeated calls reuse it without new mappings.  Replaces
+ * plan.set_pts (forward.py:77-79: cufinufft is given (L, K, H) so that H pairs with array
+ * axis 0; here x pairs with axis 0). */
 int cmt_set_pts(cmt_plan *plan, int64_t N, const void *x, const void *y, const void *z);
 
 /* Set points from per-image inverse rotation matrices (device, n_img x 3 x 3 float64) and
