@@ -407,9 +407,11 @@ __device__ __forceinline__ void spread_tab_sub(int b, int off, const int *bin_co
     const int e = lane % EW, bl = lane / EW;
 
     // FP32 real strengths: the window's columns in pairs, updated with the packed FP32 FMA
-    // (fma.rn.f32x2: two independent round-to-nearest FMAs per instruction, so the sums are
-    // those of scalar FMAs with fewer instructions issued); an odd width's last column keeps
-    // scalar FMAs (acc[r][NX - 1]).
+    // (fma.rn.f32x2: two independent round-to-nearest FMAs per instruction, fewer
+    // instructions issued; the sums are held to the same tolerance as scalar ones, with no
+    // claim of equal bits: a compensated sequence written with these builtins differed from
+    // its scalar form on sm_103a); an odd width's last column keeps scalar FMAs
+    // (acc[r][NX - 1]).
     constexpr bool PK = sizeof(T) == 4 && !CPLX;
     constexpr int NP = NX / 2;
     T acc[RX][NX], aci[RX][NX];
