@@ -336,11 +336,7 @@ constexpr int TC_BN = 256;   // default references per tile (TMEM columns per ac
 constexpr int TC_BK = 64;    // K per stage: one 128-byte swizzle row of bf16
 constexpr int TC_STAGES = 4;  // default TMA ring depth
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
-constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
-constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 constexpr int TC_THREADS = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-5 epilogue
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
-
 // shared memory of a (BN, STAGES) instantiation: the TMA ring, 1 KB alignment, barriers
 constexpr int tc_smem(int bn, int stages) { return stages * (TC_A_BYTES + bn * TC_BK * 2) + 1024 + 256; }
 

@@ -120,20 +120,22 @@ __global__ void __launch_bounds__(256) k_spread(const int *sub_bin, const int *s
     T acc[L::RMAX][L::KMAX], aci[L::RMAX][L::KMAX];
     int cur_key = -1, cur_base = 0;
     auto flush = [&]() {
-        if (W == 0 || cur_key < 0) return;
+        if constexpr (W > 0) {
+            if (cur_key < 0) return;
 #pragma unroll
-        for (int r = 0; r < L::RMAX; ++r) {
-            const int bb = bl + r * L::BR;
-            const bool ok = ez && bb < w;
+            for (int r = 0; r < L::RMAX; ++r) {
+                const int bb = bl + r * L::BR;
+                const bool ok = ez && bb < w;
 #pragma unroll
-            for (int a = 0; a < L::KMAX; ++a) {
-                if (ok) {
-                    const int idx = cur_base + bb * P + a * plane;
-                    add(idx, acc[r][a]);
-                    if (CPLX) add(copy + idx, aci[r][a]);
+                for (int a = 0; a < L::KMAX; ++a) {
+                    if (ok) {
+                        const int idx = cur_base + bb * P + a * plane;
+                        add(idx, acc[r][a]);
+                        if (CPLX) add(copy + idx, aci[r][a]);
+                    }
+                    acc[r][a] = T(0);
+                    aci[r][a] = T(0);
                 }
-                acc[r][a] = T(0);
-                aci[r][a] = T(0);
             }
         }
     };
@@ -1020,20 +1022,22 @@ __global__ void __launch_bounds__(256) k_pair(const int *sub_bin, const int *sub
     Window<T, true, W> win, acc;
     int cur_key = -1, cur_base = 0;
     auto flush = [&]() {
-        if (W == 0 || cur_key < 0) return;
+        if constexpr (W > 0) {
+            if (cur_key < 0) return;
 #pragma unroll
-        for (int r = 0; r < L::RMAX; ++r) {
-            const int bb = bl + r * L::BR;
-            const bool ok = ez && bb < w;
+            for (int r = 0; r < L::RMAX; ++r) {
+                const int bb = bl + r * L::BR;
+                const bool ok = ez && bb < w;
 #pragma unroll
-            for (int a = 0; a < L::KMAX; ++a) {
-                if (ok) {
-                    const int idx = cur_base + bb * P + a * plane;
-                    atomicAdd(&sb[idx], acc.re[r][a]);
-                    atomicAdd(&sb[copy + idx], acc.im[r][a]);
+                for (int a = 0; a < L::KMAX; ++a) {
+                    if (ok) {
+                        const int idx = cur_base + bb * P + a * plane;
+                        atomicAdd(&sb[idx], acc.re[r][a]);
+                        atomicAdd(&sb[copy + idx], acc.im[r][a]);
+                    }
+                    acc.re[r][a] = T(0);
+                    acc.im[r][a] = T(0);
                 }
-                acc.re[r][a] = T(0);
-                acc.im[r][a] = T(0);
             }
         }
     };
