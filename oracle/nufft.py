@@ -1,7 +1,7 @@
 """ORACLE (test infrastructure only): FP64 CPU 3D NUFFT and direct NUDFT.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may
-import this module.  It is the checker, never the product path.
+import this module.  It checks results and is never on the product path.
 
 The reference (cmtip) calls the third-party ``finufft`` library at
 ``cmtip/nufft/forward.py:40`` (``nufft3d2(H_, K_, L_, ugrid, out=, eps=1e-12,
