@@ -1201,7 +1201,31 @@ def kernel_cases(size="small"):
     align:  the orientation-matching size only: 5000 images x 16384 pixels against 20000
             references (BF16 operands, one tcgen05 distance launch and its re-scoring;
             about 2.5 GB on the device).
+    cg:     a CG solver at M = 81 on its own (random Toeplitz kernel, support and right-hand
+            side), its iteration graph-replayed: 3 warm-up iterations, then three timed solves
+            of 100 iterations each; prints the time per iteration (CUDA events).
     """
+    if size == "cg":
+        import torch
+        import cmtip_gb300.autocorrelation as acm
+        M, n = CFG["M"], 100
+        g = torch.Generator(device="cuda").manual_seed(0)
+        s = acm.CGSolver(M, prec=32)
+        s.set_kernel(torch.rand((2 * M,) * 3, device="cuda", generator=g))
+        s.set_operator((torch.rand(M ** 3, device="cuda", generator=g) > 0.3).float(), 1.0, 1e-3, 1e3)
+        d = torch.randn(M ** 3, device="cuda", dtype=torch.float64, generator=g)
+        x0 = torch.zeros(M ** 3, device="cuda", dtype=torch.float64)
+        s.solve(d, x0, maxiter=3, rtol=0.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        us = []
+        for _ in range(3):
+            e0.record()
+            s.solve(d, x0, maxiter=n, rtol=0.0)
+            e1.record()
+            torch.cuda.synchronize()
+            us.append(round(e0.elapsed_time(e1) / n * 1e3, 2))
+        print(f"kernel case cg (M = {M}): {us} us per iteration", flush=True)
+        return
     if size == "align":
         import torch
         import cmtip_gb300.alignment as alm
@@ -1287,7 +1311,7 @@ def _run():
     ap.add_argument("--tikhonov", action="store_true", help="run only the weighted Tikhonov solve leg and exit")
     ap.add_argument("--phase", action="store_true", help="run only the phasing leg and exit")
     ap.add_argument("--loop", action="store_true", help="run only the MTIP loop / lambda scan leg and exit")
-    ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full", "align"],
+    ap.add_argument("--kernels", nargs="?", const="small", choices=["small", "medium", "full", "align", "cg"],
                     help="run one case of each hot kernel (for ncu captures) and exit")
     args = ap.parse_args()
     if args.kernels:
