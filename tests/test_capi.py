@@ -86,3 +86,19 @@ def test_python_binding_maps_status_codes():
         _lib.call("cmt_plan_create", 3, 21, 32, 1e-6, 1, 0.0, None, ctypes.byref(ctypes.c_void_p()))
     with pytest.raises(ValueError, match="null"):
         _lib.call("cmt_phase_er", None, None, None, None, None, float("inf"), 1)
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    # no fallback: without the built library the package's first call raises ImportError
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from cmtip_gb300 import _lib\n"
+            "try:\n"
+            "    _lib.load(%r)\n"
+            "except ImportError as e:\n"
+            "    print('ImportError:', e)\n"
+            "else:\n"
+            "    print('loaded')\n") % (REPO, str(tmp_path / "absent.so"))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120).stdout
+    assert out.startswith("ImportError:") and "no non-CUDA implementation" in out
