@@ -102,3 +102,28 @@ def test_missing_library_fails_loudly(tmp_path):
             "    print('loaded')\n") % (REPO, str(tmp_path / "absent.so"))
     out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120).stdout
     assert out.startswith("ImportError:") and "no non-CUDA implementation" in out
+
+
+def test_every_entry_point_rejects_null_arguments():
+    # every function, called with null pointers and zero sizes, returns CMT_ERR_ARG before any
+    # CUDA call (destroy functions accept null, like free); run in a child so that a missing
+    # check would show as a crash of that child only
+    import subprocess
+    import sys
+    code = ("import ctypes, sys; sys.path.insert(0, %r)\n"
+            "from cmtip_gb300 import _lib\n"
+            "lib = _lib.load()\n"
+            "ints = (ctypes.c_int, ctypes.c_int64, ctypes.c_long, ctypes.c_uint, ctypes.c_size_t)\n"
+            "for name, args in sorted(_lib.SIGNATURES.items()):\n"
+            "    if name in ('cmt_version', 'cmt_last_error'):\n"
+            "        continue\n"
+            "    vals = [0.0 if a in (ctypes.c_double, ctypes.c_float) else 0 if a in ints else None\n"
+            "            for a in args]\n"
+            "    print(name, getattr(lib, name)(*vals), flush=True)\n") % REPO
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = dict(line.split() for line in r.stdout.splitlines())
+    from cmtip_gb300 import _lib
+    assert len(got) == len(_lib.SIGNATURES) - 2
+    for name, rc in got.items():
+        assert rc == ("0" if name.endswith("_destroy") else "1"), (name, rc)
